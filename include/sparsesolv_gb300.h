@@ -1,0 +1,175 @@
+/*
+ * sparsesolv_gb300.h -- C ABI of the GB300 (sm_103a) Krylov hot path.
+ *
+ * This is the boundary the reference's C++ classes and its Python module bind
+ * to. Every entry point takes plain pointers and sizes; matrices are CSR with
+ * 32-bit indices (slv_int is int in the reference,
+ * include/SparseSolv/SparseTypeDefine.hpp:41) and double or interleaved
+ * complex-double values (dcomplex = std::complex<double>,
+ * include/SparseSolv/BasicDefinesC.hpp:10, which has the same layout).
+ *
+ * What each entry point replaces in the reference (paths inside SparseSolv):
+ *   ssg_create / ssg_destroy     construction of MatSolverICCG / MatSolverMRTR
+ *                                (include/SparseSolv/MatSolverICCG.hpp:56-57,
+ *                                MatSolverMRTR.hpp:71-72); a handle owns one
+ *                                CUDA stream and all device state
+ *   ssg_set_options              the setters of MatSolverBase
+ *                                (include/SparseSolv/MatSolverBase.hpp:128-137),
+ *                                setAccelFactor (MatSolverICCG.hpp:59,
+ *                                MatSolverMRTR.hpp:74), setPreconditionType
+ *                                (MatSolverMRTR.hpp:75)
+ *   ssg_set_matrix[_device]      the SparseMat argument of solve(); CSR taken
+ *                                from SparseMatTMPL::getCols/getColPtr/
+ *                                getValuePtr (include/SparseSolv/SparseMat.hpp:80-85)
+ *   ssg_solve                    MatSolverICCG::solve / MatSolverMRTR::solve,
+ *                                pointer overloads with and without normB
+ *                                (MatSolverBase.hpp:142-150,
+ *                                src/MatSolverICCG.cpp:44-124, :348-424,
+ *                                src/MatSolverMRTR_ICver.cpp:44-128, :393-476)
+ *   ssg_solve_device             the same solve on device-resident b and x
+ *   ssg_get_residual_log         MatSolverBase::getResidualLog
+ *                                (src/MatSolverBase.cpp:55-64)
+ *   ssg_get_iters                (new) iteration count of the last solve
+ *   ssg_factor, ssg_apply_precond, ssg_spmv, ssg_level_schedule
+ *                                (new) the hot-path pieces on their own, for
+ *                                parity tests and benchmarks:
+ *                                SprsPreconditioner::IC_decomp
+ *                                (src/SprsPreconditioner.cpp:133-142),
+ *                                MatSolverBase::IC_frbc_process
+ *                                (src/MatSolverBase.cpp:177-231), Eigen's
+ *                                sparse*dense product, and the level schedule
+ *                                the GPU sweeps run over
+ *   ssg_last_error               (new) message of the last failing call
+ *
+ * Error behaviour. The reference returns false from solve() when it does not
+ * converge, prints "not Convergence!!!", and calls exit(1) when a row of the
+ * lower triangle lacks its diagonal (src/SprsPreconditioner.cpp:91-94). Here
+ * solve returns SSG_NOT_CONVERGED in the first case and SSG_ERR_NO_DIAGONAL
+ * in the second; nothing exits the process. Every device-side wait is bounded
+ * and reports SSG_ERR_TIMEOUT instead of hanging.
+ *
+ * Threading: a handle is not thread-safe (as the reference's solver objects
+ * are not); distinct handles may be used from distinct threads.
+ */
+#ifndef SPARSESOLV_GB300_H
+#define SPARSESOLV_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ssg_handle_s *ssg_handle;
+
+/* return codes */
+#define SSG_OK 0
+#define SSG_NOT_CONVERGED 1
+#define SSG_ERR_ARG (-1)
+#define SSG_ERR_CUDA (-2)
+#define SSG_ERR_NO_DIAGONAL (-3)
+#define SSG_ERR_TIMEOUT (-4)
+#define SSG_ERR_NOMEM (-5)
+#define SSG_ERR_STATE (-6)
+
+/* solver methods */
+#define SSG_METHOD_ICCG 0 /* MatSolverICCG: shifted ICCG (real) / ICCOCG (complex) */
+#define SSG_METHOD_MRTR 1 /* MatSolverMRTR: precondition_type 0 = IC, 1 = Eisenstat SGS */
+
+/* value types */
+#define SSG_REAL 0    /* double */
+#define SSG_COMPLEX 1 /* interleaved (re, im) doubles, unconjugated bilinear products */
+
+/* precision modes (build addition; does not change the method) */
+#define SSG_PREC_FP64 0  /* everything in FP64, as the reference */
+#define SSG_PREC_MIXED 1 /* FP32 factor, SpMV and sweeps inside an inner loop,
+                            FP64 outer residual and iterative refinement */
+
+/*
+ * Settings with the reference's defaults (src/MatSolverBase.cpp:32-47,
+ * include/SparseSolv/MatSolverICCG.hpp:40, MatSolverMRTR.hpp:40-43).
+ * Fill with ssg_default_options().
+ */
+typedef struct {
+    int is_init;              /* 1: start from x = 0 (setInitSolution) */
+    int is_diag_scale;        /* setDiagScale */
+    int is_save_best;         /* setSaveBest */
+    int is_save_residual_log; /* setSaveLog */
+    int diverge_judge_type;   /* setDirvegeType: 0 none, 1 bad-count judge */
+    double bad_div_val;       /* setBadDivVal */
+    int bad_div_count_thres;  /* setBadDivCount */
+    int conv_normalize_type;  /* setConvNormalizeType: 0 |b|, 1 |r0|, 2 const */
+    double conv_normalize_const; /* setConvNormalizeConst */
+    double accel_factor;      /* setAccelFactor (alpha < 0: automatic search) */
+    int precondition_type;    /* setPreconditionType (MRTR): 0 IC, 1 SGS */
+    int precision;            /* SSG_PREC_* */
+    int mrtr_reference_quirks;/* 1: reproduce the reference's IC-MRTR p update and
+                                 MRTR warm start (default 0: corrected) */
+} ssg_options;
+
+void ssg_default_options(ssg_options *o);
+
+int ssg_create(ssg_handle *h, int device);
+int ssg_destroy(ssg_handle h);
+const char *ssg_last_error(ssg_handle h);
+int ssg_set_options(ssg_handle h, const ssg_options *o);
+
+/* CSR from host memory; values are double[nnz] or (re,im) double[2*nnz] */
+int ssg_set_matrix(ssg_handle h, int n, int nnz, const int32_t *row_ptr, const int32_t *col,
+                   const double *val, int value_type);
+/* CSR already in device memory (copied device to device) */
+int ssg_set_matrix_device(ssg_handle h, int n, int nnz, const int32_t *d_row_ptr, const int32_t *d_col,
+                          const double *d_val, int value_type);
+
+/*
+ * One solve() call. b and x are host arrays of n values (x is in/out: the
+ * initial guess when is_init = 0, the solution on return). normB < 0 makes
+ * the solver compute |b| itself (the overloads without normB). Returns
+ * SSG_OK (converged), SSG_NOT_CONVERGED, or an error code.
+ */
+int ssg_solve(ssg_handle h, int method, double conv_cri, int max_ite, double normB, const double *b, double *x);
+int ssg_solve_device(ssg_handle h, int method, double conv_cri, int max_ite, double normB, const double *d_b,
+                     double *d_x);
+
+/* new values for the current pattern (same n, nnz, row_ptr, col); invalidates the factor */
+int ssg_update_values(ssg_handle h, const double *val);
+int ssg_update_values_device(ssg_handle h, const double *d_val);
+
+int ssg_get_residual_log(ssg_handle h, double *log, int cap, int *len);
+int ssg_get_iters(ssg_handle h, int *iters);
+/* accel factor actually used by the last factorisation (after an automatic search) */
+int ssg_get_accel_used(ssg_handle h, double *alpha);
+/* time of the phases of the last solve, milliseconds: [0] setup+factor, [1] iterations */
+int ssg_get_timings(ssg_handle h, double *ms, int cap);
+
+/* ---- measurement (new) ---- */
+/* the CUDA stream all work of the handle runs on (a cudaStream_t) */
+int ssg_get_stream(ssg_handle h, void **stream);
+/* per-kernel-class CUDA-event timing of the following solves (0 off, 1 on) */
+int ssg_set_profiling(ssg_handle h, int enable);
+/* classes: 0 forward sweep, 1 backward sweep, 2 SpMV, 3 fused vector/reduction
+ * kernels, 4 IC factor, 5 level schedule; per class the summed device time
+ * (ms), the launch count and the algorithmic bytes moved (unit model of each
+ * kernel); accumulated since the last ssg_set_profiling(h, 1) */
+int ssg_get_kernel_stats(ssg_handle h, double *ms, long long *launches, double *bytes, int cap);
+/* kernels this library has launched in the process so far */
+long long ssg_launch_count(void);
+
+/* ---- hot-path pieces on their own (host buffers) ---- */
+/* IC(0) factor of the current matrix with shift alpha: L in the lower(A) pattern
+ * (lrp[n+1], lci[nnzL], lval[nnzL] values) and D = 1/pivot (n values). */
+int ssg_factor(ssg_handle h, double alpha, int32_t *lrp, int32_t *lci, double *lval, double *D, int *nnzL);
+/* z = (L D L^T)^{-1} r with the factor of the last ssg_factor call */
+int ssg_apply_precond(ssg_handle h, const double *r, double *z);
+/* y = A x */
+int ssg_spmv(ssg_handle h, const double *x, double *y);
+/* level schedule of the lower (lower = 1) or upper (lower = 0) triangle of the
+ * current matrix: level[n], perm[n] (rows by level, then row id), returns the
+ * number of levels in *nlev */
+int ssg_level_schedule(ssg_handle h, int lower, int32_t *level, int32_t *perm, int *nlev);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,230 @@
+"""ctypes front end of the CPU checkers (TEST INFRASTRUCTURE ONLY).
+
+``Oracle`` wraps ``liboracle.so`` (the C restatement in sparsesolv_oracle.c);
+``Reference`` wraps ``_ref/libsparsesolv_ref.so`` (the reference's own solver
+sources compiled by oracle/Makefile), which exists only where the reference
+checkout was available at build time. Only tests, ``__graft_entry__.smoke``
+and bench.py's CPU-baseline leg use this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libsparsesolv_ref.so")
+REF_SRC = os.environ.get("SPARSESOLV_REFERENCE", "/root/reference")
+
+
+def build(force=False):
+    """Build liboracle.so, and _ref/ when the reference checkout is present."""
+    cmd = ["make", "-s", "-C", HERE, "all"]
+    if force:
+        cmd.insert(1, "-B")
+    subprocess.run(cmd, check=True)
+    if os.path.isdir(os.path.join(REF_SRC, "src")):
+        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", "REF=" + REF_SRC], check=True)
+
+
+class _Opts(ctypes.Structure):
+    _fields_ = [("is_init", ctypes.c_int), ("is_diag_scale", ctypes.c_int), ("is_save_best", ctypes.c_int),
+                ("is_save_residual_log", ctypes.c_int), ("diverge_judge_type", ctypes.c_int),
+                ("bad_div_val", ctypes.c_double), ("bad_div_count_thres", ctypes.c_int),
+                ("conv_normalize_type", ctypes.c_int), ("conv_normalize_const", ctypes.c_double),
+                ("accel_factor", ctypes.c_double), ("precondition_type", ctypes.c_int),
+                ("mrtr_reference_quirks", ctypes.c_int)]
+
+
+@dataclass
+class Settings:
+    """Solver settings with the reference's defaults (MatSolverBase.cpp:32-47,
+    MatSolverICCG.hpp:40, MatSolverMRTR.hpp:40-43); save_log on for tests."""
+    is_init: bool = True
+    is_diag_scale: bool = False
+    is_save_best: bool = False
+    is_save_residual_log: bool = True
+    diverge_judge_type: int = 0
+    bad_div_val: float = 1000.0
+    bad_div_count_thres: int = 1000
+    conv_normalize_type: int = 0
+    conv_normalize_const: float = 1.0
+    accel_factor: float = 1.05
+    precondition_type: int = 1
+    mrtr_reference_quirks: bool = False
+
+    def c(self):
+        return _Opts(int(self.is_init), int(self.is_diag_scale), int(self.is_save_best),
+                     int(self.is_save_residual_log), int(self.diverge_judge_type), float(self.bad_div_val),
+                     int(self.bad_div_count_thres), int(self.conv_normalize_type),
+                     float(self.conv_normalize_const), float(self.accel_factor), int(self.precondition_type),
+                     int(self.mrtr_reference_quirks))
+
+
+@dataclass
+class Result:
+    converged: bool
+    x: np.ndarray
+    log: np.ndarray
+    iters: int
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class _Base:
+    lib = None
+
+    def _solve(self, fn, opts_c, method, rp, ci, val, b, x0, normB, conv, maxit, extra_iters):
+        n = len(rp) - 1
+        cplx = np.iscomplexobj(val) or np.iscomplexobj(b)
+        dt = np.complex128 if cplx else np.float64
+        rp = np.ascontiguousarray(rp, np.int32)
+        ci = np.ascontiguousarray(ci, np.int32)
+        val = np.ascontiguousarray(val, dt)
+        b = np.ascontiguousarray(b, dt)
+        x = np.zeros(n, dt) if x0 is None else np.array(x0, dt, copy=True)
+        cap = maxit + 2
+        log = np.zeros(cap)
+        log_len = ctypes.c_int(0)
+        iters = ctypes.c_int(0)
+        args = [ctypes.byref(opts_c), ctypes.c_int(method), ctypes.c_int(n), _p(rp), _p(ci), _p(val), _p(b),
+                ctypes.c_double(-1.0 if normB is None else normB), ctypes.c_double(conv), ctypes.c_int(maxit),
+                _p(x), _p(log), ctypes.c_int(cap), ctypes.byref(log_len)]
+        if extra_iters:
+            args.append(ctypes.byref(iters))
+        rc = fn(*args)
+        if rc < 0:
+            raise RuntimeError("solver error %d" % rc)
+        ll = log_len.value
+        it = iters.value if extra_iters else max(ll - 1, 0)
+        return Result(bool(rc), x, log[:min(ll, cap)].copy(), it)
+
+
+class Oracle(_Base):
+    """The C restatement of the reference's solvers."""
+
+    def __init__(self):
+        if not os.path.exists(ORACLE_LIB):
+            build()
+        self.lib = ctypes.CDLL(ORACLE_LIB)
+
+    def solve(self, method, rp, ci, val, b, settings=None, x0=None, normB=None, conv=1e-8, maxit=10000):
+        """method: 'iccg' or 'mrtr' (settings.precondition_type picks IC=0 / SGS=1)."""
+        s = settings or Settings()
+        cplx = np.iscomplexobj(val) or np.iscomplexobj(b)
+        fn = self.lib.or_solve_z if cplx else self.lib.or_solve_d
+        fn.restype = ctypes.c_int
+        return self._solve(fn, s.c(), 0 if method == "iccg" else 1, rp, ci, val, b, x0, normB, conv, maxit, True)
+
+    def ic_factor(self, rp, ci, val, alpha):
+        n = len(rp) - 1
+        cplx = np.iscomplexobj(val)
+        dt = np.complex128 if cplx else np.float64
+        lrp = np.zeros(n + 1, np.int32)
+        lci = np.zeros(len(ci), np.int32)
+        lval = np.zeros(len(ci), dt)
+        D = np.zeros(n, dt)
+        rp = np.ascontiguousarray(rp, np.int32)
+        ci = np.ascontiguousarray(ci, np.int32)
+        val = np.ascontiguousarray(val, dt)
+        fn = self.lib.or_ic_factor_z if cplx else self.lib.or_ic_factor_d
+        rc = fn(ctypes.c_int(n), _p(rp), _p(ci), _p(val), ctypes.c_double(alpha), _p(lrp), _p(lci), _p(lval), _p(D))
+        if rc == -2:
+            raise RuntimeError("there is not diagonal element!")
+        nl = lrp[n]
+        return lrp, lci[:nl].copy(), lval[:nl].copy(), D
+
+    def ic_apply(self, lrp, lci, lval, D, r):
+        n = len(lrp) - 1
+        cplx = np.iscomplexobj(lval)
+        dt = np.complex128 if cplx else np.float64
+        z = np.zeros(n, dt)
+        r = np.ascontiguousarray(r, dt)
+        fn = self.lib.or_ic_apply_z if cplx else self.lib.or_ic_apply_d
+        fn(ctypes.c_int(n), _p(np.ascontiguousarray(lrp, np.int32)), _p(np.ascontiguousarray(lci, np.int32)),
+           _p(np.ascontiguousarray(lval, dt)), _p(np.ascontiguousarray(D, dt)), _p(r), _p(z))
+        return z
+
+    def spmv(self, rp, ci, val, x):
+        n = len(rp) - 1
+        cplx = np.iscomplexobj(val) or np.iscomplexobj(x)
+        dt = np.complex128 if cplx else np.float64
+        y = np.zeros(n, dt)
+        fn = self.lib.or_spmv_z if cplx else self.lib.or_spmv_d
+        fn(ctypes.c_int(n), _p(np.ascontiguousarray(rp, np.int32)), _p(np.ascontiguousarray(ci, np.int32)),
+           _p(np.ascontiguousarray(val, dt)), _p(np.ascontiguousarray(x, dt)), _p(y))
+        return y
+
+    def levels(self, rp, ci, lower=True):
+        """(level[n], perm[n], lptr[nlev+1]) of the forward (lower) or backward sweep."""
+        n = len(rp) - 1
+        level = np.zeros(n, np.int32)
+        perm = np.zeros(n, np.int32)
+        lptr = np.zeros(n + 2, np.int32)
+        rp = np.ascontiguousarray(rp, np.int32)
+        ci = np.ascontiguousarray(ci, np.int32)
+        nlev = self.lib.or_levels(ctypes.c_int(n), _p(rp), _p(ci), ctypes.c_int(1 if lower else 0),
+                                  _p(level), _p(perm), _p(lptr))
+        return level, perm, lptr[:nlev + 1].copy()
+
+    def triangle(self, rp, ci, lower=True):
+        n = len(rp) - 1
+        trp = np.zeros(n + 1, np.int32)
+        tci = np.zeros(len(ci), np.int32)
+        src = np.zeros(len(ci), np.int32)
+        self.lib.or_triangle_pattern(ctypes.c_int(n), _p(np.ascontiguousarray(rp, np.int32)),
+                                     _p(np.ascontiguousarray(ci, np.int32)), ctypes.c_int(1 if lower else 0),
+                                     _p(trp), _p(tci), _p(src))
+        m = trp[n]
+        return trp, tci[:m].copy(), src[:m].copy()
+
+    def transpose(self, rp, ci):
+        n = len(rp) - 1
+        trp = np.zeros(n + 1, np.int32)
+        tci = np.zeros(len(ci), np.int32)
+        src = np.zeros(len(ci), np.int32)
+        self.lib.or_transpose_pattern(ctypes.c_int(n), _p(np.ascontiguousarray(rp, np.int32)),
+                                      _p(np.ascontiguousarray(ci, np.int32)), _p(trp), _p(tci), _p(src))
+        return trp, tci, src
+
+
+class Reference(_Base):
+    """The reference's own solver classes compiled from its sources."""
+
+    @staticmethod
+    def available():
+        return os.path.exists(REF_LIB)
+
+    def __init__(self):
+        if not os.path.exists(REF_LIB):
+            raise RuntimeError("reference build %s is missing" % REF_LIB)
+        self.lib = ctypes.CDLL(REF_LIB)
+
+    def solve(self, method, rp, ci, val, b, settings=None, x0=None, normB=None, conv=1e-8, maxit=10000):
+        s = settings or Settings()
+        if s.mrtr_reference_quirks is False and method == "mrtr":
+            pass  # the reference always has its own behaviour
+        cplx = np.iscomplexobj(val) or np.iscomplexobj(b)
+        fn = self.lib.ref_solve_z if cplx else self.lib.ref_solve_d
+        fn.restype = ctypes.c_int
+        return self._solve(fn, s.c(), 0 if method == "iccg" else 1, rp, ci, val, b, x0, normB, conv, maxit, False)
+
+    def ic_factor(self, rp, ci, val, alpha):
+        n = len(rp) - 1
+        cplx = np.iscomplexobj(val)
+        dt = np.complex128 if cplx else np.float64
+        lrp = np.zeros(n + 1, np.int32)
+        lci = np.zeros(len(ci), np.int32)
+        lval = np.zeros(len(ci), dt)
+        D = np.zeros(n, dt)
+        fn = self.lib.ref_ic_factor_z if cplx else self.lib.ref_ic_factor_d
+        fn(ctypes.c_int(n), _p(np.ascontiguousarray(rp, np.int32)), _p(np.ascontiguousarray(ci, np.int32)),
+           _p(np.ascontiguousarray(val, dt)), ctypes.c_double(alpha), _p(lrp), _p(lci), _p(lval), _p(D))
+        nl = lrp[n]
+        return lrp, lci[:nl].copy(), lval[:nl].copy(), D

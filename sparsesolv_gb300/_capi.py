@@ -1,0 +1,251 @@
+"""ctypes declarations of the C ABI (include/sparsesolv_gb300.h) and a thin
+handle class used by the Python mirror of the reference's module."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+SSG_OK = 0
+SSG_NOT_CONVERGED = 1
+SSG_ERR_ARG = -1
+SSG_ERR_CUDA = -2
+SSG_ERR_NO_DIAGONAL = -3
+SSG_ERR_TIMEOUT = -4
+SSG_ERR_NOMEM = -5
+SSG_ERR_STATE = -6
+METHOD_ICCG = 0
+METHOD_MRTR = 1
+REAL = 0
+COMPLEX = 1
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+EXPORTED = [
+    "ssg_default_options", "ssg_create", "ssg_destroy", "ssg_last_error", "ssg_set_options", "ssg_set_matrix",
+    "ssg_set_matrix_device", "ssg_solve", "ssg_solve_device", "ssg_get_residual_log", "ssg_get_iters",
+    "ssg_get_accel_used", "ssg_get_timings", "ssg_factor", "ssg_apply_precond", "ssg_spmv", "ssg_level_schedule",
+    "ssg_update_values", "ssg_update_values_device", "ssg_get_stream", "ssg_set_profiling", "ssg_get_kernel_stats",
+    "ssg_launch_count",
+]
+KERNEL_CLASSES = ["forward sweep", "backward sweep", "spmv", "vector", "ic factor", "level schedule"]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("is_init", ctypes.c_int), ("is_diag_scale", ctypes.c_int), ("is_save_best", ctypes.c_int),
+                ("is_save_residual_log", ctypes.c_int), ("diverge_judge_type", ctypes.c_int),
+                ("bad_div_val", ctypes.c_double), ("bad_div_count_thres", ctypes.c_int),
+                ("conv_normalize_type", ctypes.c_int), ("conv_normalize_const", ctypes.c_double),
+                ("accel_factor", ctypes.c_double), ("precondition_type", ctypes.c_int),
+                ("precision", ctypes.c_int), ("mrtr_reference_quirks", ctypes.c_int)]
+
+
+def declare(lib):
+    H = ctypes.c_void_p
+    P = ctypes.c_void_p
+    I = ctypes.c_int
+    D = ctypes.c_double
+    pI = ctypes.POINTER(ctypes.c_int)
+    sig = {
+        "ssg_default_options": ([ctypes.POINTER(Options)], None),
+        "ssg_create": ([ctypes.POINTER(ctypes.c_void_p), I], I),
+        "ssg_destroy": ([H], I),
+        "ssg_last_error": ([H], ctypes.c_char_p),
+        "ssg_set_options": ([H, ctypes.POINTER(Options)], I),
+        "ssg_set_matrix": ([H, I, I, P, P, P, I], I),
+        "ssg_set_matrix_device": ([H, I, I, P, P, P, I], I),
+        "ssg_solve": ([H, I, D, I, D, P, P], I),
+        "ssg_solve_device": ([H, I, D, I, D, P, P], I),
+        "ssg_get_residual_log": ([H, P, I, pI], I),
+        "ssg_get_iters": ([H, pI], I),
+        "ssg_get_accel_used": ([H, ctypes.POINTER(ctypes.c_double)], I),
+        "ssg_get_timings": ([H, P, I], I),
+        "ssg_factor": ([H, D, P, P, P, P, pI], I),
+        "ssg_apply_precond": ([H, P, P], I),
+        "ssg_spmv": ([H, P, P], I),
+        "ssg_level_schedule": ([H, I, P, P, pI], I),
+        "ssg_update_values": ([H, P], I),
+        "ssg_update_values_device": ([H, P], I),
+        "ssg_get_stream": ([H, ctypes.POINTER(ctypes.c_void_p)], I),
+        "ssg_set_profiling": ([H, I], I),
+        "ssg_get_kernel_stats": ([H, P, P, P, I], I),
+        "ssg_launch_count": ([], ctypes.c_longlong),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+
+
+class SolverError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (code %d)" % (msg, code))
+        self.code = code
+
+
+def _p(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+class Handle:
+    """One device handle: a CUDA stream plus all device state of a solver."""
+
+    def __init__(self, device=0):
+        from ._native import load_solver
+        self.lib = load_solver()
+        h = ctypes.c_void_p()
+        rc = self.lib.ssg_create(ctypes.byref(h), int(device))
+        if rc != SSG_OK:
+            raise SolverError(rc, "ssg_create failed")
+        self.h = h
+        self.n = 0
+        self.complex = False
+        self._mat_key = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ssg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc < 0:
+            msg = self.lib.ssg_last_error(self.h)
+            raise SolverError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+        return rc
+
+    @staticmethod
+    def default_options():
+        from ._native import load_solver
+        o = Options()
+        load_solver().ssg_default_options(ctypes.byref(o))
+        return o
+
+    def set_options(self, o):
+        self._check(self.lib.ssg_set_options(self.h, ctypes.byref(o)), "ssg_set_options")
+
+    def set_matrix(self, row_ptr, col, val, key=None):
+        """Upload a CSR matrix (numpy, host). ``key`` skips re-uploads of the same matrix."""
+        if key is not None and key == self._mat_key:
+            return
+        rp = np.ascontiguousarray(row_ptr, np.int32)
+        ci = np.ascontiguousarray(col, np.int32)
+        cplx = np.iscomplexobj(val)
+        v = np.ascontiguousarray(val, np.complex128 if cplx else np.float64)
+        n = len(rp) - 1
+        self._check(self.lib.ssg_set_matrix(self.h, n, len(ci), _p(rp), _p(ci), _p(v), COMPLEX if cplx else REAL),
+                    "ssg_set_matrix")
+        self.n = n
+        self.complex = cplx
+        self._mat_key = key
+
+    def set_matrix_device(self, n, nnz, rp_ptr, ci_ptr, val_ptr, cplx):
+        self._check(self.lib.ssg_set_matrix_device(self.h, n, nnz, ctypes.c_void_p(rp_ptr), ctypes.c_void_p(ci_ptr),
+                                                   ctypes.c_void_p(val_ptr), COMPLEX if cplx else REAL),
+                    "ssg_set_matrix_device")
+        self.n = n
+        self.complex = cplx
+        self._mat_key = None
+
+    def solve(self, method, b, x, conv=1e-8, max_ite=10000, normB=-1.0):
+        """Host arrays; x is updated in place. Returns True when converged."""
+        dt = np.complex128 if self.complex else np.float64
+        assert b.dtype == dt and x.dtype == dt and b.flags.c_contiguous and x.flags.c_contiguous
+        rc = self._check(self.lib.ssg_solve(self.h, method, float(conv), int(max_ite), float(normB), _p(b), _p(x)),
+                         "ssg_solve")
+        return rc == SSG_OK
+
+    def solve_device(self, method, b_ptr, x_ptr, conv=1e-8, max_ite=10000, normB=-1.0):
+        rc = self._check(self.lib.ssg_solve_device(self.h, method, float(conv), int(max_ite), float(normB),
+                                                   ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr)), "ssg_solve_device")
+        return rc == SSG_OK
+
+    def residual_log(self):
+        n = ctypes.c_int(0)
+        self._check(self.lib.ssg_get_residual_log(self.h, None, 0, ctypes.byref(n)), "ssg_get_residual_log")
+        out = np.zeros(n.value)
+        self._check(self.lib.ssg_get_residual_log(self.h, _p(out), n.value, ctypes.byref(n)), "ssg_get_residual_log")
+        return out
+
+    def iters(self):
+        it = ctypes.c_int(0)
+        self._check(self.lib.ssg_get_iters(self.h, ctypes.byref(it)), "ssg_get_iters")
+        return it.value
+
+    def accel_used(self):
+        a = ctypes.c_double(0)
+        self._check(self.lib.ssg_get_accel_used(self.h, ctypes.byref(a)), "ssg_get_accel_used")
+        return a.value
+
+    def timings(self):
+        t = np.zeros(2)
+        self._check(self.lib.ssg_get_timings(self.h, _p(t), 2), "ssg_get_timings")
+        return t
+
+    def factor(self, alpha):
+        dt = np.complex128 if self.complex else np.float64
+        n = self.n
+        nnzL = ctypes.c_int(0)
+        self._check(self.lib.ssg_factor(self.h, float(alpha), None, None, None, None, ctypes.byref(nnzL)), "ssg_factor")
+        lrp = np.zeros(n + 1, np.int32)
+        lci = np.zeros(max(nnzL.value, 1), np.int32)
+        lval = np.zeros(max(nnzL.value, 1), dt)
+        D = np.zeros(max(n, 1), dt)
+        self._check(self.lib.ssg_factor(self.h, float(alpha), _p(lrp), _p(lci), _p(lval), _p(D), ctypes.byref(nnzL)),
+                    "ssg_factor")
+        return lrp, lci[:nnzL.value], lval[:nnzL.value], D[:n]
+
+    def apply_precond(self, r):
+        dt = np.complex128 if self.complex else np.float64
+        r = np.ascontiguousarray(r, dt)
+        z = np.zeros(self.n, dt)
+        self._check(self.lib.ssg_apply_precond(self.h, _p(r), _p(z)), "ssg_apply_precond")
+        return z
+
+    def spmv(self, x):
+        dt = np.complex128 if self.complex else np.float64
+        x = np.ascontiguousarray(x, dt)
+        y = np.zeros(self.n, dt)
+        self._check(self.lib.ssg_spmv(self.h, _p(x), _p(y)), "ssg_spmv")
+        return y
+
+    def update_values(self, val):
+        cplx = np.iscomplexobj(val)
+        v = np.ascontiguousarray(val, np.complex128 if cplx else np.float64)
+        self._check(self.lib.ssg_update_values(self.h, _p(v)), "ssg_update_values")
+
+    def update_values_device(self, ptr):
+        self._check(self.lib.ssg_update_values_device(self.h, ctypes.c_void_p(ptr)), "ssg_update_values_device")
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        self._check(self.lib.ssg_get_stream(self.h, ctypes.byref(s)), "ssg_get_stream")
+        return s.value or 0
+
+    def set_profiling(self, on):
+        self._check(self.lib.ssg_set_profiling(self.h, 1 if on else 0), "ssg_set_profiling")
+
+    def kernel_stats(self):
+        """{class: (total ms, launches, algorithmic bytes)}"""
+        k = len(KERNEL_CLASSES)
+        ms = np.zeros(k)
+        la = np.zeros(k, np.int64)
+        by = np.zeros(k)
+        self._check(self.lib.ssg_get_kernel_stats(self.h, _p(ms), _p(la), _p(by), k), "ssg_get_kernel_stats")
+        return {KERNEL_CLASSES[i]: (float(ms[i]), int(la[i]), float(by[i])) for i in range(k)}
+
+    def launch_count(self):
+        return int(self.lib.ssg_launch_count())
+
+    def level_schedule(self, lower=True):
+        level = np.zeros(max(self.n, 1), np.int32)
+        perm = np.zeros(max(self.n, 1), np.int32)
+        nlev = ctypes.c_int(0)
+        self._check(self.lib.ssg_level_schedule(self.h, 1 if lower else 0, _p(level), _p(perm), ctypes.byref(nlev)),
+                    "ssg_level_schedule")
+        return level[:self.n], perm[:self.n], nlev.value

@@ -1,0 +1,124 @@
+"""Build and load the native libraries of the package.
+
+Three shared objects are built in-tree, next to their sources:
+
+* ``libsparsesolv_gb300.so`` -- the sm_103a CUDA kernels, the C++ solver
+  drivers and the C-ABI declared in ``include/sparsesolv_gb300.h``
+  (``nvcc -gencode arch=compute_103a,code=sm_103a``);
+* ``voxel/libvoxelgen.so`` -- the host-side seeded voxel FEM system generator
+  (plain C, ``-ffp-contract=off`` so that x86-64 and aarch64 builds produce
+  bit-identical matrices).
+
+Nothing here falls back to a CPU implementation: :func:`load_solver` raises
+when the CUDA library is missing or cannot be loaded.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+REPO_DIR = os.path.dirname(PKG_DIR)
+CSRC = os.path.join(PKG_DIR, "csrc")
+INCLUDE = os.path.join(REPO_DIR, "include")
+SOLVER_LIB = os.path.join(PKG_DIR, "libsparsesolv_gb300.so")
+VOXEL_LIB = os.path.join(PKG_DIR, "voxel", "libvoxelgen.so")
+
+NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+# translation units of the CUDA library (compiled in parallel, then linked)
+CUDA_SOURCES = [
+    "ss_levels.cu",
+    "ss_factor.cu",
+    "ss_trsv.cu",
+    "ss_spmv_vec.cu",
+    "ss_solver.cu",
+    "ss_capi.cu",
+]
+
+
+def _run(cmd):
+    proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError("command failed (%d): %s\n%s" % (proc.returncode, " ".join(cmd), proc.stdout))
+    return proc.stdout
+
+
+def _newer(target, sources):
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(s) <= t for s in sources)
+
+
+def build_voxel(force=False):
+    src = os.path.join(PKG_DIR, "voxel", "voxelgen.c")
+    if not force and _newer(VOXEL_LIB, [src]):
+        return VOXEL_LIB
+    _run(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared", "-o", VOXEL_LIB, src, "-lm"])
+    return VOXEL_LIB
+
+
+def build_solver(force=False, verbose=False):
+    """Compile the CUDA library for sm_103a (cross-compiles without a GPU)."""
+    srcs = [os.path.join(CSRC, s) for s in CUDA_SOURCES]
+    hdrs = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
+    hdrs.append(os.path.join(INCLUDE, "sparsesolv_gb300.h"))
+    if not force and _newer(SOLVER_LIB, srcs + hdrs):
+        return SOLVER_LIB
+    objdir = os.path.join(PKG_DIR, "_build")
+    os.makedirs(objdir, exist_ok=True)
+    common = [NVCC, *ARCH_FLAGS, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+              "-I", INCLUDE, "-I", CSRC]
+    if verbose:
+        common += ["-Xptxas", "-v"]
+
+    def compile_one(src):
+        obj = os.path.join(objdir, os.path.basename(src) + ".o")
+        out = _run(common + ["-c", src, "-o", obj])
+        return obj, out
+
+    with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
+        results = list(ex.map(compile_one, srcs))
+    objs = [r[0] for r in results]
+    if verbose:
+        for _, out in results:
+            sys.stdout.write(out)
+    _run([NVCC, *ARCH_FLAGS, "-shared", "-o", SOLVER_LIB, *objs, "-lcudart"])
+    return SOLVER_LIB
+
+
+def build_all(force=False, verbose=False):
+    build_voxel(force)
+    build_solver(force, verbose)
+
+
+_solver = None
+_voxel = None
+
+
+def load_voxel():
+    global _voxel
+    if _voxel is None:
+        if not os.path.exists(VOXEL_LIB):
+            build_voxel()
+        _voxel = ctypes.CDLL(VOXEL_LIB)
+    return _voxel
+
+
+def load_solver():
+    """Load the CUDA library; raises if it is missing (there is no CPU path)."""
+    global _solver
+    if _solver is None:
+        if not os.path.exists(SOLVER_LIB):
+            raise RuntimeError(
+                "sparsesolv_gb300: CUDA library %s is missing; run "
+                "`python -c 'import __graft_entry__ as g; g.build()'` first" % SOLVER_LIB)
+        _solver = ctypes.CDLL(SOLVER_LIB)
+        from . import _capi
+        _capi.declare(_solver)
+    return _solver

@@ -1,0 +1,328 @@
+// ss_capi.cu -- the extern "C" entry points declared in include/sparsesolv_gb300.h.
+#include <cstring>
+#include <new>
+
+#include "ss_solver.cuh"
+
+using ssg::cplx;
+using ssg::Error;
+using ssg::Handle;
+
+namespace ssg {
+long long launch_count();
+}
+
+struct ssg_handle_s {
+    Handle *h;
+    ssg::DBuf io_b, io_x;
+};
+
+namespace {
+
+template <typename F>
+int guarded(ssg_handle hd, F &&f) {
+    if (!hd || !hd->h) return SSG_ERR_ARG;
+    try {
+        SSG_CUDA(cudaSetDevice(hd->h->device));
+        return f(*hd->h);
+    } catch (const Error &e) {
+        hd->h->last_error = e.msg;
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        hd->h->last_error = "host allocation failed";
+        return SSG_ERR_NOMEM;
+    }
+}
+
+size_t vbytes(const Handle &h) { return h.vtype == SSG_COMPLEX ? 16 : 8; }
+
+}  // namespace
+
+extern "C" {
+
+void ssg_default_options(ssg_options *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    // src/MatSolverBase.cpp:32-47
+    o->is_init = 1;
+    o->is_diag_scale = 0;
+    o->is_save_best = 0;
+    o->is_save_residual_log = 0;
+    o->diverge_judge_type = 0;
+    o->bad_div_val = 1000.0;
+    o->bad_div_count_thres = 1000;
+    o->conv_normalize_type = 0;
+    o->conv_normalize_const = 1.0;
+    // include/SparseSolv/MatSolverICCG.hpp:40, MatSolverMRTR.hpp:40-43
+    o->accel_factor = 1.05;
+    o->precondition_type = 1;
+    o->precision = SSG_PREC_FP64;
+    o->mrtr_reference_quirks = 0;
+}
+
+int ssg_create(ssg_handle *out, int device) {
+    if (!out) return SSG_ERR_ARG;
+    *out = nullptr;
+    ssg_handle_s *hd = new (std::nothrow) ssg_handle_s();
+    if (!hd) return SSG_ERR_NOMEM;
+    try {
+        hd->h = new Handle(device);
+    } catch (const Error &e) {
+        delete hd;
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        delete hd;
+        return SSG_ERR_NOMEM;
+    }
+    *out = hd;
+    return SSG_OK;
+}
+
+int ssg_destroy(ssg_handle hd) {
+    if (!hd) return SSG_ERR_ARG;
+    if (hd->h) cudaSetDevice(hd->h->device);
+    hd->io_b.release();
+    hd->io_x.release();
+    delete hd->h;
+    delete hd;
+    return SSG_OK;
+}
+
+const char *ssg_last_error(ssg_handle hd) {
+    if (!hd || !hd->h) return "invalid handle";
+    return hd->h->last_error.c_str();
+}
+
+int ssg_set_options(ssg_handle hd, const ssg_options *o) {
+    if (!o) return SSG_ERR_ARG;
+    return guarded(hd, [&](Handle &h) {
+        h.opt = *o;
+        return SSG_OK;
+    });
+}
+
+int ssg_set_matrix(ssg_handle hd, int n, int nnz, const int32_t *row_ptr, const int32_t *col, const double *val,
+                   int value_type) {
+    if (!row_ptr || (nnz > 0 && (!col || !val))) return SSG_ERR_ARG;
+    return guarded(hd, [&](Handle &h) {
+        h.set_matrix(n, nnz, row_ptr, col, val, value_type, cudaMemcpyHostToDevice);
+        return SSG_OK;
+    });
+}
+
+int ssg_set_matrix_device(ssg_handle hd, int n, int nnz, const int32_t *row_ptr, const int32_t *col,
+                          const double *val, int value_type) {
+    if (!row_ptr || (nnz > 0 && (!col || !val))) return SSG_ERR_ARG;
+    return guarded(hd, [&](Handle &h) {
+        h.set_matrix(n, nnz, row_ptr, col, val, value_type, cudaMemcpyDeviceToDevice);
+        return SSG_OK;
+    });
+}
+
+static int check_solve_args(const Handle &h, int method, int max_ite) {
+    if (h.vtype < 0) return SSG_ERR_STATE;
+    if (method != SSG_METHOD_ICCG && method != SSG_METHOD_MRTR) return SSG_ERR_ARG;
+    if (max_ite < 0) return SSG_ERR_ARG;
+    return SSG_OK;
+}
+
+int ssg_solve_device(ssg_handle hd, int method, double conv_cri, int max_ite, double normB, const double *d_b,
+                     double *d_x) {
+    return guarded(hd, [&](Handle &h) {
+        const int rc = check_solve_args(h, method, max_ite);
+        if (rc) return rc;
+        if (h.n > 0 && (!d_b || !d_x)) return SSG_ERR_ARG;
+        if (h.vtype == SSG_COMPLEX) return h.solve<cplx>(method, conv_cri, max_ite, normB, (const cplx *)d_b, (cplx *)d_x);
+        return h.solve<double>(method, conv_cri, max_ite, normB, d_b, d_x);
+    });
+}
+
+int ssg_solve(ssg_handle hd, int method, double conv_cri, int max_ite, double normB, const double *b, double *x) {
+    return guarded(hd, [&](Handle &h) {
+        const int rc = check_solve_args(h, method, max_ite);
+        if (rc) return rc;
+        if (h.n > 0 && (!b || !x)) return SSG_ERR_ARG;
+        const size_t bytes = vbytes(h) * (size_t)h.n;
+        hd->io_b.ensure(bytes + 16);
+        hd->io_x.ensure(bytes + 16);
+        if (bytes) {
+            SSG_CUDA(cudaMemcpyAsync(hd->io_b.p, b, bytes, cudaMemcpyHostToDevice, h.stream));
+            SSG_CUDA(cudaMemcpyAsync(hd->io_x.p, x, bytes, cudaMemcpyHostToDevice, h.stream));
+        }
+        int res;
+        if (h.vtype == SSG_COMPLEX)
+            res = h.solve<cplx>(method, conv_cri, max_ite, normB, hd->io_b.as<cplx>(), hd->io_x.as<cplx>());
+        else
+            res = h.solve<double>(method, conv_cri, max_ite, normB, hd->io_b.as<double>(), hd->io_x.as<double>());
+        if (bytes) SSG_CUDA(cudaMemcpyAsync(x, hd->io_x.p, bytes, cudaMemcpyDeviceToHost, h.stream));
+        SSG_CUDA(cudaStreamSynchronize(h.stream));
+        return res;
+    });
+}
+
+int ssg_update_values(ssg_handle hd, const double *val) {
+    return guarded(hd, [&](Handle &h) {
+        if (h.nnz > 0 && !val) return SSG_ERR_ARG;
+        h.update_values(val, cudaMemcpyHostToDevice);
+        return SSG_OK;
+    });
+}
+
+int ssg_update_values_device(ssg_handle hd, const double *d_val) {
+    return guarded(hd, [&](Handle &h) {
+        if (h.nnz > 0 && !d_val) return SSG_ERR_ARG;
+        h.update_values(d_val, cudaMemcpyDeviceToDevice);
+        return SSG_OK;
+    });
+}
+
+int ssg_get_stream(ssg_handle hd, void **stream) {
+    if (!stream) return SSG_ERR_ARG;
+    return guarded(hd, [&](Handle &h) {
+        *stream = (void *)h.stream;
+        return SSG_OK;
+    });
+}
+
+int ssg_set_profiling(ssg_handle hd, int enable) {
+    return guarded(hd, [&](Handle &h) {
+        h.prof.on = enable != 0;
+        for (int c = 0; c < ssg::PC_N; ++c) {
+            h.prof.ms[c] = 0.0;
+            h.prof.launches[c] = 0;
+            h.prof.bytes[c] = 0.0;
+        }
+        h.prof.recs.clear();
+        h.prof.used = 0;
+        return SSG_OK;
+    });
+}
+
+int ssg_get_kernel_stats(ssg_handle hd, double *ms, long long *launches, double *bytes, int cap) {
+    return guarded(hd, [&](Handle &h) {
+        for (int c = 0; c < ssg::PC_N && c < cap; ++c) {
+            if (ms) ms[c] = h.prof.ms[c];
+            if (launches) launches[c] = h.prof.launches[c];
+            if (bytes) bytes[c] = h.prof.bytes[c];
+        }
+        return SSG_OK;
+    });
+}
+
+long long ssg_launch_count(void) { return ssg::launch_count(); }
+
+int ssg_get_residual_log(ssg_handle hd, double *log, int cap, int *len) {
+    return guarded(hd, [&](Handle &h) {
+        // MatSolverBase::getResidualLog: zeros of the stored size when logging is off
+        const int sz = (int)h.residual_log.size();
+        if (len) *len = sz;
+        if (log)
+            for (int i = 0; i < sz && i < cap; ++i) log[i] = h.opt.is_save_residual_log ? h.residual_log[i] : 0.0;
+        return SSG_OK;
+    });
+}
+
+int ssg_get_iters(ssg_handle hd, int *iters) {
+    if (!iters) return SSG_ERR_ARG;
+    return guarded(hd, [&](Handle &h) {
+        *iters = h.iters;
+        return SSG_OK;
+    });
+}
+
+int ssg_get_accel_used(ssg_handle hd, double *alpha) {
+    if (!alpha) return SSG_ERR_ARG;
+    return guarded(hd, [&](Handle &h) {
+        *alpha = h.alpha_used;
+        return SSG_OK;
+    });
+}
+
+int ssg_get_timings(ssg_handle hd, double *ms, int cap) {
+    if (!ms) return SSG_ERR_ARG;
+    return guarded(hd, [&](Handle &h) {
+        if (cap > 0) ms[0] = h.t_setup_ms;
+        if (cap > 1) ms[1] = h.t_iter_ms;
+        return SSG_OK;
+    });
+}
+
+int ssg_factor(ssg_handle hd, double alpha, int32_t *lrp, int32_t *lci, double *lval, double *D, int *nnzL) {
+    return guarded(hd, [&](Handle &h) {
+        if (h.vtype < 0) return SSG_ERR_STATE;
+        const size_t vb = vbytes(h);
+        if (h.vtype == SSG_COMPLEX)
+            h.ensure_factor<cplx>(alpha, false);
+        else
+            h.ensure_factor<double>(alpha, false);
+        if (nnzL) *nnzL = h.nnzL;
+        ssg::DBuf nat;
+        nat.alloc(vb * (size_t)(h.nnzL + 1));
+        if (h.vtype == SSG_COMPLEX)
+            ssg::gather_values<cplx>(h.nat2lev.as<int>(), h.Lval.as<cplx>(), nat.as<cplx>(), h.nnzL, h.stream);
+        else
+            ssg::gather_values<double>(h.nat2lev.as<int>(), h.Lval.as<double>(), nat.as<double>(), h.nnzL, h.stream);
+        if (lrp) SSG_CUDA(cudaMemcpyAsync(lrp, h.Lnat_rp.p, sizeof(int) * (size_t)(h.n + 1), cudaMemcpyDeviceToHost, h.stream));
+        if (lci && h.nnzL)
+            SSG_CUDA(cudaMemcpyAsync(lci, h.Lnat_ci.p, sizeof(int) * (size_t)h.nnzL, cudaMemcpyDeviceToHost, h.stream));
+        if (lval && h.nnzL) SSG_CUDA(cudaMemcpyAsync(lval, nat.p, vb * (size_t)h.nnzL, cudaMemcpyDeviceToHost, h.stream));
+        if (D && h.n) SSG_CUDA(cudaMemcpyAsync(D, h.Dvec.p, vb * (size_t)h.n, cudaMemcpyDeviceToHost, h.stream));
+        SSG_CUDA(cudaStreamSynchronize(h.stream));
+        return SSG_OK;
+    });
+}
+
+int ssg_apply_precond(ssg_handle hd, const double *r, double *z) {
+    return guarded(hd, [&](Handle &h) {
+        if (!h.fac_valid || h.fac_version != h.version) return SSG_ERR_STATE;
+        const size_t bytes = vbytes(h) * (size_t)h.n;
+        h.ensure_work(vbytes(h));
+        hd->io_b.ensure(bytes + 16);
+        hd->io_x.ensure(bytes + 16);
+        SSG_CUDA(cudaMemcpyAsync(hd->io_b.p, r, bytes, cudaMemcpyHostToDevice, h.stream));
+        if (h.vtype == SSG_COMPLEX)
+            h.apply_precond<cplx>(hd->io_b.as<cplx>(), hd->io_x.as<cplx>(), nullptr);
+        else
+            h.apply_precond<double>(hd->io_b.as<double>(), hd->io_x.as<double>(), nullptr);
+        SSG_CUDA(cudaMemcpyAsync(z, hd->io_x.p, bytes, cudaMemcpyDeviceToHost, h.stream));
+        SSG_CUDA(cudaStreamSynchronize(h.stream));
+        h.check_err("preconditioner");
+        return SSG_OK;
+    });
+}
+
+int ssg_spmv(ssg_handle hd, const double *x, double *y) {
+    return guarded(hd, [&](Handle &h) {
+        if (h.vtype < 0) return SSG_ERR_STATE;
+        const size_t bytes = vbytes(h) * (size_t)h.n;
+        hd->io_b.ensure(bytes + 16);
+        hd->io_x.ensure(bytes + 16);
+        SSG_CUDA(cudaMemcpyAsync(hd->io_b.p, x, bytes, cudaMemcpyHostToDevice, h.stream));
+        if (h.vtype == SSG_COMPLEX)
+            ssg::spmv<cplx>(h.n, h.A_rp.as<int>(), h.A_ci.as<int>(), h.A_val.as<cplx>(), hd->io_b.as<cplx>(),
+                            hd->io_x.as<cplx>(), h.stream);
+        else
+            ssg::spmv<double>(h.n, h.A_rp.as<int>(), h.A_ci.as<int>(), h.A_val.as<double>(), hd->io_b.as<double>(),
+                              hd->io_x.as<double>(), h.stream);
+        SSG_CUDA(cudaMemcpyAsync(y, hd->io_x.p, bytes, cudaMemcpyDeviceToHost, h.stream));
+        SSG_CUDA(cudaStreamSynchronize(h.stream));
+        return SSG_OK;
+    });
+}
+
+int ssg_level_schedule(ssg_handle hd, int lower, int32_t *level, int32_t *perm, int *nlev) {
+    return guarded(hd, [&](Handle &h) {
+        if (h.vtype < 0) return SSG_ERR_STATE;
+        h.ensure_patterns(false, !lower);
+        const ssg::Tri &T = lower ? h.Lf : h.Ub;
+        if (nlev) *nlev = T.nlev;
+        if (level && h.n)
+            SSG_CUDA(cudaMemcpyAsync(level, T.level.p, sizeof(int) * (size_t)h.n, cudaMemcpyDeviceToHost, h.stream));
+        if (perm && h.n)
+            SSG_CUDA(cudaMemcpyAsync(perm, T.perm.p, sizeof(int) * (size_t)h.n, cudaMemcpyDeviceToHost, h.stream));
+        SSG_CUDA(cudaStreamSynchronize(h.stream));
+        return SSG_OK;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,237 @@
+// ss_factor.cu -- shifted IC(0) factorisation and diagonal scaling on the GPU.
+//
+// The factor restates SprsPreconditioner::detail::IC_decomp_sub
+// (src/SprsPreconditioner.cpp:43-111) on the level-ordered lower triangle:
+//   L_ij = a_ij - sum_{k<j, k in row i and row j} L_ik L_jk D_k     (j < i)
+//   L_ii = alpha a_ii - sum_{k<i} L_ik^2 D_k
+//   D_i  = 1 / L_ii   (1 / DBL_EPSILON when |L_ii| < 1e-12)
+// One warp owns a row; the entries of the row are updated in column order
+// (each uses the already updated L_ik of the same row), the sums over k are
+// warp reductions. Rows are claimed in level order through a ticket, and a
+// row waits (bounded) for the rows it reads to publish their "done" flags.
+#include <cfloat>
+
+#include "ss_internal.cuh"
+
+namespace ssg {
+
+constexpr int FAC_MAX_PER_LANE = 8;  // rows of the lower triangle up to 256 entries
+
+template <typename T>
+__device__ __forceinline__ T ldcg(const T *p) {
+    return __ldcg(p);
+}
+template <>
+__device__ __forceinline__ cplx ldcg<cplx>(const cplx *p) {
+    const double2 v = __ldcg((const double2 *)p);
+    return {v.x, v.y};
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_ic_factor(int n, const int *perm, const int *ipos, const int *prp,
+                                                   const int *pci, T *lval, T *D, int *done, double alpha,
+                                                   int *ticket, int *err) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(ticket, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= n) return;
+        const int i = perm[t];
+        const int a = prp[t], m = prp[t + 1] - a;
+        int bad = 0;
+        if (m > 32 * FAC_MAX_PER_LANE || m < 1) bad = 1;
+        int c[FAC_MAX_PER_LANE];
+        T v[FAC_MAX_PER_LANE], dk[FAC_MAX_PER_LANE];
+        // load the row and wait for every row it depends on (all j < i)
+#pragma unroll
+        for (int q = 0; q < FAC_MAX_PER_LANE; ++q) {
+            const int k = lane + 32 * q;
+            c[q] = (!bad && k < m) ? pci[a + k] : INT_MAX;
+            v[q] = (!bad && k < m) ? lval[a + k] : Sc<T>::zero();
+            dk[q] = Sc<T>::zero();
+            if (c[q] < i) {
+                const volatile int *f = done + c[q];
+                if (*f == 0) {
+                    const unsigned long long start = gtimer();
+                    int polls = 0;
+                    while (*f == 0) {
+                        if ((++polls & 63) == 0) {
+                            if (*(volatile int *)err) break;
+                            if (gtimer() - start > SPIN_LIMIT_NS) {
+                                atomicExch(err, ERR_TIMEOUT);
+                                break;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        __threadfence();
+#pragma unroll
+        for (int q = 0; q < FAC_MAX_PER_LANE; ++q)
+            if (c[q] < i) dk[q] = ldcg(D + c[q]);
+        // off-diagonal entries in column order
+        const int mo = bad ? 0 : m - 1;  // entries before the (expected) diagonal
+        for (int jj = 0; jj < mo; ++jj) {
+            // column j = c of entry jj (owned by lane jj % 32, slot jj / 32)
+            int cj = 0;
+            T s = Sc<T>::zero();
+#pragma unroll
+            for (int q = 0; q < FAC_MAX_PER_LANE; ++q) {
+                if (q == jj / 32) {
+                    cj = __shfl_sync(0xffffffffu, c[q], jj & 31);
+                    s = Sc<T>::shfl(v[q], jj & 31);
+                }
+            }
+            if (cj >= i) break;
+            // row j of the factor (final: its done flag was observed above)
+            const int pj = ipos[cj];
+            const int aj = prp[pj], mj = prp[pj + 1] - aj;
+            T part = Sc<T>::zero();
+            for (int base = 0; base < mj; base += 32) {
+                const int l = base + lane;
+                const int cl = l < mj ? ldcg(pci + aj + l) : INT_MAX;
+                const T vl = l < mj ? ldcg(lval + aj + l) : Sc<T>::zero();
+                const int cnt = min(32, mj - base);
+                for (int src = 0; src < cnt; ++src) {
+                    const int cc = __shfl_sync(0xffffffffu, cl, src);
+                    const T vv = Sc<T>::shfl(vl, src);
+                    if (cc >= cj) break;  // uniform: only entries left of the diagonal of row j
+#pragma unroll
+                    for (int q = 0; q < FAC_MAX_PER_LANE; ++q)
+                        if (lane + 32 * q < jj && c[q] == cc) part = part + v[q] * vv * dk[q];
+                }
+            }
+            part = warp_sum(part);
+            s = s - part;
+#pragma unroll
+            for (int q = 0; q < FAC_MAX_PER_LANE; ++q)
+                if (lane + 32 * q == jj) v[q] = s;
+        }
+        // the last entry must be the diagonal (src/SprsPreconditioner.cpp:88-94)
+        int last_c = 0;
+        T diag = Sc<T>::zero();
+        if (!bad) {
+#pragma unroll
+            for (int q = 0; q < FAC_MAX_PER_LANE; ++q) {
+                if (q == (m - 1) / 32) {
+                    last_c = __shfl_sync(0xffffffffu, c[q], (m - 1) & 31);
+                    diag = Sc<T>::shfl(v[q], (m - 1) & 31);
+                }
+            }
+        }
+        if (bad || last_c != i) {
+            if (lane == 0) atomicExch(err, (m > 32 * FAC_MAX_PER_LANE) ? ERR_ROW_TOO_LONG : ERR_NO_DIAG);
+            if (lane == 0) D[i] = Sc<T>::one();
+        } else {
+            T sq = Sc<T>::zero();
+#pragma unroll
+            for (int q = 0; q < FAC_MAX_PER_LANE; ++q)
+                if (lane + 32 * q < m - 1 && c[q] < i) sq = sq + v[q] * v[q] * dk[q];
+            sq = warp_sum(sq);
+            const T s = diag * Sc<T>::from(alpha) - sq;
+#pragma unroll
+            for (int q = 0; q < FAC_MAX_PER_LANE; ++q)
+                if (lane + 32 * q == m - 1) v[q] = s;
+            if (lane == 0) D[i] = (Sc<T>::absv(s) < 1.0e-12) ? Sc<T>::from(1.0 / DBL_EPSILON) : Sc<T>::one() / s;
+        }
+#pragma unroll
+        for (int q = 0; q < FAC_MAX_PER_LANE; ++q)
+            if (lane + 32 * q < m && !bad) lval[a + lane + 32 * q] = v[q];
+        __syncwarp();
+        __threadfence();
+        if (lane == 0) *(volatile int *)(done + i) = 1;
+    }
+}
+
+template <typename T>
+void ic_factor(const Tri &L, T *lval, T *D, double alpha, int *d_err, int *d_ticket, cudaStream_t s) {
+    if (L.n == 0) return;
+    DBuf done;
+    done.alloc(sizeof(int) * (size_t)L.n);
+    SSG_CUDA(cudaMemsetAsync(done.p, 0, sizeof(int) * (size_t)L.n, s));
+    SSG_CUDA(cudaMemsetAsync(d_ticket, 0, sizeof(int), s));
+    int dev = 0, sms = 0;
+    SSG_CUDA(cudaGetDevice(&dev));
+    SSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int warps = min(L.n, sms * 32);
+    k_ic_factor<T><<<div_up(warps * 32, 256), 256, 0, s>>>(L.n, L.perm.as<int>(), L.ipos.as<int>(), L.prp.as<int>(),
+                                                           L.pci.as<int>(), lval, D, done.as<int>(), alpha, d_ticket,
+                                                           d_err);
+    SSG_LAUNCHED();
+    SSG_CUDA(cudaStreamSynchronize(s));
+}
+
+// ---------------------------------------------------------------- diagonal scaling
+// SprsPreconditioner::DiagScaling (src/SprsPreconditioner.cpp:150-231):
+// d_i = 1/sqrt(|a_ii|) for real, 1/sqrt(std::norm(a_ii)) = 1/|a_ii| for complex
+// (the reference's quirk, kept), 1/DBL_EPSILON when the root is < 1e-12.
+template <typename T>
+__global__ void k_diag_scaling(int n, const int *rp, const int *ci, const T *val, const T *b, T *d, T *bs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int k = rp[i]; k < rp[i + 1]; ++k) {
+        if (ci[k] == i) {
+            const double t1 = Sc<T>::is_complex ? Sc<T>::abs2(val[k]) : Sc<T>::absv(val[k]);
+            const double t1b = sqrt(t1);
+            const double t2 = (t1b < 1.0e-12) ? 1.0 / DBL_EPSILON : 1.0 / t1b;
+            d[i] = Sc<T>::from(t2);
+            if (b) bs[i] = b[i] * Sc<T>::from(t2);
+            return;
+        }
+    }
+    d[i] = Sc<T>::zero();
+    if (b) bs[i] = Sc<T>::zero();
+}
+
+// D A D: MatSolverBase::makeDiagMatTrans (src/MatSolverBase.cpp:99-141)
+template <typename T>
+__global__ void k_dad(int n, const int *rp, const int *ci, const T *val, const T *d, T *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const T di = d[i];
+    for (int k = rp[i]; k < rp[i + 1]; ++k) out[k] = val[k] * (di * d[ci[k]]);
+}
+
+template <typename T>
+__global__ void k_pivots_positive(int n, const T *D, int *flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && !(Sc<T>::re(D[i]) > 0.0)) atomicExch(flag, 0);
+}
+
+template <typename T>
+void diag_scaling(int n, const int *rp, const int *ci, const T *val, const T *b, T *d, T *bs, cudaStream_t s) {
+    if (n == 0) return;
+    k_diag_scaling<T><<<div_up(n, 256), 256, 0, s>>>(n, rp, ci, val, b, d, bs);
+    SSG_LAUNCHED();
+}
+template <typename T>
+void dad_values(int n, const int *rp, const int *ci, const T *val, const T *d, T *out, cudaStream_t s) {
+    if (n == 0) return;
+    k_dad<T><<<div_up(n, 256), 256, 0, s>>>(n, rp, ci, val, d, out);
+    SSG_LAUNCHED();
+}
+template <typename T>
+void all_pivots_positive(int n, const T *D, int *d_flag, cudaStream_t s) {
+    SSG_CUDA(cudaMemsetAsync(d_flag, 0, sizeof(int), s));
+    const int one = 1;
+    SSG_CUDA(cudaMemcpyAsync(d_flag, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+    if (n > 0) {
+        k_pivots_positive<T><<<div_up(n, 256), 256, 0, s>>>(n, D, d_flag);
+        SSG_LAUNCHED();
+    }
+}
+
+#define SSG_INST(T)                                                                                      \
+    template void ic_factor<T>(const Tri &, T *, T *, double, int *, int *, cudaStream_t);              \
+    template void diag_scaling<T>(int, const int *, const int *, const T *, const T *, T *, T *,        \
+                                  cudaStream_t);                                                         \
+    template void dad_values<T>(int, const int *, const int *, const T *, const T *, T *, cudaStream_t); \
+    template void all_pivots_positive<T>(int, const T *, int *, cudaStream_t);
+SSG_INST(double)
+SSG_INST(cplx)
+#undef SSG_INST
+
+}  // namespace ssg

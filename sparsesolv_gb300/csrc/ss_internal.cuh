@@ -1,0 +1,105 @@
+// ss_internal.cuh -- host-side internal interfaces between the translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "ss_common.cuh"
+
+namespace ssg {
+
+// Thrown inside the library, converted to a return code at the C ABI.
+struct Error {
+    int code;
+    std::string msg;
+};
+
+void cuda_check(cudaError_t e, const char *what);
+#define SSG_CUDA(call) ::ssg::cuda_check((call), #call)
+// after every kernel launch: count it and surface launch errors
+void note_launch();
+#define SSG_LAUNCHED() ::ssg::note_launch()
+
+// ---------------------------------------------------------------- device memory
+// Owning device buffer (cudaMallocAsync on the handle's stream is avoided:
+// buffers live as long as the handle, allocated once per matrix pattern).
+struct DBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    DBuf(DBuf &&o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+    DBuf &operator=(DBuf &&o) noexcept {
+        if (this != &o) { release(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+        return *this;
+    }
+    ~DBuf() { release(); }
+    void release();
+    void alloc(size_t b);           // exact size, content undefined
+    void ensure(size_t b);          // grow when smaller
+    template <typename U>
+    U *as() const { return (U *)p; }
+};
+
+// ---------------------------------------------------------------- level-scheduled triangle
+// One triangular factor in the layout the sweeps stream: rows in level order
+// (level, then row id), each row's entries contiguous and in the original
+// column order, column indices kept as original row ids.
+struct Tri {
+    int n = 0, nnz = 0, nlev = 0;
+    bool lower = true;           // lower: deps j < i, diagonal last; upper: deps j > i, diagonal first
+    DBuf level, perm, ipos;      // level[i], perm[t] = row, ipos[row] = t
+    DBuf prp, pci, psrc;         // level-ordered CSR; psrc[k] = source value index
+    std::vector<int> lptr;       // host copy of level pointers
+    DBuf lptr_d;
+};
+
+// ss_levels.cu
+void scan_exclusive(int *d_in_out, int count, int *d_total, cudaStream_t s, DBuf &tmp);
+// triangle of a CSR pattern (explicit zeros kept): rp/ci natural order -> trp/tci/tsrc
+void triangle_pattern(int n, const int *rp, const int *ci, bool lower, DBuf &trp, DBuf &tci, DBuf &tsrc,
+                      int &tnnz, cudaStream_t s, DBuf &tmp);
+// transpose of a CSR pattern with sorted rows, tsrc[k] = entry of the source
+void transpose_pattern(int n, int nnz, const int *rp, const int *ci, DBuf &trp, DBuf &tci, DBuf &tsrc,
+                       cudaStream_t s, DBuf &tmp);
+// level schedule + level-ordered copy of a triangle given in natural order;
+// src (may be null) is composed into psrc.
+void build_tri(Tri &T, int n, int nnz, const int *rp, const int *ci, const int *src, bool lower,
+               int *d_err, cudaStream_t s, DBuf &tmp);
+// out[k] = in[src[k]] for k < count (values of width sizeof(T))
+template <typename T>
+void gather_values(const int *src, const T *in, T *out, int count, cudaStream_t s);
+
+// ss_factor.cu
+template <typename T>
+void ic_factor(const Tri &L, T *lval, T *D, double alpha, int *d_err, int *d_ticket, cudaStream_t s);
+template <typename T>
+void diag_scaling(int n, const int *rp, const int *ci, const T *val, const T *b, T *d, T *bs, cudaStream_t s);
+template <typename T>
+void dad_values(int n, const int *rp, const int *ci, const T *val, const T *d, T *out, cudaStream_t s);
+template <typename T>
+void all_pivots_positive(int n, const T *D, int *d_flag, cudaStream_t s);
+
+// ss_trsv.cu
+enum SweepMode : int {
+    SW_FWD_DIV = 0,   // out_i = (rhs_i - sum_{j<i} v_ij out_j) / v_ii        (diag last)
+    SW_BWD_IC = 1,    // out_i = D_i * (-sum_{j>i} v_ij out_j) + aux_i         (diag first, skipped)
+    SW_BWD_DIV = 2,   // out_i = (rhs_i - sum_{j>i} v_ij out_j) / v_ii        (diag first)
+    SW_FWD_EIS = 3,   // y_i = (rhs_i - aux_i - sum v_ij y_j) / v_ii, out2_i = y_i + aux_i
+};
+template <typename T>
+void sweep(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *D, T *out, T *out2,
+           int *d_ticket, int *d_err, cudaStream_t s);
+
+// ss_spmv_vec.cu -- see the Krylov state there
+struct KState;
+template <typename T>
+void spmv(int n, const int *rp, const int *ci, const T *val, const T *x, T *y, cudaStream_t s);
+size_t part_bytes();
+// nat2lev[e] = level-ordered position of entry e of the natural-order triangle (rp)
+void level_positions(const Tri &T, const int *rp, int *nat2lev, cudaStream_t s);
+
+}  // namespace ssg

@@ -1,0 +1,118 @@
+// ss_solver.cuh -- the solver handle behind the C ABI.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "sparsesolv_gb300.h"
+#include "ss_internal.cuh"
+#include "ss_krylov.cuh"
+
+namespace ssg {
+
+// per-kernel-class event timing (ssg_set_profiling)
+enum : int { PC_FWD = 0, PC_BWD = 1, PC_SPMV = 2, PC_VEC = 3, PC_FACTOR = 4, PC_LEVELS = 5, PC_N = 6 };
+struct ProfRec {
+    int cls, iter;
+    bool pre;  // launched before the iteration's convergence decision
+    cudaEvent_t a, b;
+    double bytes;
+};
+struct Prof {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    std::vector<ProfRec> recs;
+    double ms[PC_N] = {};
+    long long launches[PC_N] = {};
+    double bytes[PC_N] = {};
+    int iter = 0;
+    bool pre = true;
+};
+
+struct Handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    ssg_options opt{};
+    std::string last_error;
+
+    // ---- the matrix, natural order (SparseMat's CSR)
+    int n = 0, nnz = 0, vtype = -1;
+    uint64_t version = 0;  // bumps on every set_matrix
+    DBuf A_rp, A_ci, A_val;
+
+    // ---- patterns and level schedules (depend on the sparsity pattern)
+    uint64_t pat_version = ~0ull;
+    DBuf Lnat_rp, Lnat_ci, Lnat_src;  // lower(A), src -> A entries
+    int nnzL = 0;
+    DBuf Unat_rp, Unat_ci, Unat_src;  // upper(A), src -> A entries
+    int nnzU = 0;
+    Tri Lf;          // forward schedule over lower(A); psrc -> A entries
+    Tri Ltb;         // backward schedule over trans(lower(A)); psrc -> positions of Lf
+    bool ltb_ready = false;
+    Tri Ub;          // backward schedule over upper(A); psrc -> A entries
+    bool ub_ready = false;
+    DBuf nat2lev;    // natural lower entry -> position in Lf
+
+    // ---- values
+    DBuf Lval, Ltval, Cval, Uval, Dvec;  // factor (Lf / Ltb layouts), SGS triangles, 1/pivot
+    bool fac_valid = false;
+    uint64_t fac_version = 0;
+    double fac_alpha_req = 0.0, alpha_used = 0.0;
+    int fac_scaled = -1;
+    bool sgs_valid = false;
+    uint64_t sgs_version = 0;
+    DBuf dscale, dad;  // diagonal scaling d and D A D values
+    bool dad_valid = false;
+    uint64_t dad_version = 0;
+
+    // ---- work space
+    DBuf vec[12];
+    DBuf part, state, logbuf, small;  // small: ticket[4], err[1], pad, doubles[8]
+    KState *h_state = nullptr;        // pinned
+    double *h_scal = nullptr;         // pinned scratch
+
+    // ---- results of the last solve
+    std::vector<double> residual_log;
+    int iters = 0;
+    double t_setup_ms = 0.0, t_iter_ms = 0.0;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+
+    Prof prof;
+    int prof_begin(int cls);
+    void prof_end(int idx, double bytes);
+    void prof_flush(int iters_done);
+    template <typename F>
+    void timed(int cls, double bytes, F &&fn) {
+        const int idx = prof_begin(cls);
+        fn();
+        prof_end(idx, bytes);
+    }
+
+    int *ticket() { return small.as<int>(); }
+    int *err() { return small.as<int>() + 4; }
+    double *dscal() { return (double *)(small.as<char>() + 64); }
+    KState *st() { return state.as<KState>(); }
+
+    Handle(int dev);
+    ~Handle();
+    void set_matrix(int n_, int nnz_, const int32_t *rp, const int32_t *ci, const double *val, int vt,
+                    cudaMemcpyKind kind);
+    void update_values(const double *val, cudaMemcpyKind kind);
+    void ensure_patterns(bool need_ltb, bool need_ub);
+    void check_err(const char *where);
+    template <typename T>
+    void ensure_scaled();
+    template <typename T>
+    void ensure_factor(double alpha, bool scaled);
+    template <typename T>
+    void ensure_sgs();
+    template <typename T>
+    int solve(int method, double conv, int max_ite, double normB, const T *d_b, T *d_x);
+    template <typename T>
+    void apply_precond(const T *d_r, T *d_z, const KState *st);
+    void ensure_work(size_t elem_bytes);
+};
+
+}  // namespace ssg

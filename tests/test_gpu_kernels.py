@@ -1,0 +1,119 @@
+"""GPU parity of the hot-path pieces, through the C ABI, against the oracle:
+level sets and level permutation (bit-exact), IC(0) factor, the IC
+preconditioner sweeps, SpMV."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from sparsesolv_gb300 import _capi
+from sparsesolv_gb300 import voxel
+
+pytestmark = pytest.mark.gpu
+
+
+def _random_spd_pattern(n, density, seed, cplx=False):
+    rng = np.random.default_rng(seed)
+    A = sp.random(n, n, density=density, random_state=rng, format="csr")
+    A = A + A.T + sp.eye(n) * (n * 0.5)
+    A = A.tocsr()
+    A.sort_indices()
+    val = A.data.astype(np.complex128) * (1 + 0.1j) if cplx else A.data
+    return A.indptr.astype(np.int32), A.indices.astype(np.int32), val
+
+
+def _cases():
+    out = {}
+    out["cc8"] = voxel.curl_curl_case(8, seed=21).assemble()[:3]
+    out["cfg1"] = voxel.config1().assemble()[:3]
+    out["rand"] = _random_spd_pattern(3000, 0.002, 5)
+    out["ec6"] = voxel.eddy_current_case(6, seed=9).assemble()[:3]
+    out["rand_c"] = _random_spd_pattern(1500, 0.004, 6, cplx=True)
+    return out
+
+
+CASES = _cases()
+
+
+@pytest.fixture(scope="module")
+def handle(gpu):
+    h = _capi.Handle(0)
+    yield h
+    h.close()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("lower", [True, False])
+def test_level_schedule_bit_exact(handle, oracle, name, lower):
+    rp, ci, val = CASES[name]
+    handle.set_matrix(rp, ci, val)
+    level, perm, nlev = handle.level_schedule(lower)
+    trp, tci, _ = oracle.triangle(rp, ci, lower)
+    olevel, operm, olptr = oracle.levels(trp, tci, lower)
+    assert nlev == len(olptr) - 1
+    assert np.array_equal(level, olevel)
+    assert np.array_equal(perm, operm)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("alpha", [1.0, 1.1])
+def test_ic_factor(handle, oracle, name, alpha):
+    rp, ci, val = CASES[name]
+    handle.set_matrix(rp, ci, val)
+    lrp, lci, lval, D = handle.factor(alpha)
+    orp, oci, oval, oD = oracle.ic_factor(rp, ci, val, alpha)
+    assert np.array_equal(lrp, orp) and np.array_equal(lci, oci)   # integer pattern: bit-exact
+    scale = np.abs(oval).max()
+    assert np.allclose(lval, oval, rtol=1e-9, atol=1e-12 * scale)
+    assert np.allclose(D, oD, rtol=1e-9, atol=0)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_ic_preconditioner_apply(handle, oracle, name):
+    rp, ci, val = CASES[name]
+    handle.set_matrix(rp, ci, val)
+    lrp, lci, lval, D = handle.factor(1.1)
+    rng = np.random.default_rng(1)
+    n = len(rp) - 1
+    r = rng.standard_normal(n)
+    if np.iscomplexobj(val):
+        r = r + 1j * rng.standard_normal(n)
+    z = handle.apply_precond(r)
+    zo = oracle.ic_apply(lrp, lci, lval, D, r)   # oracle substitution on the GPU's factor
+    assert np.linalg.norm(z - zo) <= 1e-11 * np.linalg.norm(zo)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_spmv(handle, oracle, name):
+    rp, ci, val = CASES[name]
+    handle.set_matrix(rp, ci, val)
+    n = len(rp) - 1
+    x = np.random.default_rng(2).standard_normal(n)
+    if np.iscomplexobj(val):
+        x = x * (1 - 0.5j)
+    y = handle.spmv(x)
+    yo = oracle.spmv(rp, ci, val, x)
+    assert np.allclose(y, yo, rtol=1e-13, atol=1e-13 * np.abs(yo).max())
+
+
+def test_missing_diagonal_reports_error(handle):
+    rp = np.array([0, 1, 2, 4], np.int32)
+    ci = np.array([0, 1, 0, 1], np.int32)  # row 2 lacks its diagonal
+    handle.set_matrix(rp, ci, np.array([2.0, 2.0, 1.0, 1.0]))
+    with pytest.raises(_capi.SolverError) as e:
+        handle.factor(1.0)
+    assert e.value.code == _capi.SSG_ERR_NO_DIAGONAL
+    # the handle stays usable
+    rp, ci, val = CASES["cc8"]
+    handle.set_matrix(rp, ci, val)
+    handle.factor(1.1)
+
+
+def test_factor_golden_fixture(handle, golden, golden_cases):
+    data, meta = golden
+    for key in ["doc5/ic1.00", "doc5/ic1.10", "cc6/ic1.10", "ec5/ic1.10"]:
+        rp, ci, va, b = golden_cases[key.split("/")[0]]
+        handle.set_matrix(rp, ci, va)
+        lrp, lci, lval, D = handle.factor(meta["factors"][key]["alpha"])
+        assert np.array_equal(lrp, data[key + "/lrp"]) and np.array_equal(lci, data[key + "/lci"])
+        assert np.allclose(lval, data[key + "/lval"], rtol=1e-9, atol=1e-12 * np.abs(lval).max())
+        assert np.allclose(D, data[key + "/D"], rtol=1e-9)

@@ -1,0 +1,194 @@
+"""GPU solver parity through the C ABI and through the SparseSolvPy mirror.
+
+Parity bar (real): iteration count within 3% of the reference's (golden
+fixtures made by the reference itself), residual log within 1e-6 relative,
+solution within 1e-6 relative of the FP64 oracle solve with the same method,
+shift and preconditioner (the curl-curl system is singular, so x is compared
+method to method), true residual |b - A x| / |b| below 1e-7.
+Complex (COCG / complex MRTR on singular eddy-current systems): iteration
+count within 10%, first log entries within 1e-8, A x within 5e-8 |b|."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle.oracle import Settings
+from sparsesolv_gb300 import SparseSolvPy as ssp
+from sparsesolv_gb300 import _capi
+
+pytestmark = pytest.mark.gpu
+
+METHOD = {"iccg": _capi.METHOD_ICCG, "mrtr": _capi.METHOD_MRTR}
+
+
+def iter_slack(iters, is_complex):
+    return max(2, int((0.10 if is_complex else 0.03) * iters + 0.999))
+
+
+@pytest.fixture(scope="module")
+def handle(gpu):
+    h = _capi.Handle(0)
+    yield h
+    h.close()
+
+
+def gpu_solve(h, method, rp, ci, va, b, s, x0=None, maxit=5000, conv=1e-8, normB=-1.0):
+    h.set_matrix(rp, ci, va, key=(id(rp), id(va)))
+    o = h.default_options()
+    for f, _ in o._fields_:
+        if hasattr(s, f):
+            setattr(o, f, type(getattr(o, f))(getattr(s, f)))
+    h.set_options(o)
+    dt = np.complex128 if np.iscomplexobj(va) else np.float64
+    x = np.zeros(len(b), dt) if x0 is None else np.array(x0, dt)
+    ok = h.solve(METHOD[method], np.ascontiguousarray(b, dt), x, conv=conv, max_ite=maxit, normB=normB)
+    return ok, x, h.residual_log(), h.iters()
+
+
+def true_res(rp, ci, va, b, x):
+    A = sp.csr_matrix((va, ci, rp))
+    return np.linalg.norm(b - A @ x) / np.linalg.norm(b)
+
+
+REAL_RUNS = ["cc10/iccg", "cc10/mrtr_ic", "cc10/mrtr_sgs", "cc10/iccg_diag", "cc10/iccg_norm1",
+             "cfg1/iccg", "cfg1/mrtr_ic", "cfg1/mrtr_sgs"]
+
+
+@pytest.mark.parametrize("key", REAL_RUNS)
+def test_real_against_reference_golden(handle, oracle, golden, golden_cases, key):
+    data, meta = golden
+    run = meta["runs"][key]
+    rp, ci, va, b = golden_cases[key.split("/")[0]]
+    s = Settings(**run["settings"])
+    s.is_save_residual_log = True
+    ok, x, log, iters = gpu_solve(handle, run["method"], rp, ci, va, b, s)
+    assert ok == run["converged"]
+    assert abs(iters - run["iters"]) <= iter_slack(run["iters"], False)
+    glog = data[key + "/log"]
+    m = min(len(log), len(glog))
+    assert np.allclose(log[:m], glog[:m], rtol=1e-6, atol=1e-13 * glog[0])
+    # same method, shift and preconditioner in the FP64 oracle (corrected MRTR p update)
+    ores = oracle.solve(run["method"], rp, ci, va, b, s)
+    assert np.linalg.norm(x - ores.x) <= 1e-6 * np.linalg.norm(ores.x)
+    assert true_res(rp, ci, va, b, x) < 1e-7
+
+
+def test_mrtr_reference_quirk_mode_reproduces_reference_x(handle, golden, golden_cases):
+    data, meta = golden
+    rp, ci, va, b = golden_cases["cc10"]
+    s = Settings(**meta["runs"]["cc10/mrtr_ic"]["settings"])
+    s.mrtr_reference_quirks = True
+    ok, x, log, iters = gpu_solve(handle, "mrtr", rp, ci, va, b, s)
+    gx = data["cc10/mrtr_ic/x"]
+    assert np.linalg.norm(x - gx) <= 1e-6 * np.linalg.norm(gx)
+    assert true_res(rp, ci, va, b, x) > 1e-3   # the reference's x is not a solution
+
+
+@pytest.mark.parametrize("key", ["ec8/iccg", "ec8/mrtr_ic", "ec8/mrtr_sgs"])
+def test_complex_against_reference_golden(handle, golden, golden_cases, key):
+    data, meta = golden
+    run = meta["runs"][key]
+    rp, ci, va, b = golden_cases["ec8"]
+    s = Settings(**run["settings"])
+    ok, x, log, iters = gpu_solve(handle, run["method"], rp, ci, va, b, s)
+    assert ok == run["converged"]
+    assert abs(iters - run["iters"]) <= iter_slack(run["iters"], True)
+    glog = data[key + "/log"]
+    assert np.allclose(log[:10], glog[:10], rtol=1e-8)
+    if run["method"] == "iccg":
+        A = sp.csr_matrix((va, ci, rp))
+        gx = data[key + "/x"]
+        assert np.linalg.norm(A @ (x - gx)) <= 5e-8 * np.linalg.norm(b)
+    elif run["settings"]["precondition_type"] == 0:
+        assert true_res(rp, ci, va, b, x) < 1e-7   # corrected p update gives a solution
+
+
+def test_auto_alpha(handle, golden, golden_cases):
+    data, meta = golden
+    rp, ci, va, b = golden_cases["cc10"]
+    s = Settings(accel_factor=-1.0)
+    ok, x, log, iters = gpu_solve(handle, "iccg", rp, ci, va, b, s)
+    assert ok and abs(iters - meta["runs"]["cc10/iccg_auto"]["iters"]) <= 2
+    assert handle.accel_used() == 1.0
+    assert true_res(rp, ci, va, b, x) < 1e-7
+
+
+@pytest.mark.parametrize("method,pt", [("iccg", 1), ("mrtr", 0), ("mrtr", 1)])
+def test_options_against_oracle(handle, oracle, golden_cases, method, pt):
+    rp, ci, va, b = golden_cases["cc10"]
+    for over in (dict(is_save_best=True), dict(diverge_judge_type=1, bad_div_val=1.5, bad_div_count_thres=3),
+                 dict(conv_normalize_type=2, conv_normalize_const=1e-3), dict(is_diag_scale=True)):
+        for maxit in (4, 3000):
+            s = Settings(accel_factor=1.1, precondition_type=pt, **over)
+            ok, x, log, iters = gpu_solve(handle, method, rp, ci, va, b, s, maxit=maxit)
+            o = oracle.solve(method, rp, ci, va, b, s, maxit=maxit)
+            assert ok == o.converged and iters == o.iters, (over, maxit)
+            assert np.allclose(log, o.log, rtol=1e-6, atol=1e-13 * o.log[0])
+            assert np.linalg.norm(x - o.x) <= 1e-6 * np.linalg.norm(o.x)
+
+
+@pytest.mark.parametrize("method,pt", [("iccg", 1), ("mrtr", 0), ("mrtr", 1)])
+def test_warm_start(handle, oracle, golden_cases, method, pt):
+    rp, ci, va, b = golden_cases["cc10"]
+    x_part = oracle.solve("iccg", rp, ci, va, b, Settings(accel_factor=1.1), maxit=6).x
+    s = Settings(accel_factor=1.1, is_init=False, precondition_type=pt)
+    ok, x, log, iters = gpu_solve(handle, method, rp, ci, va, b, s, x0=x_part)
+    o = oracle.solve(method, rp, ci, va, b, s, x0=x_part)
+    assert ok and iters == o.iters
+    assert np.allclose(log, o.log, rtol=1e-6, atol=1e-13 * o.log[0])
+    assert true_res(rp, ci, va, b, x) < 1e-7
+
+
+def test_zero_rhs_and_early_exit(handle, golden_cases):
+    rp, ci, va, b = golden_cases["cc10"]
+    s = Settings(accel_factor=1.1)
+    ok, x, log, iters = gpu_solve(handle, "iccg", rp, ci, va, np.zeros_like(b), s)
+    assert ok and iters == 0 and np.all(x == 0) and log.tolist() == [0.0]
+    # starting from the solution: returns at once with an empty log
+    ok, xs, _, _ = gpu_solve(handle, "iccg", rp, ci, va, b, s)
+    s2 = Settings(accel_factor=1.1, is_init=False)
+    ok2, x2, log2, iters2 = gpu_solve(handle, "iccg", rp, ci, va, b, s2, x0=xs, conv=1e-6)
+    assert ok2 and iters2 == 0 and len(log2) == 0
+
+
+def test_deterministic_and_factor_reuse(handle, golden_cases):
+    rp, ci, va, b = golden_cases["cfg1"]
+    s = Settings(accel_factor=1.1)
+    _, x1, l1, _ = gpu_solve(handle, "iccg", rp, ci, va, b, s)
+    _, x2, l2, _ = gpu_solve(handle, "iccg", rp, ci, va, b, s)   # factor cached on the device
+    assert np.array_equal(x1, x2) and np.array_equal(l1, l2)
+
+
+def test_sparsesolvpy_mirror(gpu, golden, golden_cases):
+    data, meta = golden
+    rp, ci, va, b = golden_cases["cfg1"]
+    n = len(rp) - 1
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    A = ssp.SparseMat(len(ci), rows.tolist(), ci.tolist(), va.tolist())
+    s = ssp.MatSolverICCG()
+    s.setSaveLog(True)
+    s.setAccelFactor(1.1)
+    ok, x = s.solve_real(1e-8, 5000, A, b, np.zeros(n))
+    log = s.getResidualLog()
+    assert ok and len(log) - 1 == meta["runs"]["cfg1/iccg"]["iters"] == s.getIterations()
+    m = ssp.MatSolverMRTR()
+    m.setSaveLog(True)
+    ok, x = m.solve_real(1e-8, 5000, A, b, np.zeros(n))     # default: SGS
+    assert ok and abs(len(m.getResidualLog()) - 1 - meta["runs"]["cfg1/mrtr_sgs"]["iters"]) <= 1
+    # logging off: the reference returns zeros of the stored size
+    m.setSaveLog(False)
+    m.solve_real(1e-8, 5000, A, b, np.zeros(n))
+    assert all(v == 0.0 for v in m.getResidualLog())
+
+
+def test_sparsesolvpy_complex_builder(gpu, golden_cases):
+    rp, ci, va, b = golden_cases["ec8"]
+    n = len(rp) - 1
+    bld = ssp.SparseBuilderC(n)
+    for i in range(n):
+        for k in range(rp[i], rp[i + 1]):
+            bld.add(i, int(ci[k]), complex(va[k]))
+    A = ssp.SparseMatC(bld)
+    s = ssp.MatSolverICCG()
+    s.setAccelFactor(1.1)
+    ok, x = s.solve_complex(1e-8, 5000, A, b, np.zeros(n, complex))
+    assert ok and true_res(rp, ci, va, b, x) < 5e-8

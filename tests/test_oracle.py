@@ -1,0 +1,185 @@
+"""Pins the CPU oracle (oracle/sparsesolv_oracle.c) against the reference.
+
+The reference has no tests of its own, so its outputs were captured into
+tests/golden/ by tests/golden/make_golden.py, which runs the reference's
+solver classes compiled from their sources. These tests check the oracle
+against those fixtures, against an independent dense IC(0) on the 5x5 example
+matrix of the reference's documentation, and (when the reference build
+oracle/_ref exists on this machine) against the reference live."""
+import numpy as np
+import pytest
+
+from oracle.oracle import Reference, Settings
+
+REAL_LOG_RTOL = 1e-7      # reference sums dots with vectorised Eigen; the oracle sums serially
+COMPLEX_HEAD = 10         # COCG / complex MRTR logs agree this far, then rounding noise grows
+# alpha = 1.0 (the automatic search's first accepted value) leaves near-zero
+# pivots on the singular curl-curl matrix; rounding then grows from iteration
+# ~10 on, in the reference and the oracle alike, without changing the count.
+NOISY = {"cc10/iccg_auto"}
+
+
+def iter_slack(iters, is_complex):
+    """Allowed iteration-count difference. Real systems: 3% (the parity bar).
+    Complex COCG / MRTR on these singular eddy-current systems stagnate near
+    the tolerance and reorder under last-bit differences (the reference and
+    the oracle differ by 5 of 83 on ec8), so complex runs get 10%."""
+    return max(2, int((0.10 if is_complex else 0.03) * iters + 0.999))
+
+
+def _settings(meta_settings, **over):
+    s = Settings(**{k: v for k, v in meta_settings.items()})
+    for k, v in over.items():
+        setattr(s, k, v)
+    return s
+
+
+def test_golden_inputs_unchanged(golden, golden_cases):
+    from make_golden import digest
+    _, meta = golden
+    for name, (rp, ci, va, b) in golden_cases.items():
+        assert meta["cases"][name]["sha256"] == digest(rp, ci, va, b), name
+
+
+@pytest.mark.parametrize("key", [
+    "doc5/iccg", "cc10/iccg", "cc10/mrtr_ic", "cc10/mrtr_sgs", "cc10/iccg_diag", "cc10/iccg_auto",
+    "cc10/iccg_norm1", "cfg1/iccg", "cfg1/mrtr_ic", "cfg1/mrtr_sgs", "ec8/iccg", "ec8/mrtr_ic", "ec8/mrtr_sgs"])
+def test_oracle_matches_reference_golden(oracle, golden, golden_cases, key):
+    data, meta = golden
+    run = meta["runs"][key]
+    case = key.split("/")[0]
+    rp, ci, va, b = golden_cases[case]
+    # the golden MRTR solutions carry the reference's own p update
+    s = _settings(run["settings"], mrtr_reference_quirks=True)
+    res = oracle.solve(run["method"], rp, ci, va, b, s, conv=1e-8, maxit=5000)
+    glog = data[key + "/log"]
+    assert res.converged == run["converged"]
+    if np.iscomplexobj(va) or key in NOISY:
+        assert abs(res.iters - run["iters"]) <= iter_slack(run["iters"], np.iscomplexobj(va))
+        h = min(COMPLEX_HEAD, len(glog), len(res.log))
+        assert np.allclose(res.log[:h], glog[:h], rtol=1e-8, atol=0)
+    else:
+        assert res.iters == run["iters"]
+        assert np.allclose(res.log, glog, rtol=REAL_LOG_RTOL, atol=1e-14 * glog[0])
+    # (the reference's complex IC-MRTR x carries its p-update defect and is not a solution)
+    if key + "/x" in data and not (np.iscomplexobj(va) and run["method"] == "mrtr"):
+        gx = data[key + "/x"]
+        if np.iscomplexobj(va):
+            # the eddy-current operator is singular in the air (gradients); compare A x
+            import scipy.sparse as sp
+            A = sp.csr_matrix((va, ci, rp))
+            assert np.linalg.norm(A @ (res.x - gx)) <= 5e-8 * np.linalg.norm(b)
+        else:
+            rel = np.linalg.norm(res.x - gx) / np.linalg.norm(gx)
+            assert rel < 1e-9, rel
+
+
+@pytest.mark.parametrize("key", ["doc5/ic1.00", "doc5/ic1.10", "cc6/ic1.10", "ec5/ic1.10"])
+def test_oracle_factor_matches_reference_golden(oracle, golden, golden_cases, key):
+    data, meta = golden
+    case = key.split("/")[0]
+    rp, ci, va, b = golden_cases[case]
+    lrp, lci, lval, D = oracle.ic_factor(rp, ci, va, meta["factors"][key]["alpha"])
+    assert np.array_equal(lrp, data[key + "/lrp"]) and np.array_equal(lci, data[key + "/lci"])
+    assert np.allclose(lval, data[key + "/lval"], rtol=1e-12, atol=1e-300)
+    assert np.allclose(D, data[key + "/D"], rtol=1e-12, atol=1e-300)
+
+
+def _dense_ic0(A, alpha):
+    """Independent IC(0) (root-free L D L^T on the pattern of tril(A)), dense loops."""
+    n = A.shape[0]
+    mask = np.tril(A != 0)
+    L = np.zeros_like(A)
+    D = np.zeros(n)
+    for i in range(n):
+        for j in range(i):
+            if not mask[i, j]:
+                continue
+            s = A[i, j]
+            for k in range(j):
+                if mask[i, k] and mask[j, k]:
+                    s -= L[i, k] * L[j, k] * D[k]
+            L[i, j] = s
+        s = alpha * A[i, i] - sum(L[i, k] ** 2 * D[k] for k in range(i) if mask[i, k])
+        L[i, i] = s
+        D[i] = 1.0 / s
+    return L, D
+
+
+@pytest.mark.parametrize("alpha", [1.0, 1.1, 1.3])
+def test_known_answer_ic_doc_matrix(oracle, alpha):
+    from make_golden import DOC5, dense_to_csr
+    rp, ci, va = dense_to_csr(DOC5)
+    lrp, lci, lval, D = oracle.ic_factor(rp, ci, va, alpha)
+    L, Dd = _dense_ic0(DOC5, alpha)
+    dense = np.zeros_like(DOC5)
+    for i in range(5):
+        for k in range(lrp[i], lrp[i + 1]):
+            dense[i, lci[k]] = lval[k]
+    assert np.allclose(dense, L, rtol=1e-14, atol=1e-14)
+    assert np.allclose(D, Dd, rtol=1e-14)
+    # (L D L^T) z = r through the oracle's substitution
+    r = np.arange(1.0, 6.0)
+    z = oracle.ic_apply(lrp, lci, lval, D, r)
+    M = L @ np.diag(Dd) @ L.T
+    assert np.allclose(M @ z, r, rtol=1e-12)
+
+
+def test_missing_diagonal_is_an_error(oracle):
+    rp = np.array([0, 1, 2, 4], np.int32)
+    ci = np.array([0, 1, 0, 1], np.int32)  # row 2 has no diagonal
+    va = np.array([2.0, 2.0, 1.0, 1.0])
+    with pytest.raises(RuntimeError, match="diagonal"):
+        oracle.ic_factor(rp, ci, va, 1.0)
+
+
+def test_levels_are_a_valid_schedule(oracle, golden_cases):
+    rp, ci, va, b = golden_cases["cc10"]
+    for lower in (True, False):
+        level, perm, lptr = oracle.levels(rp, ci, lower)
+        n = len(rp) - 1
+        assert sorted(perm.tolist()) == list(range(n))
+        for i in range(n):
+            deps = [c for c in ci[rp[i]:rp[i + 1]] if (c < i if lower else c > i)]
+            want = 1 + max(level[deps]) if deps else 0
+            assert level[i] == want
+        # rows by level then row id
+        keys = level[perm].astype(np.int64) * n + perm
+        assert np.all(np.diff(keys) > 0)
+        assert lptr[-1] == n
+
+
+needs_ref = pytest.mark.skipif(not Reference.available(), reason="reference build oracle/_ref not present")
+
+
+@needs_ref
+@pytest.mark.parametrize("over", [
+    dict(is_save_best=True, accel_factor=1.1),
+    dict(diverge_judge_type=1, bad_div_val=1.5, bad_div_count_thres=3, accel_factor=1.1),
+    dict(conv_normalize_type=2, conv_normalize_const=1e-3, accel_factor=1.1),
+    dict(accel_factor=1.3, is_diag_scale=True),
+])
+@pytest.mark.parametrize("method,pt", [("iccg", 1), ("mrtr", 0), ("mrtr", 1)])
+def test_oracle_vs_reference_live(oracle, golden_cases, over, method, pt):
+    rp, ci, va, b = golden_cases["cc10"]
+    s = Settings(precondition_type=pt, mrtr_reference_quirks=True, **over)
+    ref = Reference()
+    for maxit in (5, 3000):
+        r1 = oracle.solve(method, rp, ci, va, b, s, maxit=maxit)
+        r2 = ref.solve(method, rp, ci, va, b, s, maxit=maxit)
+        assert r1.converged == r2.converged and r1.iters == len(r2.log) - 1
+        assert np.allclose(r1.log, r2.log, rtol=REAL_LOG_RTOL, atol=1e-14 * r2.log[0])
+        assert np.linalg.norm(r1.x - r2.x) <= 1e-8 * np.linalg.norm(r2.x)
+
+
+@needs_ref
+def test_oracle_vs_reference_warm_start(oracle, golden_cases):
+    rp, ci, va, b = golden_cases["cc10"]
+    ref = Reference()
+    x_part = oracle.solve("iccg", rp, ci, va, b, Settings(accel_factor=1.1), maxit=6).x
+    for method, pt in (("iccg", 1), ("mrtr", 0), ("mrtr", 1)):
+        s = Settings(accel_factor=1.1, is_init=False, precondition_type=pt, mrtr_reference_quirks=True)
+        r1 = oracle.solve(method, rp, ci, va, b, s, x0=x_part)
+        r2 = ref.solve(method, rp, ci, va, b, s, x0=x_part)
+        assert r1.iters == len(r2.log) - 1
+        assert np.allclose(r1.log, r2.log, rtol=REAL_LOG_RTOL, atol=1e-14 * r2.log[0])
