@@ -167,6 +167,21 @@ __device__ __forceinline__ unsigned long long gtimer() {
     return t;
 }
 
+// xor-shuffle within a group of G lanes using only the group's own lanes:
+// groups of one warp may wait on each other (a row of one group depending on
+// a row of another), so a full-warp mask could tie them together
+__device__ __forceinline__ unsigned group_mask(int G) {
+    return G >= 32 ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+}
+__device__ __forceinline__ double gshfl_xor(double v, int m, unsigned mask) { return __shfl_xor_sync(mask, v, m); }
+__device__ __forceinline__ float gshfl_xor(float v, int m, unsigned mask) { return __shfl_xor_sync(mask, v, m); }
+__device__ __forceinline__ cplx gshfl_xor(cplx v, int m, unsigned mask) {
+    return {__shfl_xor_sync(mask, v.x, m), __shfl_xor_sync(mask, v.y, m)};
+}
+__device__ __forceinline__ cplxf gshfl_xor(cplxf v, int m, unsigned mask) {
+    return {__shfl_xor_sync(mask, v.x, m), __shfl_xor_sync(mask, v.y, m)};
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll

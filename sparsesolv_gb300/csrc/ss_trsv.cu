@@ -123,8 +123,9 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep(int n, const int *__restri
                 const T x = wait_value(poll + c, err);
                 acc = acc + v * x;
             }
+            const unsigned gm = group_mask(G);
 #pragma unroll
-            for (int m = G / 2; m >= 1; m >>= 1) acc = acc + Sc<T>::shfl_xor(acc, m);
+            for (int m = G / 2; m >= 1; m >>= 1) acc = acc + gshfl_xor(acc, m, gm);
             if (gl == 0) {
                 // an empty row has no divisor: the result becomes inf/NaN, never an out-of-row read
                 const T dv = (e > a) ? val[dpos] : Sc<T>::zero();
