@@ -155,6 +155,14 @@ int ssg_get_kernel_stats(ssg_handle h, double *ms, long long *launches, double *
 /* kernels this library has launched in the process so far */
 long long ssg_launch_count(void);
 
+/* launch tuning (new; results do not depend on it beyond last-bit rounding) */
+#define SSG_TUNE_SWEEP_CTA_PER_SM 0  /* resident CTAs per SM claiming sweep rows (0 = default 8) */
+#define SSG_TUNE_SWEEP_GROUP 1       /* lanes per row in the sweeps: 0 auto, 4, 8, 16, 32 */
+#define SSG_TUNE_SWEEP_BACKOFF_NS 2  /* sleep between polls of an unsolved entry */
+#define SSG_TUNE_FACTOR_BACKOFF_NS 3 /* sleep between polls of an unfinished factor row */
+#define SSG_TUNE_RECIPROCAL_DIAG 4   /* 1 (default): multiply by precomputed 1/diagonal in the sweeps */
+int ssg_set_tuning(ssg_handle h, int key, int value);
+
 /* ---- hot-path pieces on their own (host buffers) ---- */
 /* IC(0) factor of the current matrix with shift alpha: L in the lower(A) pattern
  * (lrp[n+1], lci[nnzL], lval[nnzL] values) and D = 1/pivot (n values). */

@@ -26,8 +26,13 @@ EXPORTED = [
     "ssg_set_matrix_device", "ssg_solve", "ssg_solve_device", "ssg_get_residual_log", "ssg_get_iters",
     "ssg_get_accel_used", "ssg_get_timings", "ssg_factor", "ssg_apply_precond", "ssg_spmv", "ssg_level_schedule",
     "ssg_update_values", "ssg_update_values_device", "ssg_get_stream", "ssg_set_profiling", "ssg_get_kernel_stats",
-    "ssg_launch_count",
+    "ssg_launch_count", "ssg_set_tuning",
 ]
+TUNE_SWEEP_CTA_PER_SM = 0
+TUNE_SWEEP_GROUP = 1
+TUNE_SWEEP_BACKOFF_NS = 2
+TUNE_FACTOR_BACKOFF_NS = 3
+TUNE_RECIPROCAL_DIAG = 4
 KERNEL_CLASSES = ["forward sweep", "backward sweep", "spmv", "vector", "ic factor", "level schedule"]
 
 
@@ -70,6 +75,7 @@ def declare(lib):
         "ssg_set_profiling": ([H, I], I),
         "ssg_get_kernel_stats": ([H, P, P, P, I], I),
         "ssg_launch_count": ([], ctypes.c_longlong),
+        "ssg_set_tuning": ([H, I, I], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -238,6 +244,9 @@ class Handle:
         by = np.zeros(k)
         self._check(self.lib.ssg_get_kernel_stats(self.h, _p(ms), _p(la), _p(by), k), "ssg_get_kernel_stats")
         return {KERNEL_CLASSES[i]: (float(ms[i]), int(la[i]), float(by[i])) for i in range(k)}
+
+    def set_tuning(self, key, value):
+        self._check(self.lib.ssg_set_tuning(self.h, int(key), int(value)), "ssg_set_tuning")
 
     def launch_count(self):
         return int(self.lib.ssg_launch_count())

@@ -41,6 +41,10 @@ CUDA_SOURCES = [
 ]
 
 
+# the IC factor restates the reference's arithmetic operation by operation; no FMA contraction there
+EXTRA_FLAGS = {"ss_factor.cu": ["-fmad=false"]}
+
+
 def _run(cmd):
     proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if proc.returncode != 0:
@@ -79,7 +83,7 @@ def build_solver(force=False, verbose=False):
 
     def compile_one(src):
         obj = os.path.join(objdir, os.path.basename(src) + ".o")
-        out = _run(common + ["-c", src, "-o", obj])
+        out = _run(common + EXTRA_FLAGS.get(os.path.basename(src), []) + ["-c", src, "-o", obj])
         return obj, out
 
     with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:

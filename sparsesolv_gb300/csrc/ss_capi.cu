@@ -211,6 +211,35 @@ int ssg_get_kernel_stats(ssg_handle hd, double *ms, long long *launches, double 
 
 long long ssg_launch_count(void) { return ssg::launch_count(); }
 
+int ssg_set_tuning(ssg_handle hd, int key, int value) {
+    return guarded(hd, [&](Handle &h) {
+        switch (key) {
+            case SSG_TUNE_SWEEP_CTA_PER_SM:
+                if (value < 0 || value > 32) return SSG_ERR_ARG;
+                h.swcfg.cta_per_sm = value;
+                break;
+            case SSG_TUNE_SWEEP_GROUP:
+                if (value != 0 && value != 4 && value != 8 && value != 16 && value != 32) return SSG_ERR_ARG;
+                h.swcfg.group = value;
+                break;
+            case SSG_TUNE_SWEEP_BACKOFF_NS:
+                if (value < 0 || value > 100000) return SSG_ERR_ARG;
+                h.swcfg.backoff_ns = value;
+                break;
+            case SSG_TUNE_FACTOR_BACKOFF_NS:
+                if (value < 0 || value > 100000) return SSG_ERR_ARG;
+                h.fac_backoff_ns = value;
+                break;
+            case SSG_TUNE_RECIPROCAL_DIAG:
+                h.use_inv_diag = value != 0;
+                break;
+            default:
+                return SSG_ERR_ARG;
+        }
+        return SSG_OK;
+    });
+}
+
 int ssg_get_residual_log(ssg_handle hd, double *log, int cap, int *len) {
     return guarded(hd, [&](Handle &h) {
         // MatSolverBase::getResidualLog: zeros of the stored size when logging is off

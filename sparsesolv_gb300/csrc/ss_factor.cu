@@ -146,22 +146,156 @@ __global__ void __launch_bounds__(256) k_ic_factor(int n, const int *perm, const
     }
 }
 
+// ---------------------------------------------------------------- fast factor
+// Rows of at most 32 entries (every row of the voxel curl-curl matrices has 17
+// in its lower triangle): lane k owns entry k of row i. The entries are
+// finished left to right; as soon as entry kk is final, every lane jj > kk
+// subtracts its contribution L_ik L_jk D_k (when column k also appears in
+// row j) -- the same terms, subtracted in the same order, as the reference's
+// loop over kk, so with FMA contraction off (this file is compiled with
+// -fmad=false) the real factor is bit-identical to the reference's. Row j of
+// each entry is staged in shared memory once its done flag is seen; its start
+// in the level-ordered arrays comes from a per-entry table built once per
+// pattern.
+constexpr int FF_MAXROW = 32;
 template <typename T>
-void ic_factor(const Tri &L, T *lval, T *D, double alpha, int *d_err, int *d_ticket, cudaStream_t s) {
+__host__ __device__ constexpr int ff_warps() { return sizeof(T) == 8 ? 3 : 2; }  // static shared memory below 48 KB
+
+template <typename T>
+__global__ void __launch_bounds__(ff_warps<T>() * 32) k_ic_factor_fast(int n, const int *perm, const int *prp,
+                                                                       const int *pci, const int2 *dep, T *lval,
+                                                                       T *D, int *done, double alpha, int *ticket,
+                                                                       int *err, int backoff_ns) {
+    constexpr int FF_WARPS = ff_warps<T>();
+    __shared__ int s_c[FF_WARPS][FF_MAXROW][FF_MAXROW - 1];
+    __shared__ T s_v[FF_WARPS][FF_MAXROW][FF_MAXROW - 1];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(ticket, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= n) return;
+        const int i = perm[t];
+        const int a = prp[t], m = prp[t + 1] - a;
+        const bool have = lane < m;
+        const int c = have ? pci[a + lane] : INT_MAX;
+        T v = have ? lval[a + lane] : Sc<T>::zero();
+        const int last_c = __shfl_sync(0xffffffffu, c, (m - 1) & 31);
+        if (m < 1 || m > FF_MAXROW || last_c != i) {
+            // no diagonal last (src/SprsPreconditioner.cpp:88-94) or too long for this kernel
+            if (lane == 0) {
+                atomicExch(err, m > FF_MAXROW ? ERR_ROW_TOO_LONG : ERR_NO_DIAG);
+                D[i] = Sc<T>::one();
+            }
+            __syncwarp();
+            __threadfence();
+            if (lane == 0) *(volatile int *)(done + i) = 1;
+            continue;
+        }
+        const bool off = have && lane < m - 1;  // off-diagonal entry (column < i)
+        int mj = 0;
+        T dk = Sc<T>::zero();
+        if (off) {
+            const volatile int *f = done + c;
+            if (*f == 0) {
+                const unsigned long long start = gtimer();
+                int polls = 0;
+                while (*f == 0) {
+                    if (backoff_ns) __nanosleep(backoff_ns);
+                    if ((++polls & 15) == 0) {
+                        if (*(volatile int *)err) break;
+                        if (gtimer() - start > SPIN_LIMIT_NS) {
+                            atomicExch(err, ERR_TIMEOUT);
+                            break;
+                        }
+                    }
+                }
+            }
+            __threadfence();
+            dk = ldcg(D + c);
+            // row j = c without its diagonal (its last entry); the loads are independent
+            const int2 dj = dep[a + lane];  // (start, length) of row j in level order
+            mj = min(dj.y - 1, FF_MAXROW - 1);
+#pragma unroll
+            for (int l = 0; l < FF_MAXROW - 1; ++l) {
+                if (l < mj) {
+                    s_c[w][lane][l] = ldcg(pci + dj.x + l);
+                    s_v[w][lane][l] = ldcg(lval + dj.x + l);
+                }
+            }
+        }
+        __syncwarp();
+        // diagonal lane starts from alpha * a_ii (src/SprsPreconditioner.cpp:95)
+        if (lane == m - 1) v = v * Sc<T>::from(alpha);
+        int ptr = 0;
+        for (int kk = 0; kk < m - 1; ++kk) {
+            const T Lk = Sc<T>::shfl(v, kk);       // final L_ik
+            const int ck = __shfl_sync(0xffffffffu, c, kk);
+            const T Dk = Sc<T>::shfl(dk, kk);
+            if (off && lane > kk) {
+                while (ptr < mj && s_c[w][lane][ptr] < ck) ++ptr;
+                if (ptr < mj && s_c[w][lane][ptr] == ck) v = v - (Lk * s_v[w][lane][ptr]) * Dk;
+            } else if (lane == m - 1) {
+                v = v - (Lk * Lk) * Dk;
+            }
+        }
+        if (have) lval[a + lane] = v;
+        if (lane == m - 1) D[i] = (Sc<T>::absv(v) < 1.0e-12) ? Sc<T>::from(1.0 / DBL_EPSILON) : Sc<T>::one() / v;
+        __syncwarp();
+        __threadfence();
+        if (lane == 0) *(volatile int *)(done + i) = 1;
+    }
+}
+
+__global__ void k_dep_starts(int nnz, const int *pci, const int *ipos, const int *prp, int2 *dep) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnz) return;
+    const int p = ipos[pci[k]];
+    dep[k] = make_int2(prp[p], prp[p + 1] - prp[p]);
+}
+
+__global__ void k_max_rowlen(int n, const int *prp, int *out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) atomicMax(out, prp[t + 1] - prp[t]);
+}
+
+void factor_plan(const Tri &L, DBuf &dep, int &max_row, cudaStream_t s) {
+    dep.ensure(sizeof(int2) * (size_t)(L.nnz + 1));
+    max_row = 0;
     if (L.n == 0) return;
-    DBuf done;
-    done.alloc(sizeof(int) * (size_t)L.n);
-    SSG_CUDA(cudaMemsetAsync(done.p, 0, sizeof(int) * (size_t)L.n, s));
+    k_dep_starts<<<div_up(L.nnz, 256), 256, 0, s>>>(L.nnz, L.pci.as<int>(), L.ipos.as<int>(), L.prp.as<int>(),
+                                                    dep.as<int2>());
+    SSG_LAUNCHED();
+    DBuf mx;
+    mx.alloc(sizeof(int));
+    SSG_CUDA(cudaMemsetAsync(mx.p, 0, sizeof(int), s));
+    k_max_rowlen<<<div_up(L.n, 256), 256, 0, s>>>(L.n, L.prp.as<int>(), mx.as<int>());
+    SSG_LAUNCHED();
+    SSG_CUDA(cudaMemcpyAsync(&max_row, mx.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SSG_CUDA(cudaStreamSynchronize(s));
+}
+
+template <typename T>
+void ic_factor(const Tri &L, T *lval, T *D, double alpha, int *d_err, int *d_ticket, cudaStream_t s,
+               const int2 *dep, int max_row, int *done, int backoff_ns) {
+    if (L.n == 0) return;
+    SSG_CUDA(cudaMemsetAsync(done, 0, sizeof(int) * (size_t)L.n, s));
     SSG_CUDA(cudaMemsetAsync(d_ticket, 0, sizeof(int), s));
     int dev = 0, sms = 0;
     SSG_CUDA(cudaGetDevice(&dev));
     SSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int warps = min(L.n, sms * 32);
-    k_ic_factor<T><<<div_up(warps * 32, 256), 256, 0, s>>>(L.n, L.perm.as<int>(), L.ipos.as<int>(), L.prp.as<int>(),
-                                                           L.pci.as<int>(), lval, D, done.as<int>(), alpha, d_ticket,
-                                                           d_err);
+    if (dep && max_row <= FF_MAXROW) {
+        constexpr int W = ff_warps<T>();
+        const int blocks = min(div_up(L.n, W), sms * 8);
+        k_ic_factor_fast<T><<<blocks, W * 32, 0, s>>>(L.n, L.perm.as<int>(), L.prp.as<int>(), L.pci.as<int>(), dep,
+                                                      lval, D, done, alpha, d_ticket, d_err, backoff_ns);
+    } else {
+        const int warps = min(L.n, sms * 32);
+        k_ic_factor<T><<<div_up(warps * 32, 256), 256, 0, s>>>(L.n, L.perm.as<int>(), L.ipos.as<int>(),
+                                                               L.prp.as<int>(), L.pci.as<int>(), lval, D, done,
+                                                               alpha, d_ticket, d_err);
+    }
     SSG_LAUNCHED();
-    SSG_CUDA(cudaStreamSynchronize(s));
 }
 
 // ---------------------------------------------------------------- diagonal scaling
@@ -225,7 +359,8 @@ void all_pivots_positive(int n, const T *D, int *d_flag, cudaStream_t s) {
 }
 
 #define SSG_INST(T)                                                                                      \
-    template void ic_factor<T>(const Tri &, T *, T *, double, int *, int *, cudaStream_t);              \
+    template void ic_factor<T>(const Tri &, T *, T *, double, int *, int *, cudaStream_t, const int2 *, int,  \
+                               int *, int);                                                                  \
     template void diag_scaling<T>(int, const int *, const int *, const T *, const T *, T *, T *,        \
                                   cudaStream_t);                                                         \
     template void dad_values<T>(int, const int *, const int *, const T *, const T *, T *, cudaStream_t); \

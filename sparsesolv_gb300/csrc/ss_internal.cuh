@@ -74,8 +74,12 @@ template <typename T>
 void gather_values(const int *src, const T *in, T *out, int count, cudaStream_t s);
 
 // ss_factor.cu
+// per entry of L: (start, length) of its dependency row in level order; longest row
+void factor_plan(const Tri &L, DBuf &dep, int &max_row, cudaStream_t s);
+// asynchronous; done[n] is scratch the caller owns
 template <typename T>
-void ic_factor(const Tri &L, T *lval, T *D, double alpha, int *d_err, int *d_ticket, cudaStream_t s);
+void ic_factor(const Tri &L, T *lval, T *D, double alpha, int *d_err, int *d_ticket, cudaStream_t s,
+               const int2 *dep, int max_row, int *done, int backoff_ns);
 template <typename T>
 void diag_scaling(int n, const int *rp, const int *ci, const T *val, const T *b, T *d, T *bs, cudaStream_t s);
 template <typename T>
@@ -93,6 +97,14 @@ enum SweepMode : int {
 template <typename T>
 void sweep(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *D, T *out, T *out2,
            int *d_ticket, int *d_err, cudaStream_t s);
+// launch shape of the sweeps (tunable; 0 = automatic)
+struct SweepCfg {
+    int cta_per_sm = 0;   // resident CTAs per SM claiming rows (0: 8)
+    int group = 0;        // lanes per row: 4, 8, 16 or 32 (0: from the mean row length)
+    int backoff_ns = 0;   // __nanosleep between polls of an unsolved entry
+};
+template <typename T>
+void inv_diag(const Tri &tri, const T *val, T *inv, cudaStream_t s);
 
 // ss_spmv_vec.cu -- see the Krylov state there
 struct KState;

@@ -98,8 +98,9 @@ template <typename T>
 void dot_into(int n, const T *a, const T *b, double *out2, double *part, cudaStream_t s);  // out2 = a.b (2 doubles)
 template <typename T>
 void fill_sentinel_st(T *p, int n, const KState *st, cudaStream_t s);
+struct SweepCfg;
 template <typename T>
 void sweep_st(const struct Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *D, T *out, T *out2,
-              int *d_ticket, int *d_err, const KState *st, cudaStream_t s);
+              int *d_ticket, int *d_err, const KState *st, cudaStream_t s, const SweepCfg &cfg, const T *dinv);
 
 }  // namespace ssg

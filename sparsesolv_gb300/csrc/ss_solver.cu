@@ -156,6 +156,7 @@ void Handle::ensure_patterns(bool need_ltb, bool need_ub) {
         check_err("level schedule");
         nat2lev.ensure(sizeof(int) * (size_t)(nnzL + 1));
         level_positions(Lf, Lnat_rp.as<int>(), nat2lev.as<int>(), stream);
+        factor_plan(Lf, dep, max_row, stream);
         pat_version = version;
         ltb_ready = ub_ready = false;
     }
@@ -203,10 +204,14 @@ void Handle::ensure_factor(double alpha, bool scaled) {
     Lval.ensure(sizeof(T) * (size_t)(nnzL + 1));
     Ltval.ensure(sizeof(T) * (size_t)(nnzL + 1));
     Dvec.ensure(sizeof(T) * (size_t)(n + 1));
+    invL.ensure(sizeof(T) * (size_t)(n + 1));
+    done_buf.ensure(sizeof(int) * (size_t)(n + 1));
     auto factor_once = [&](double a) {
         gather_values<T>(Lf.psrc.as<int>(), aval, Lval.as<T>(), nnzL, stream);
-        timed(PC_FACTOR, 2.0 * (4.0 + sizeof(T)) * nnzL + (double)sizeof(T) * n,
-              [&] { ic_factor<T>(Lf, Lval.as<T>(), Dvec.as<T>(), a, err(), ticket() + 2, stream); });
+        timed(PC_FACTOR, 2.0 * (4.0 + sizeof(T)) * nnzL + (double)sizeof(T) * n, [&] {
+            ic_factor<T>(Lf, Lval.as<T>(), Dvec.as<T>(), a, err(), ticket() + 2, stream, dep.as<int2>(), max_row,
+                         done_buf.as<int>(), fac_backoff_ns);
+        });
         check_err("IC factorisation");
     };
     if (alpha < 0.0) {
@@ -236,6 +241,7 @@ void Handle::ensure_factor(double alpha, bool scaled) {
         alpha_used = alpha;
     }
     gather_values<T>(Ltb.psrc.as<int>(), Lval.as<T>(), Ltval.as<T>(), nnzL, stream);
+    inv_diag<T>(Lf, Lval.as<T>(), invL.as<T>(), stream);
     fac_valid = true;
     fac_version = version;
     fac_alpha_req = alpha;
@@ -251,6 +257,10 @@ void Handle::ensure_sgs() {
     Uval.ensure(sizeof(T) * (size_t)(nnzU + 1));
     gather_values<T>(Lf.psrc.as<int>(), dad.as<T>(), Cval.as<T>(), nnzL, stream);
     gather_values<T>(Ub.psrc.as<int>(), dad.as<T>(), Uval.as<T>(), nnzU, stream);
+    invC.ensure(sizeof(T) * (size_t)(n + 1));
+    invU.ensure(sizeof(T) * (size_t)(n + 1));
+    inv_diag<T>(Lf, Cval.as<T>(), invC.as<T>(), stream);
+    inv_diag<T>(Ub, Uval.as<T>(), invU.as<T>(), stream);
     sgs_valid = true;
     sgs_version = version;
 }
@@ -268,12 +278,13 @@ void Handle::apply_precond(const T *d_r, T *d_z, const KState *stp) {
     const size_t v = sizeof(T);
     timed(PC_VEC, (double)v * n, [&] { fill_sentinel_st<T>(y, n, stp, stream); });
     timed(PC_FWD, tri_bytes(Lf, v, 2), [&] {
-        sweep_st<T>(Lf, Lval.as<T>(), SW_FWD_DIV, d_r, nullptr, nullptr, y, nullptr, ticket(), err(), stp, stream);
+        sweep_st<T>(Lf, Lval.as<T>(), SW_FWD_DIV, d_r, nullptr, nullptr, y, nullptr, ticket(), err(), stp, stream,
+                    swcfg, use_inv_diag ? invL.as<T>() : nullptr);
     });
     timed(PC_VEC, (double)v * n, [&] { fill_sentinel_st<T>(d_z, n, stp, stream); });
     timed(PC_BWD, tri_bytes(Ltb, v, 3), [&] {
         sweep_st<T>(Ltb, Ltval.as<T>(), SW_BWD_IC, nullptr, y, Dvec.as<T>(), d_z, nullptr, ticket() + 1, err(), stp,
-                    stream);
+                    stream, swcfg, (const T *)nullptr);
     });
 }
 
@@ -349,7 +360,8 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
     if (sgs && n) {
         // rd = C^{-1} r (src/MatSolverMRTR_SGSver.cpp:118-132)
         fill_sentinel_st<T>(t1, n, nullptr, s);
-        sweep_st<T>(Lf, Cval.as<T>(), SW_FWD_DIV, r, nullptr, nullptr, t1, nullptr, ticket(), err(), nullptr, s);
+        sweep_st<T>(Lf, Cval.as<T>(), SW_FWD_DIV, r, nullptr, nullptr, t1, nullptr, ticket(), err(), nullptr, s, swcfg,
+                    use_inv_diag ? invC.as<T>() : nullptr);
         std::swap(r, t1);
     }
     norm2<T>(n, r, scal, part.as<double>(), s);
@@ -453,11 +465,13 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
             // u = U^{-1} rd ; ARd = u + C^{-1}(rd - u)  (src/MatSolverMRTR_SGSver.cpp:184-189)
             timed(PC_VEC, nv, [&] { fill_sentinel_st<T>(u, n, st, s); });
             timed(PC_BWD, tri_bytes(Ub, vb, 2), [&] {
-                sweep_st<T>(Ub, Uval.as<T>(), SW_BWD_DIV, r, nullptr, nullptr, u, nullptr, ticket(), err(), st, s);
+                sweep_st<T>(Ub, Uval.as<T>(), SW_BWD_DIV, r, nullptr, nullptr, u, nullptr, ticket(), err(), st, s, swcfg,
+                            use_inv_diag ? invU.as<T>() : nullptr);
             });
             timed(PC_VEC, nv, [&] { fill_sentinel_st<T>(t1, n, st, s); });
             timed(PC_FWD, tri_bytes(Lf, vb, 4), [&] {
-                sweep_st<T>(Lf, Cval.as<T>(), SW_FWD_EIS, r, u, nullptr, t1, w, ticket() + 1, err(), st, s);
+                sweep_st<T>(Lf, Cval.as<T>(), SW_FWD_EIS, r, u, nullptr, t1, w, ticket() + 1, err(), st, s, swcfg,
+                            use_inv_diag ? invC.as<T>() : nullptr);
             });
             timed(PC_VEC, 3 * nv, [&] { mrtr_dots<T>(n, st, w, r, w, y, part.as<double>(), s); });
             timed(PC_VEC, 10 * nv, [&] { mrtr_update<T>(n, st, p, u, x, y, w, r, part.as<double>(), log, false, s); });

@@ -54,9 +54,13 @@ struct Handle {
     Tri Ub;          // backward schedule over upper(A); psrc -> A entries
     bool ub_ready = false;
     DBuf nat2lev;    // natural lower entry -> position in Lf
+    DBuf dep;        // per entry of Lf: (start, length) of its dependency row
+    int max_row = 0; // longest row of Lf
+    DBuf done_buf;   // factor row flags
 
     // ---- values
     DBuf Lval, Ltval, Cval, Uval, Dvec;  // factor (Lf / Ltb layouts), SGS triangles, 1/pivot
+    DBuf invL, invC, invU;               // reciprocal diagonals (natural order) for the dividing sweeps
     bool fac_valid = false;
     uint64_t fac_version = 0;
     double fac_alpha_req = 0.0, alpha_used = 0.0;
@@ -78,6 +82,11 @@ struct Handle {
     int iters = 0;
     double t_setup_ms = 0.0, t_iter_ms = 0.0;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+
+    // launch tuning (ssg_set_tuning)
+    SweepCfg swcfg;
+    int fac_backoff_ns = 0;
+    bool use_inv_diag = true;
 
     Prof prof;
     int prof_begin(int cls);

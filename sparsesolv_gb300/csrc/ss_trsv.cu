@@ -71,12 +71,13 @@ struct Ready<cplxf> {
 };
 
 template <typename T>
-__device__ __forceinline__ T wait_value(const T *p, int *err) {
+__device__ __forceinline__ T wait_value(const T *p, int *err, int backoff_ns) {
     T v;
     if (Ready<T>::ok(p, v)) return v;
     const unsigned long long start = gtimer();
     int polls = 0;
     while (!Ready<T>::ok(p, v)) {
+        if (backoff_ns) __nanosleep(backoff_ns);
         if ((++polls & 31) == 0) {
             if (*(volatile int *)err) return Ready<T>::nan();
             if (gtimer() - start > SPIN_LIMIT_NS) {
@@ -94,7 +95,8 @@ template <typename T, int G, int MODE>
 __global__ void __launch_bounds__(SW_THREADS) k_sweep(int n, const int *__restrict__ perm, const int *__restrict__ prp,
                                                       const int *__restrict__ pci, const T *__restrict__ val,
                                                       const T *rhs, const T *aux, const T *D, T *out, T *out2,
-                                                      int *ticket, int *err, const KState *st) {
+                                                      int *ticket, int *err, const KState *st, const T *dinv,
+                                                      int backoff_ns) {
     if (st && !st->active) return;
     constexpr int ROWS = SW_THREADS / G;
     __shared__ int s_base;
@@ -120,26 +122,29 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep(int n, const int *__restri
             for (int k = ob + gl; k < oe; k += G) {
                 const int c = pci[k];
                 const T v = val[k];
-                const T x = wait_value(poll + c, err);
+                const T x = wait_value(poll + c, err, backoff_ns);
                 acc = acc + v * x;
             }
             const unsigned gm = group_mask(G);
 #pragma unroll
             for (int m = G / 2; m >= 1; m >>= 1) acc = acc + gshfl_xor(acc, m, gm);
             if (gl == 0) {
-                // an empty row has no divisor: the result becomes inf/NaN, never an out-of-row read
-                const T dv = (e > a) ? val[dpos] : Sc<T>::zero();
+                // an empty row has no divisor: the result becomes inf/NaN, never an out-of-row read.
+                // With dinv the division by the diagonal is a multiplication by its
+                // precomputed reciprocal (off the critical path; rounding within 1 ulp).
                 T res;
-                if (MODE == SW_FWD_DIV) {
-                    res = (rhs[r] - acc) / dv;
-                } else if (MODE == SW_FWD_EIS) {
-                    const T u = aux[r];
-                    res = ((rhs[r] - u) - acc) / dv;
-                    out2[r] = res + u;
-                } else if (MODE == SW_BWD_IC) {
+                if (MODE == SW_BWD_IC) {
                     res = D[r] * (Sc<T>::zero() - acc) + aux[r];
                 } else {
-                    res = (rhs[r] - acc) / dv;
+                    T num = rhs[r] - acc;
+                    T u = Sc<T>::zero();
+                    if (MODE == SW_FWD_EIS) {
+                        u = aux[r];
+                        num = (rhs[r] - u) - acc;
+                    }
+                    if (dinv) res = num * dinv[r];
+                    else res = num / ((e > a) ? val[dpos] : Sc<T>::zero());
+                    if (MODE == SW_FWD_EIS) out2[r] = res + u;
                 }
                 Ready<T>::publish(out + r, res);
             }
@@ -149,29 +154,22 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep(int n, const int *__restri
 
 template <typename T, int G>
 static void launch_sweep(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *D, T *out,
-                         T *out2, int *ticket, int *err, const KState *st, int grid, cudaStream_t s) {
+                         T *out2, int *ticket, int *err, const KState *st, int grid, const T *dinv, int backoff,
+                         cudaStream_t s) {
     const int *perm = tri.perm.as<int>(), *prp = tri.prp.as<int>(), *pci = tri.pci.as<int>();
+#define SSG_SW(M)                                                                                                 \
+    k_sweep<T, G, M><<<grid, SW_THREADS, 0, s>>>(tri.n, perm, prp, pci, val, rhs, aux, D, out, out2, ticket, err, \
+                                                 st, dinv, backoff)
     switch (mode) {
-        case SW_FWD_DIV:
-            k_sweep<T, G, SW_FWD_DIV><<<grid, SW_THREADS, 0, s>>>(tri.n, perm, prp, pci, val, rhs, aux, D, out, out2,
-                                                                  ticket, err, st);
-            break;
-        case SW_BWD_IC:
-            k_sweep<T, G, SW_BWD_IC><<<grid, SW_THREADS, 0, s>>>(tri.n, perm, prp, pci, val, rhs, aux, D, out, out2,
-                                                                 ticket, err, st);
-            break;
-        case SW_BWD_DIV:
-            k_sweep<T, G, SW_BWD_DIV><<<grid, SW_THREADS, 0, s>>>(tri.n, perm, prp, pci, val, rhs, aux, D, out, out2,
-                                                                  ticket, err, st);
-            break;
-        default:
-            k_sweep<T, G, SW_FWD_EIS><<<grid, SW_THREADS, 0, s>>>(tri.n, perm, prp, pci, val, rhs, aux, D, out, out2,
-                                                                  ticket, err, st);
-            break;
+        case SW_FWD_DIV: SSG_SW(SW_FWD_DIV); break;
+        case SW_BWD_IC: SSG_SW(SW_BWD_IC); break;
+        case SW_BWD_DIV: SSG_SW(SW_BWD_DIV); break;
+        default: SSG_SW(SW_FWD_EIS); break;
     }
+#undef SSG_SW
 }
 
-static int sweep_grid(int n, int rows_per_cta) {
+static int sweep_grid(int n, int rows_per_cta, int cta_per_sm) {
     static int sms = 0;
     if (!sms) {
         int dev = 0;
@@ -180,7 +178,8 @@ static int sweep_grid(int n, int rows_per_cta) {
         if (sms <= 0) sms = 1;
     }
     const int want = div_up(n, rows_per_cta);
-    return want < sms * 8 ? want : sms * 8;
+    const int cap = sms * (cta_per_sm > 0 ? cta_per_sm : 8);
+    return want < cap ? want : cap;
 }
 
 // group width from the mean off-diagonal count of the triangle
@@ -193,31 +192,54 @@ static int sweep_group(const Tri &tri) {
 
 template <typename T>
 void sweep_st(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *D, T *out, T *out2,
-              int *d_ticket, int *d_err, const KState *st, cudaStream_t s) {
+              int *d_ticket, int *d_err, const KState *st, cudaStream_t s, const SweepCfg &cfg, const T *dinv) {
     if (tri.n == 0) return;
     SSG_CUDA(cudaMemsetAsync(d_ticket, 0, sizeof(int), s));
-    const int G = sweep_group(tri);
-    const int grid = sweep_grid(tri.n, SW_THREADS / G);
+    const int G = cfg.group ? cfg.group : sweep_group(tri);
+    const int grid = sweep_grid(tri.n, SW_THREADS / G, cfg.cta_per_sm);
     if (G == 8)
-        launch_sweep<T, 8>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, s);
+        launch_sweep<T, 8>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, dinv, cfg.backoff_ns, s);
     else if (G == 16)
-        launch_sweep<T, 16>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, s);
+        launch_sweep<T, 16>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, dinv, cfg.backoff_ns,
+                            s);
+    else if (G == 4)
+        launch_sweep<T, 4>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, dinv, cfg.backoff_ns, s);
     else
-        launch_sweep<T, 32>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, s);
+        launch_sweep<T, 32>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, dinv, cfg.backoff_ns,
+                            s);
     SSG_LAUNCHED();
 }
 
 template <typename T>
 void sweep(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *D, T *out, T *out2,
            int *d_ticket, int *d_err, cudaStream_t s) {
-    sweep_st<T>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, nullptr, s);
+    sweep_st<T>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, nullptr, s, SweepCfg{}, nullptr);
+}
+
+// reciprocal of each row's diagonal (last entry for a forward triangle, first for a backward one)
+template <typename T>
+__global__ void k_inv_diag(int n, const int *perm, const int *prp, const T *val, int fwd, T *inv) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int a = prp[t], e = prp[t + 1];
+    const T d = (e > a) ? val[fwd ? e - 1 : a] : Sc<T>::zero();
+    inv[perm[t]] = Sc<T>::one() / d;
+}
+
+template <typename T>
+void inv_diag(const Tri &tri, const T *val, T *inv, cudaStream_t s) {
+    if (tri.n == 0) return;
+    k_inv_diag<T><<<div_up(tri.n, 256), 256, 0, s>>>(tri.n, tri.perm.as<int>(), tri.prp.as<int>(), val,
+                                                      tri.lower ? 1 : 0, inv);
+    SSG_LAUNCHED();
 }
 
 #define SSG_INST(T)                                                                                               \
     template void sweep<T>(const Tri &, const T *, int, const T *, const T *, const T *, T *, T *, int *, int *,  \
                            cudaStream_t);                                                                         \
+    template void inv_diag<T>(const Tri &, const T *, T *, cudaStream_t);                                        \
     template void sweep_st<T>(const Tri &, const T *, int, const T *, const T *, const T *, T *, T *, int *, int *, \
-                              const KState *, cudaStream_t);
+                              const KState *, cudaStream_t, const SweepCfg &, const T *);
 SSG_INST(double)
 SSG_INST(cplx)
 SSG_INST(float)

@@ -121,3 +121,16 @@ def test_factor_golden_fixture(handle, golden, golden_cases):
         assert np.array_equal(lrp, data[key + "/lrp"]) and np.array_equal(lci, data[key + "/lci"])
         assert np.allclose(lval, data[key + "/lval"], rtol=1e-9, atol=1e-12 * np.abs(lval).max())
         assert np.allclose(D, data[key + "/D"], rtol=1e-9)
+
+
+@pytest.mark.parametrize("name", ["cc8", "cfg1", "rand"])
+@pytest.mark.parametrize("alpha", [1.0, 1.1])
+def test_ic_factor_real_bit_identical(handle, oracle, name, alpha):
+    """The real factor repeats the reference's operations in the reference's
+    order without FMA contraction, so it matches the oracle (itself
+    bit-identical to the reference's IC_decomp) exactly."""
+    rp, ci, val = CASES[name]
+    handle.set_matrix(rp, ci, val)
+    _, _, lval, D = handle.factor(alpha)
+    _, _, oval, oD = oracle.ic_factor(rp, ci, val, alpha)
+    assert np.array_equal(lval, oval) and np.array_equal(D, oD)
