@@ -35,6 +35,7 @@ CUDA_SOURCES = [
     "ss_levels.cu",
     "ss_factor.cu",
     "ss_trsv.cu",
+    "ss_cluster.cu",
     "ss_spmv_vec.cu",
     "ss_solver.cu",
     "ss_capi.cu",

@@ -233,6 +233,14 @@ int ssg_set_tuning(ssg_handle hd, int key, int value) {
             case SSG_TUNE_RECIPROCAL_DIAG:
                 h.use_inv_diag = value != 0;
                 break;
+            case SSG_TUNE_SWEEP_MODE:
+                if (value < 0 || value > 2) return SSG_ERR_ARG;
+                h.sweep_mode = value;
+                break;
+            case SSG_TUNE_CLUSTER_RING_KB:
+                if (value < 4 || value > 200) return SSG_ERR_ARG;
+                h.cl_ring_bytes = value * 1024;
+                break;
             default:
                 return SSG_ERR_ARG;
         }

@@ -55,6 +55,10 @@ struct Tri {
     DBuf prp, pci, psrc;         // level-ordered CSR; psrc[k] = source value index
     std::vector<int> lptr;       // host copy of level pointers
     DBuf lptr_d;
+    // cluster sweep plan (ss_cluster.cu)
+    bool cl_ready = false;
+    int cl_C = 0, cl_S = 0, cl_elem = 0, cl_ring_bytes = 0;
+    DBuf cl_code;                // per level-ordered entry: row id, or -1 - (owner << 20 | ring slot)
 };
 
 // ss_levels.cu
@@ -105,6 +109,14 @@ struct SweepCfg {
 };
 template <typename T>
 void inv_diag(const Tri &tri, const T *val, T *inv, cudaStream_t s);
+
+// ss_cluster.cu: one-cluster level-synchronous sweeps
+int cluster_size_available();  // 16, 8 or 0
+void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBuf &tmp);
+struct KState;
+template <typename T>
+void sweep_cluster(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *D, T *out, T *out2,
+                   const T *dinv, const KState *st, int group, cudaStream_t s);
 
 // ss_spmv_vec.cu -- see the Krylov state there
 struct KState;

@@ -355,6 +355,8 @@ void build_tri(Tri &T, int n, int nnz, const int *rp, const int *ci, const int *
     T.n = n;
     T.nnz = nnz;
     T.lower = lower;
+    T.cl_ready = false;
+    T.cl_elem = 0;
     T.level.ensure(sizeof(int) * (size_t)n);
     T.perm.ensure(sizeof(int) * (size_t)n);
     T.ipos.ensure(sizeof(int) * (size_t)n);

@@ -271,11 +271,31 @@ static double tri_bytes(const Tri &T, size_t v, int vecs) {
     return (4.0 + (double)v) * T.nnz + 4.0 * (T.n + 1) + (double)vecs * (double)v * T.n;
 }
 
+bool Handle::cluster_ok(Tri &t, size_t elem) {
+    if (sweep_mode == 1 || t.n == 0) return false;
+    if (!t.cl_ready || t.cl_elem != (int)elem || t.cl_ring_bytes != cl_ring_bytes) {
+        DBuf tmp;
+        cluster_plan(t, elem, cl_ring_bytes, stream, tmp);
+    }
+    return t.cl_ready;
+}
+
 // z = (L D L^T)^{-1} r using vec[10] as the forward result
 template <typename T>
 void Handle::apply_precond(const T *d_r, T *d_z, const KState *stp) {
     T *y = vec[10].as<T>();
     const size_t v = sizeof(T);
+    if (cluster_ok(Lf, v) && cluster_ok(Ltb, v)) {
+        timed(PC_FWD, tri_bytes(Lf, v, 2), [&] {
+            sweep_cluster<T>(Lf, Lval.as<T>(), SW_FWD_DIV, d_r, nullptr, nullptr, y, nullptr,
+                             use_inv_diag ? invL.as<T>() : nullptr, stp, swcfg.group, stream);
+        });
+        timed(PC_BWD, tri_bytes(Ltb, v, 3), [&] {
+            sweep_cluster<T>(Ltb, Ltval.as<T>(), SW_BWD_IC, nullptr, y, Dvec.as<T>(), d_z, nullptr, nullptr, stp,
+                             swcfg.group, stream);
+        });
+        return;
+    }
     timed(PC_VEC, (double)v * n, [&] { fill_sentinel_st<T>(y, n, stp, stream); });
     timed(PC_FWD, tri_bytes(Lf, v, 2), [&] {
         sweep_st<T>(Lf, Lval.as<T>(), SW_FWD_DIV, d_r, nullptr, nullptr, y, nullptr, ticket(), err(), stp, stream,
@@ -359,9 +379,14 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
     }
     if (sgs && n) {
         // rd = C^{-1} r (src/MatSolverMRTR_SGSver.cpp:118-132)
-        fill_sentinel_st<T>(t1, n, nullptr, s);
-        sweep_st<T>(Lf, Cval.as<T>(), SW_FWD_DIV, r, nullptr, nullptr, t1, nullptr, ticket(), err(), nullptr, s, swcfg,
-                    use_inv_diag ? invC.as<T>() : nullptr);
+        if (cluster_ok(Lf, sizeof(T))) {
+            sweep_cluster<T>(Lf, Cval.as<T>(), SW_FWD_DIV, r, nullptr, nullptr, t1, nullptr,
+                             use_inv_diag ? invC.as<T>() : nullptr, nullptr, swcfg.group, s);
+        } else {
+            fill_sentinel_st<T>(t1, n, nullptr, s);
+            sweep_st<T>(Lf, Cval.as<T>(), SW_FWD_DIV, r, nullptr, nullptr, t1, nullptr, ticket(), err(), nullptr, s,
+                        swcfg, use_inv_diag ? invC.as<T>() : nullptr);
+        }
         std::swap(r, t1);
     }
     norm2<T>(n, r, scal, part.as<double>(), s);
@@ -441,6 +466,7 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
     const double nv = (double)vb * n;
     const double spmv_bytes = (4.0 + vb) * nnz + 4.0 * (n + 1) + 2.0 * nv;
     int iter_no = 0;
+    const bool sgs_cluster = sgs && cluster_ok(Ub, sizeof(T)) && cluster_ok(Lf, sizeof(T));
     auto one_iteration = [&]() {
         prof.iter = ++iter_no;
         prof.pre = true;
@@ -463,16 +489,27 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
             timed(PC_VEC, 5 * nv, [&] { mrtr_zu<T>(n, st, z, w, u, s); });
         } else {
             // u = U^{-1} rd ; ARd = u + C^{-1}(rd - u)  (src/MatSolverMRTR_SGSver.cpp:184-189)
-            timed(PC_VEC, nv, [&] { fill_sentinel_st<T>(u, n, st, s); });
-            timed(PC_BWD, tri_bytes(Ub, vb, 2), [&] {
-                sweep_st<T>(Ub, Uval.as<T>(), SW_BWD_DIV, r, nullptr, nullptr, u, nullptr, ticket(), err(), st, s, swcfg,
-                            use_inv_diag ? invU.as<T>() : nullptr);
-            });
-            timed(PC_VEC, nv, [&] { fill_sentinel_st<T>(t1, n, st, s); });
-            timed(PC_FWD, tri_bytes(Lf, vb, 4), [&] {
-                sweep_st<T>(Lf, Cval.as<T>(), SW_FWD_EIS, r, u, nullptr, t1, w, ticket() + 1, err(), st, s, swcfg,
-                            use_inv_diag ? invC.as<T>() : nullptr);
-            });
+            if (sgs_cluster) {
+                timed(PC_BWD, tri_bytes(Ub, vb, 2), [&] {
+                    sweep_cluster<T>(Ub, Uval.as<T>(), SW_BWD_DIV, r, nullptr, nullptr, u, nullptr,
+                                     use_inv_diag ? invU.as<T>() : nullptr, st, swcfg.group, s);
+                });
+                timed(PC_FWD, tri_bytes(Lf, vb, 4), [&] {
+                    sweep_cluster<T>(Lf, Cval.as<T>(), SW_FWD_EIS, r, u, nullptr, t1, w,
+                                     use_inv_diag ? invC.as<T>() : nullptr, st, swcfg.group, s);
+                });
+            } else {
+                timed(PC_VEC, nv, [&] { fill_sentinel_st<T>(u, n, st, s); });
+                timed(PC_BWD, tri_bytes(Ub, vb, 2), [&] {
+                    sweep_st<T>(Ub, Uval.as<T>(), SW_BWD_DIV, r, nullptr, nullptr, u, nullptr, ticket(), err(), st, s,
+                                swcfg, use_inv_diag ? invU.as<T>() : nullptr);
+                });
+                timed(PC_VEC, nv, [&] { fill_sentinel_st<T>(t1, n, st, s); });
+                timed(PC_FWD, tri_bytes(Lf, vb, 4), [&] {
+                    sweep_st<T>(Lf, Cval.as<T>(), SW_FWD_EIS, r, u, nullptr, t1, w, ticket() + 1, err(), st, s, swcfg,
+                                use_inv_diag ? invC.as<T>() : nullptr);
+                });
+            }
             timed(PC_VEC, 3 * nv, [&] { mrtr_dots<T>(n, st, w, r, w, y, part.as<double>(), s); });
             timed(PC_VEC, 10 * nv, [&] { mrtr_update<T>(n, st, p, u, x, y, w, r, part.as<double>(), log, false, s); });
             prof.pre = false;

@@ -134,3 +134,23 @@ def test_ic_factor_real_bit_identical(handle, oracle, name, alpha):
     _, _, lval, D = handle.factor(alpha)
     _, _, oval, oD = oracle.ic_factor(rp, ci, val, alpha)
     assert np.array_equal(lval, oval) and np.array_equal(D, oD)
+
+
+@pytest.mark.parametrize("name", ["cc8", "cfg1", "rand", "ec6"])
+def test_cluster_and_syncfree_sweeps_agree(handle, name):
+    """The one-cluster level-synchronous sweep and the sync-free sweep do the
+    same per-row arithmetic (same lanes, same order), so the preconditioner
+    results are identical."""
+    rp, ci, val = CASES[name]
+    handle.set_matrix(rp, ci, val)
+    handle.factor(1.1)
+    n = len(rp) - 1
+    r = np.random.default_rng(3).standard_normal(n)
+    if np.iscomplexobj(val):
+        r = r + 0.5j * np.random.default_rng(4).standard_normal(n)
+    out = {}
+    for mode in (1, 2):
+        handle.set_tuning(_capi.TUNE_SWEEP_MODE, mode)
+        out[mode] = handle.apply_precond(r)
+    handle.set_tuning(_capi.TUNE_SWEEP_MODE, 0)
+    assert np.array_equal(out[1], out[2])
