@@ -156,12 +156,12 @@ int ssg_get_kernel_stats(ssg_handle h, double *ms, long long *launches, double *
 long long ssg_launch_count(void);
 
 /* launch tuning (new; results do not depend on it beyond last-bit rounding) */
-#define SSG_TUNE_SWEEP_CTA_PER_SM 0  /* resident CTAs per SM claiming sweep rows (0 = default 8) */
+#define SSG_TUNE_SWEEP_CTA_PER_SM 0  /* resident CTAs per SM claiming sweep rows (default 2; 0 = 8) */
 #define SSG_TUNE_SWEEP_GROUP 1       /* lanes per row in the sweeps: 0 auto, 4, 8, 16, 32 */
 #define SSG_TUNE_SWEEP_BACKOFF_NS 2  /* sleep between polls of an unsolved entry */
 #define SSG_TUNE_FACTOR_BACKOFF_NS 3 /* sleep between polls of an unfinished factor row */
 #define SSG_TUNE_RECIPROCAL_DIAG 4   /* 1 (default): multiply by precomputed 1/diagonal in the sweeps */
-#define SSG_TUNE_SWEEP_MODE 5        /* 0 auto (cluster sweep when the GPU schedules it), 1 sync-free, 2 cluster */
+#define SSG_TUNE_SWEEP_MODE 5        /* 0 auto, 1 sync-free (default), 2 one-cluster level-synchronous */
 #define SSG_TUNE_CLUSTER_RING_KB 6   /* distributed shared-memory ring per CTA of the cluster sweep (KB) */
 int ssg_set_tuning(ssg_handle h, int key, int value);
 

@@ -325,7 +325,7 @@ template <typename T>
 void sweep_cluster(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *D, T *out, T *out2,
                    const T *dinv, const KState *st, int group, cudaStream_t s) {
     if (tri.n == 0) return;
-    const int G = group ? group : 16;
+    const int G = group ? group : sweep_group(tri);
     if (G == 8)
         launch_cluster<T, 8>(tri, val, mode, rhs, aux, D, out, out2, dinv, st, s);
     else if (G == 32)

@@ -103,12 +103,13 @@ void sweep(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, c
            int *d_ticket, int *d_err, cudaStream_t s);
 // launch shape of the sweeps (tunable; 0 = automatic)
 struct SweepCfg {
-    int cta_per_sm = 0;   // resident CTAs per SM claiming rows (0: 8)
+    int cta_per_sm = 2;   // resident CTAs per SM claiming rows
     int group = 0;        // lanes per row: 4, 8, 16 or 32 (0: from the mean row length)
     int backoff_ns = 0;   // __nanosleep between polls of an unsolved entry
 };
 template <typename T>
 void inv_diag(const Tri &tri, const T *val, T *inv, cudaStream_t s);
+int sweep_group(const Tri &tri);  // lanes per row from the mean row length
 
 // ss_cluster.cu: one-cluster level-synchronous sweeps
 int cluster_size_available();  // 16, 8 or 0

@@ -87,7 +87,7 @@ struct Handle {
     SweepCfg swcfg;
     int fac_backoff_ns = 0;
     bool use_inv_diag = true;
-    int sweep_mode = 0;            // 0 auto (cluster when available), 1 sync-free, 2 cluster
+    int sweep_mode = 1;            // 0 auto, 1 sync-free (default), 2 cluster
     int cl_ring_bytes = 96 * 1024; // distributed shared-memory ring per CTA
     bool cluster_ok(Tri &t, size_t elem);
 

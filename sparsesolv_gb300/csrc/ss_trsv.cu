@@ -183,7 +183,7 @@ static int sweep_grid(int n, int rows_per_cta, int cta_per_sm) {
 }
 
 // group width from the mean off-diagonal count of the triangle
-static int sweep_group(const Tri &tri) {
+int sweep_group(const Tri &tri) {
     const double mean = tri.n ? (double)(tri.nnz - tri.n) / tri.n : 0.0;
     if (mean <= 6.0) return 8;
     if (mean <= 24.0) return 16;
