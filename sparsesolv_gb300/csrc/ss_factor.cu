@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(256) k_ic_factor(int n, const int *perm, const
 // in the level-ordered arrays comes from a per-entry table built once per
 // pattern.
 constexpr int FF_MAXROW = 32;
+int factor_blocks_per_sm = 4;  // rows in flight: enough for a level, few enough not to congest L2
 template <typename T>
 __host__ __device__ constexpr int ff_warps() { return sizeof(T) == 8 ? 3 : 2; }  // static shared memory below 48 KB
 
@@ -286,7 +287,7 @@ void ic_factor(const Tri &L, T *lval, T *D, double alpha, int *d_err, int *d_tic
     SSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     if (dep && max_row <= FF_MAXROW) {
         constexpr int W = ff_warps<T>();
-        const int blocks = min(div_up(L.n, W), sms * 8);
+        const int blocks = min(div_up(L.n, W), sms * factor_blocks_per_sm);
         k_ic_factor_fast<T><<<blocks, W * 32, 0, s>>>(L.n, L.perm.as<int>(), L.prp.as<int>(), L.pci.as<int>(), dep,
                                                       lval, D, done, alpha, d_ticket, d_err, backoff_ns);
     } else {

@@ -262,6 +262,7 @@ __global__ void k_levels(int n, const int *rp, const int *ci, int lower, int *le
                         const unsigned long long start = gtimer();
                         int polls = 0;
                         while ((v = *pl) < 0) {
+                            __nanosleep(32);
                             if ((++polls & 63) == 0) {
                                 if (*(volatile int *)err) { v = 0; break; }
                                 if (gtimer() - start > SPIN_LIMIT_NS) {
@@ -369,7 +370,8 @@ void build_tri(Tri &T, int n, int nnz, const int *rp, const int *ci, const int *
         int dev = 0, sms = 0;
         SSG_CUDA(cudaGetDevice(&dev));
         SSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        const int warps = min(div_up(n, LV_ROWS_PER_TICKET), sms * 32);
+        // few enough warps that the spinning rows do not congest L2 (about one level's width in flight)
+        const int warps = min(div_up(n, LV_ROWS_PER_TICKET), sms * 4);
         k_levels<<<div_up(warps * 32, 256), 256, 0, s>>>(n, rp, ci, lower ? 1 : 0, T.level.as<int>(), ticket, nlev_d,
                                                          d_err);
         SSG_LAUNCHED();
