@@ -35,6 +35,7 @@ TUNE_FACTOR_BACKOFF_NS = 3
 TUNE_RECIPROCAL_DIAG = 4
 TUNE_SWEEP_MODE = 5
 TUNE_CLUSTER_RING_KB = 6
+TUNE_CLUSTER_GROUP = 7
 KERNEL_CLASSES = ["forward sweep", "backward sweep", "spmv", "vector", "ic factor", "level schedule"]
 
 

@@ -241,6 +241,10 @@ int ssg_set_tuning(ssg_handle hd, int key, int value) {
                 if (value < 4 || value > 200) return SSG_ERR_ARG;
                 h.cl_ring_bytes = value * 1024;
                 break;
+            case SSG_TUNE_CLUSTER_GROUP:
+                if (value != 4 && value != 8 && value != 16 && value != 32) return SSG_ERR_ARG;
+                h.cl_group = value;
+                break;
             default:
                 return SSG_ERR_ARG;
         }

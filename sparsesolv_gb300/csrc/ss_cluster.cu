@@ -2,21 +2,30 @@
 // cluster, with recent results exchanged through distributed shared memory.
 //
 // The sync-free sweep (ss_trsv.cu) pays several L2 round trips per dependency
-// level (publish, poll, gather). Here one cluster of C CTAs (C = 16 where the
-// GPU allows non-portable cluster sizes, else 8) runs the whole sweep:
-//   for each level l:  every CTA solves its contiguous share of the level's
-//                      rows, writes each result to the output vector in HBM
-//                      and to its own shared-memory ring; then all CTAs meet
-//                      at a cluster barrier (release / acquire).
-// A dependency produced within the last few levels is read from the
-// producing CTA's ring with ld.shared::cluster; older ones from L2. Which of
-// the two applies, and the (CTA, slot) of a ring entry, are integer facts of
-// the pattern computed once (ClusterPlan): entry k of the level-ordered
-// triangle carries code[k] = j (read out[j] from memory) or
-// -1 - (owner << 20 | slot). A slot is only used when no later value of the
-// owner can have overwritten it before the consumer's level ends.
-// There is no spin-wait at all: the only waits are cluster barriers, which
-// every CTA reaches the same number of times.
+// level (publish, poll, gather): about 2.8 us per level on GB300. Here one
+// cluster of C CTAs (16 where non-portable cluster sizes are allowed, else 8)
+// runs the whole sweep, one cluster barrier per level:
+//
+//   compute warps   solve their share of level l (a contiguous run of the
+//                   level-ordered rows), reading each dependency either from
+//                   the producing CTA's shared-memory ring (ld.shared::cluster)
+//                   or, when it is older than the ring holds, from L2; they
+//                   write results only to their own ring, so their
+//                   barrier.cluster.arrive.release has no global store to wait for;
+//                   then they stage level l+3's matrix span and level l+2's
+//                   gathered inputs with cp.async while the barrier completes.
+//   store warp      copies level l's results from the ring to the output
+//                   vector in HBM; it arrives relaxed, except at every K-th
+//                   level, where its release (issued before that level's stores)
+//                   publishes everything it stored earlier.
+//
+// Which source serves each dependency is decided once per pattern (cluster_plan):
+// the ring when its slot cannot have been overwritten before the consumer's
+// level ends, memory when a release covering the value precedes the
+// consumer's level. An entry that satisfies neither makes the plan infeasible
+// and the sync-free sweep is used. There is no spin-wait: the only waits are
+// cp.async completion, CTA barriers and cluster barriers, reached the same
+// number of times by every thread.
 #include <algorithm>
 
 #include "ss_internal.cuh"
@@ -24,8 +33,10 @@
 
 namespace ssg {
 
-constexpr int CL_THREADS = 512;
 constexpr int CL_SLOT_BITS = 20;
+constexpr int CL_STORE_K = 8;   // store warp releases every K levels
+constexpr int CL_SPAN_BUFS = 4; // matrix span staged 3 levels ahead
+constexpr int CL_GATH_BUFS = 3; // gathered inputs staged 2 levels ahead
 
 __device__ __forceinline__ unsigned cluster_rank() {
     unsigned r;
@@ -40,6 +51,9 @@ __device__ __forceinline__ unsigned cluster_size() {
 __device__ __forceinline__ void cluster_arrive_release() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
 }
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+    asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
+}
 __device__ __forceinline__ void cluster_wait_acquire() {
     asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
 }
@@ -48,45 +62,47 @@ __device__ __forceinline__ unsigned map_shared(unsigned local_addr, unsigned ran
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local_addr), "r"(rank));
     return r;
 }
+__device__ __forceinline__ void bar_arrive(int id, int count) {
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void bar_sync(int id, int count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+template <int BYTES>
+__device__ __forceinline__ void cp_async(unsigned dst, const void *src) {
+    if (BYTES == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(dst), "l"(src), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 template <typename T>
 __device__ __forceinline__ T ld_dsmem(unsigned addr);
 template <>
 __device__ __forceinline__ double ld_dsmem<double>(unsigned addr) {
     double v;
-    asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
+    asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr));
     return v;
 }
 template <>
 __device__ __forceinline__ float ld_dsmem<float>(unsigned addr) {
     float v;
-    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr) : "memory");
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr));
     return v;
 }
 template <>
 __device__ __forceinline__ cplx ld_dsmem<cplx>(unsigned addr) {
     cplx v;
-    asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "r"(addr) : "memory");
+    asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "r"(addr));
     return v;
 }
 template <>
 __device__ __forceinline__ cplxf ld_dsmem<cplxf>(unsigned addr) {
     cplxf v;
-    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr) : "memory");
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
     return v;
-}
-template <typename T>
-__device__ __forceinline__ T ld_ro(const T *p) {
-    return __ldg(p);
-}
-template <>
-__device__ __forceinline__ cplx ld_ro<cplx>(const cplx *p) {
-    const double2 v = __ldg((const double2 *)p);
-    return {v.x, v.y};
-}
-template <>
-__device__ __forceinline__ cplxf ld_ro<cplxf>(const cplxf *p) {
-    const float2 v = __ldg((const float2 *)p);
-    return {v.x, v.y};
 }
 template <typename T>
 __device__ __forceinline__ T ld_l2(const T *p) {
@@ -103,73 +119,209 @@ __device__ __forceinline__ cplxf ld_l2<cplxf>(const cplxf *p) {
     return {v.x, v.y};
 }
 
+// shared-memory carve-up, identical on host and device
+struct ClLayout {
+    int S;      // ring slots (values)
+    int cap_r;  // rows of the largest per-CTA chunk of a level
+    int cap_e;  // entries of the largest per-CTA chunk of a level
+    int ring2;  // second ring for the fused Eisenstat output (0/1)
+    int ngath;  // gathered per-row inputs (1 or 2)
+    // byte offsets
+    int o_ring, o_ring2, o_span, span_bytes, o_codes, o_vals, o_prp, o_perm, o_lvec, o_gath, gath_bytes, total;
+};
+
+__host__ __device__ inline int al16(int x) { return (x + 15) & ~15; }
+
+__host__ __device__ inline ClLayout cl_layout(int S, int cap_r, int cap_e, int elem, int ring2, int ngath) {
+    ClLayout L;
+    L.S = S;
+    L.cap_r = cap_r;
+    L.cap_e = cap_e;
+    L.ring2 = ring2;
+    L.ngath = ngath;
+    int o = 0;
+    L.o_ring = o;
+    o += al16(S * elem);
+    L.o_ring2 = o;
+    if (ring2) o += al16(S * elem);
+    L.o_span = o;
+    int so = 0;
+    L.o_codes = so;
+    so += al16(cap_e * 4);
+    L.o_vals = so;
+    so += al16(cap_e * elem);
+    L.o_prp = so;
+    so += al16((cap_r + 1) * 4);
+    L.o_perm = so;
+    so += al16(cap_r * 4);
+    L.o_lvec = so;
+    so += al16(cap_r * elem);
+    L.span_bytes = so;
+    o += CL_SPAN_BUFS * so;
+    L.o_gath = o;
+    L.gath_bytes = al16(cap_r * elem * ngath);
+    o += CL_GATH_BUFS * L.gath_bytes;
+    L.total = o;
+    return L;
+}
+
 template <typename T, int G, int MODE>
-__global__ void __launch_bounds__(CL_THREADS) k_sweep_cluster(int nlev, const int *__restrict__ lptr,
-                                                              const int *__restrict__ perm,
-                                                              const int *__restrict__ prp,
-                                                              const int *__restrict__ code,
-                                                              const T *__restrict__ val, const T *rhs, const T *aux,
-                                                              const T *D, T *out, T *out2, const T *dinv,
-                                                              const KState *st, int ring_cap) {
+__global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, const int *__restrict__ lptr,
+                                                        const int *__restrict__ perm, const int *__restrict__ prp,
+                                                        const int *__restrict__ code, const T *__restrict__ val,
+                                                        const T *__restrict__ lvec, const T *rhs, const T *aux, T *out,
+                                                        T *out2, const KState *st, ClLayout Lay) {
     if (st && !st->active) return;  // uniform across the cluster
     extern __shared__ __align__(16) unsigned char cl_smem[];
-    T *ring = (T *)cl_smem;
-    const unsigned ring_base = (unsigned)__cvta_generic_to_shared(ring);
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(cl_smem);
+    T *ring = (T *)(cl_smem + Lay.o_ring);
+    T *ring2 = (T *)(cl_smem + Lay.o_ring2);
     const int C = (int)cluster_size();
     const int rank = (int)cluster_rank();
-    constexpr int NG = CL_THREADS / G;
-    const int g = threadIdx.x / G, gl = threadIdx.x % G;
-    const unsigned gm = group_mask(G);
-    const bool fwd = (MODE == SW_FWD_DIV || MODE == SW_FWD_EIS);
-    int produced = 0;  // values this CTA has written to its ring so far
-    for (int l = 0; l < nlev; ++l) {
+    const int tid = threadIdx.x;
+    const bool is_store = tid >= ncomp;
+    const int nthreads = blockDim.x;
+    const int NG = ncomp / G;
+    const int g = tid / G, gl = tid % G;
+    constexpr bool fwd = (MODE == SW_FWD_DIV || MODE == SW_FWD_EIS);
+    constexpr bool eis = (MODE == SW_FWD_EIS);
+    constexpr int VB = (int)sizeof(T);
+
+    auto chunk_of = [&](int l, int &rs, int &re) {
         const int L0 = __ldg(lptr + l), L1 = __ldg(lptr + l + 1);
         const int chunk = (L1 - L0 + C - 1) / C;
-        const int rs = min(L0 + rank * chunk, L1), re = min(rs + chunk, L1);
-        for (int t = rs + g; t < re; t += NG) {
-            const int r = __ldg(perm + t);
-            const int a = __ldg(prp + t), e = __ldg(prp + t + 1);
-            const int ob = fwd ? a : a + 1;
-            const int oe = fwd ? (e > a ? e - 1 : a) : e;
-            T acc = Sc<T>::zero();
-#pragma unroll 2
-            for (int k = ob + gl; k < oe; k += G) {
-                const int cd = __ldg(code + k);
-                const T v = ld_ro(val + k);
-                T x;
-                if (cd >= 0) {
-                    x = ld_l2(out + cd);
-                } else {
-                    const int s = -1 - cd;
-                    x = ld_dsmem<T>(map_shared(ring_base + (unsigned)((s & ((1 << CL_SLOT_BITS) - 1)) * sizeof(T)),
-                                               (unsigned)(s >> CL_SLOT_BITS)));
-                }
-                acc = acc + v * x;
-            }
-#pragma unroll
-            for (int m = G / 2; m >= 1; m >>= 1) acc = acc + gshfl_xor(acc, m, gm);
-            if (gl == 0) {
-                T res;
-                if (MODE == SW_BWD_IC) {
-                    res = D[r] * (Sc<T>::zero() - acc) + aux[r];
-                } else {
-                    T num = rhs[r] - acc;
-                    T u = Sc<T>::zero();
-                    if (MODE == SW_FWD_EIS) {
-                        u = aux[r];
-                        num = (rhs[r] - u) - acc;
-                    }
-                    if (dinv) res = num * dinv[r];
-                    else res = num / ((e > a) ? val[fwd ? e - 1 : a] : Sc<T>::zero());
-                    if (MODE == SW_FWD_EIS) out2[r] = res + u;
-                }
-                out[r] = res;
-                ring[(produced + (t - rs)) % ring_cap] = res;
+        rs = min(L0 + rank * chunk, L1);
+        re = min(rs + chunk, L1);
+    };
+    auto span_base = [&](int l) { return Lay.o_span + (l % CL_SPAN_BUFS) * Lay.span_bytes; };
+    auto gath_base = [&](int l) { return Lay.o_gath + (l % CL_GATH_BUFS) * Lay.gath_bytes; };
+    // stage the matrix span of level l: entry codes and values, row pointers, row ids, per-row vector
+    auto stage_span = [&](int l) {
+        if (l >= nlev || is_store) return;
+        int rs, re;
+        chunk_of(l, rs, re);
+        const int cnt = re - rs;
+        if (cnt <= 0) return;
+        const int e0 = __ldg(prp + rs), e1 = __ldg(prp + re);
+        const int sb = span_base(l);
+        for (int i = tid; i < e1 - e0; i += ncomp) {
+            cp_async<4>(sbase + sb + Lay.o_codes + 4 * i, code + e0 + i);
+            cp_async<VB>(sbase + sb + Lay.o_vals + VB * i, val + e0 + i);
+        }
+        for (int i = tid; i <= cnt; i += ncomp) cp_async<4>(sbase + sb + Lay.o_prp + 4 * i, prp + rs + i);
+        for (int i = tid; i < cnt; i += ncomp) {
+            cp_async<4>(sbase + sb + Lay.o_perm + 4 * i, perm + rs + i);
+            if (lvec) cp_async<VB>(sbase + sb + Lay.o_lvec + VB * i, lvec + rs + i);
+        }
+    };
+    // gather level l's per-row inputs (rhs and/or aux by row id); its span must be staged
+    auto stage_gath = [&](int l) {
+        if (l >= nlev || is_store) return;
+        int rs, re;
+        chunk_of(l, rs, re);
+        const int cnt = re - rs;
+        const int *sperm = (const int *)(cl_smem + span_base(l) + Lay.o_perm);
+        const int gb = gath_base(l);
+        for (int i = tid; i < cnt; i += ncomp) {
+            const int r = sperm[i];
+            if (MODE == SW_BWD_IC) {
+                cp_async<VB>(sbase + gb + VB * i, aux + r);
+            } else {
+                cp_async<VB>(sbase + gb + VB * i, rhs + r);
+                if (eis) cp_async<VB>(sbase + gb + VB * (Lay.cap_r + i), aux + r);
             }
         }
-        produced += re - rs;
-        cluster_arrive_release();
-        cluster_wait_acquire();
+    };
+
+    // prologue: spans of levels 0..2, then gathers of levels 0..1
+    stage_span(0);
+    stage_span(1);
+    stage_span(2);
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+    stage_gath(0);
+    stage_gath(1);
+    cp_async_commit();
+
+    int produced = 0;  // values this CTA has written to its ring so far
+    for (int l = 0; l < nlev; ++l) {
+        // A: everything staged for levels <= l+2 has landed and is visible CTA-wide
+        cp_async_wait_all();
+        __syncthreads();
+        int rs, re;
+        chunk_of(l, rs, re);
+        const int cnt = re - rs;
+        const unsigned char *sp = cl_smem + span_base(l);
+        const int *scode = (const int *)(sp + Lay.o_codes);
+        const T *sval = (const T *)(sp + Lay.o_vals);
+        const int *sprp = (const int *)(sp + Lay.o_prp);
+        const int *sperm = (const int *)(sp + Lay.o_perm);
+        const T *slvec = (const T *)(sp + Lay.o_lvec);
+        const T *sg = (const T *)(cl_smem + gath_base(l));
+        if (!is_store) {
+            // B: solve the rows of this level
+            const unsigned gm = group_mask(G);
+            const int base_e = cnt > 0 ? sprp[0] : 0;
+            for (int q = g; q < cnt; q += NG) {
+                const int a = sprp[q] - base_e, e = sprp[q + 1] - base_e;
+                const int ob = fwd ? a : a + 1;
+                const int oe = fwd ? (e > a ? e - 1 : a) : e;
+                T acc = Sc<T>::zero();
+                for (int k = ob + gl; k < oe; k += G) {
+                    const int cd = scode[k];
+                    T x;
+                    if (cd >= 0) {
+                        x = ld_l2(out + cd);
+                    } else {
+                        const int sl = -1 - cd;
+                        x = ld_dsmem<T>(map_shared(
+                            sbase + Lay.o_ring + (unsigned)((sl & ((1 << CL_SLOT_BITS) - 1)) * VB),
+                            (unsigned)(sl >> CL_SLOT_BITS)));
+                    }
+                    acc = acc + sval[k] * x;
+                }
+#pragma unroll
+                for (int m = G / 2; m >= 1; m >>= 1) acc = acc + gshfl_xor(acc, m, gm);
+                if (gl == 0) {
+                    T res;
+                    if (MODE == SW_BWD_IC) {
+                        res = slvec[q] * (Sc<T>::zero() - acc) + sg[q];
+                    } else {
+                        T num = sg[q] - acc;
+                        T u = Sc<T>::zero();
+                        if (eis) {
+                            u = sg[Lay.cap_r + q];
+                            num = (sg[q] - u) - acc;
+                        }
+                        if (lvec) res = num * slvec[q];
+                        else res = num / ((e > a) ? sval[fwd ? e - 1 : a] : Sc<T>::zero());
+                        if (eis) ring2[(produced + q) % Lay.S] = res + u;
+                    }
+                    ring[(produced + q) % Lay.S] = res;
+                }
+            }
+            // results are in the ring: let the store warp copy them out
+            bar_arrive(1, nthreads);
+            cluster_arrive_release();
+            // C: stage the span of level l+3 and the gathers of level l+2 while the barrier completes
+            stage_span(l + 3);
+            stage_gath(l + 2);
+            cp_async_commit();
+            cluster_wait_acquire();
+        } else {
+            bar_sync(1, nthreads);
+            // release at every K-th level publishes the stores of the earlier levels
+            if (l % CL_STORE_K == 0) cluster_arrive_release();
+            else cluster_arrive_relaxed();
+            for (int i = tid - ncomp; i < cnt; i += nthreads - ncomp) {
+                const int r = sperm[i];
+                out[r] = ring[(produced + i) % Lay.S];
+                if (eis) out2[r] = ring2[(produced + i) % Lay.S];
+            }
+            cluster_wait_acquire();
+        }
+        produced += cnt;
     }
 }
 
@@ -188,29 +340,41 @@ __global__ void k_cl_positions(int n, const int *perm, const int *level, const i
     ord[p] = (l > 0 ? end_ord[(l - 1) * C + c] : 0) + (off - c * chunk);
 }
 
-// per entry: ring (owner, slot) when still resident during the consumer's level, else the row id
+// per entry: ring (owner, slot) when still resident, memory index when published, else infeasible
 __global__ void k_cl_codes(int n, const int *perm, const int *level, const int *prp, const int *pci, const int *ipos,
-                           const unsigned char *owner, const int *ord, const int *end_ord, int C, int S,
-                           int *code) {
+                           const unsigned char *owner, const int *ord, const int *end_ord, int C, int S, int K,
+                           int *code, int *infeasible) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int lt = level[perm[t]];
     for (int k = prp[t]; k < prp[t + 1]; ++k) {
         const int j = pci[k];
+        const int lj = level[j];
+        if (lj >= lt) {  // the row itself (diagonal): never read as a dependency
+            code[k] = j;
+            continue;
+        }
         const int p = ipos[j];
         const int c = owner[p];
         const int o = ord[p];
-        const int written = end_ord[lt * C + c];  // values of c written by the end of level lt
-        code[k] = (level[j] < lt && written - o <= S) ? -1 - ((c << CL_SLOT_BITS) | (o % S)) : j;
+        const int written = end_ord[lt * C + c];  // values of c in its ring by the end of level lt
+        // the first release covering the stores of level lj: the arrive of the
+        // first level after lj that is a multiple of K; seen by levels after it
+        const int rel = (lj / K + 1) * K;
+        if (written - o <= S) code[k] = -1 - ((c << CL_SLOT_BITS) | (o % S));
+        else if (rel <= lt - 1) code[k] = j;
+        else {
+            code[k] = j;
+            atomicExch(infeasible, 1);
+        }
     }
 }
 
 static int g_cluster_size = -1;
 
-// largest cluster the device schedules for this kernel shape (16 or 8), 0 if none
 template <typename T>
 static int probe_cluster(int smem) {
-    auto kern = k_sweep_cluster<T, 16, SW_FWD_DIV>;
+    auto kern = k_sweep_cluster<T, 4, SW_FWD_DIV>;
     for (int C : {16, 8}) {
         if (C > 8) {
             if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
@@ -224,7 +388,7 @@ static int probe_cluster(int smem) {
         }
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(C);
-        cfg.blockDim = dim3(CL_THREADS);
+        cfg.blockDim = dim3(544);
         cfg.dynamicSmemBytes = smem;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
@@ -240,55 +404,95 @@ static int probe_cluster(int smem) {
     return 0;
 }
 
+constexpr int CL_SMEM_MAX = 220 * 1024;
+
+int cluster_size_available() {
+    if (g_cluster_size < 0) g_cluster_size = probe_cluster<double>(CL_SMEM_MAX);
+    return g_cluster_size;
+}
+
 void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBuf &tmp) {
+    (void)tmp;
     T.cl_ready = false;
     if (T.n == 0) return;
-    if (g_cluster_size < 0) g_cluster_size = probe_cluster<double>(ring_bytes);
-    const int C = g_cluster_size;
+    const int C = cluster_size_available();
     if (C <= 0) return;
     const int nlev = T.nlev;
-    const int S = ring_bytes / (int)elem_bytes;
-    // end_ord[l][c]: values CTA c has produced by the end of level l
+    // end_ord[l][c]: values CTA c has produced by the end of level l; the largest chunk
     std::vector<int> end_ord((size_t)nlev * C);
     std::vector<int> run(C, 0);
+    int cap_r = 1;
     for (int l = 0; l < nlev; ++l) {
         const int L0 = T.lptr[l], L1 = T.lptr[l + 1];
         const int chunk = (L1 - L0 + C - 1) / C;
+        cap_r = std::max(cap_r, chunk);
         for (int c = 0; c < C; ++c) {
             const int rs = std::min(L0 + c * chunk, L1), re = std::min(rs + chunk, L1);
             run[c] += re - rs;
             end_ord[(size_t)l * C + c] = run[c];
         }
     }
-    DBuf eo, owner, ord;
+    // largest entry span of a chunk (needs the row pointers)
+    std::vector<int> prp(T.n + 1);
+    SSG_CUDA(cudaMemcpyAsync(prp.data(), T.prp.p, sizeof(int) * (size_t)(T.n + 1), cudaMemcpyDeviceToHost, s));
+    SSG_CUDA(cudaStreamSynchronize(s));
+    int cap_e = 1;
+    for (int l = 0; l < nlev; ++l) {
+        const int L0 = T.lptr[l], L1 = T.lptr[l + 1];
+        const int chunk = (L1 - L0 + C - 1) / C;
+        for (int c = 0; c < C; ++c) {
+            const int rs = std::min(L0 + c * chunk, L1), re = std::min(rs + chunk, L1);
+            cap_e = std::max(cap_e, prp[re] - prp[rs]);
+        }
+    }
+    const int elem = (int)elem_bytes;
+    // sized for the fused Eisenstat sweep (second ring, two gathered inputs), the largest mode
+    const ClLayout lay = cl_layout(ring_bytes / elem, cap_r, cap_e, elem, 1, 2);
+    if (lay.total > CL_SMEM_MAX || lay.S >= (1 << CL_SLOT_BITS)) return;  // sync-free sweep instead
+    const int S = lay.S;
+    DBuf eo, owner, ord, inf;
     eo.alloc(sizeof(int) * end_ord.size());
     SSG_CUDA(cudaMemcpyAsync(eo.p, end_ord.data(), sizeof(int) * end_ord.size(), cudaMemcpyHostToDevice, s));
     owner.alloc((size_t)T.n);
     ord.alloc(sizeof(int) * (size_t)T.n);
+    inf.alloc(sizeof(int));
+    SSG_CUDA(cudaMemsetAsync(inf.p, 0, sizeof(int), s));
     k_cl_positions<<<div_up(T.n, 256), 256, 0, s>>>(T.n, T.perm.as<int>(), T.level.as<int>(), T.lptr_d.as<int>(),
                                                    eo.as<int>(), C, owner.as<unsigned char>(), ord.as<int>());
     SSG_LAUNCHED();
     T.cl_code.ensure(sizeof(int) * (size_t)(T.nnz + 1));
     k_cl_codes<<<div_up(T.n, 256), 256, 0, s>>>(T.n, T.perm.as<int>(), T.level.as<int>(), T.prp.as<int>(),
                                                 T.pci.as<int>(), T.ipos.as<int>(), owner.as<unsigned char>(),
-                                                ord.as<int>(), eo.as<int>(), C, S, T.cl_code.as<int>());
+                                                ord.as<int>(), eo.as<int>(), C, S, CL_STORE_K, T.cl_code.as<int>(),
+                                                inf.as<int>());
     SSG_LAUNCHED();
+    int infeasible = 0;
+    SSG_CUDA(cudaMemcpyAsync(&infeasible, inf.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     SSG_CUDA(cudaStreamSynchronize(s));
+    if (infeasible) return;
     T.cl_C = C;
     T.cl_S = S;
-    T.cl_elem = (int)elem_bytes;
+    T.cl_elem = elem;
     T.cl_ring_bytes = ring_bytes;
+    T.cl_cap_r = cap_r;
+    T.cl_cap_e = cap_e;
     T.cl_ready = true;
-    (void)tmp;
 }
 
 template <typename T, int G>
-static void launch_cluster(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *D, T *out,
-                           T *out2, const T *dinv, const KState *st, cudaStream_t s) {
+static void launch_cluster(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *lvec, T *out,
+                           T *out2, const KState *st, cudaStream_t s) {
+    const int elem = (int)sizeof(T);
+    const ClLayout lay = cl_layout(tri.cl_S, tri.cl_cap_r, tri.cl_cap_e, elem, mode == SW_FWD_EIS ? 1 : 0,
+                                   mode == SW_FWD_EIS ? 2 : 1);
+    // compute threads: enough groups for the widest chunk, 64..512, plus one store warp
+    int ncomp = std::min(512, std::max(64, ((tri.cl_cap_r * G + 31) / 32) * 32));
+    ncomp = (ncomp / G) * G;
+    const int nthreads = ncomp + 32;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(tri.cl_C);
-    cfg.blockDim = dim3(CL_THREADS);
-    cfg.dynamicSmemBytes = tri.cl_ring_bytes;
+    cfg.blockDim = dim3(nthreads);
+    cfg.dynamicSmemBytes = lay.total;
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -299,18 +503,18 @@ static void launch_cluster(const Tri &tri, const T *val, int mode, const T *rhs,
     cfg.numAttrs = 1;
     const int *lp = tri.lptr_d.as<int>(), *pm = tri.perm.as<int>(), *pr = tri.prp.as<int>(),
               *cd = tri.cl_code.as<int>();
-    const int ring_cap = tri.cl_S;
-#define SSG_CL(M)                                                                                       \
-    do {                                                                                                \
-        auto kern = k_sweep_cluster<T, G, M>;                                                           \
-        static int prepared_bytes = -1;                                                                 \
-        if (prepared_bytes != tri.cl_ring_bytes) {                                                      \
-            if (tri.cl_C > 8) SSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1)); \
-            SSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, tri.cl_ring_bytes)); \
-            prepared_bytes = tri.cl_ring_bytes;                                                         \
-        }                                                                                               \
-        SSG_CUDA(cudaLaunchKernelEx(&cfg, kern, tri.nlev, lp, pm, pr, cd, val, rhs, aux, D, out, out2, dinv, st, \
-                                    ring_cap));                                                         \
+#define SSG_CL(M)                                                                                                \
+    do {                                                                                                         \
+        auto kern = k_sweep_cluster<T, G, M>;                                                                    \
+        static bool prepared = false;                                                                            \
+        if (!prepared) {                                                                                         \
+            if (tri.cl_C > 8)                                                                                    \
+                SSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));         \
+            SSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, CL_SMEM_MAX));      \
+            prepared = true;                                                                                     \
+        }                                                                                                        \
+        SSG_CUDA(cudaLaunchKernelEx(&cfg, kern, tri.nlev, ncomp, lp, pm, pr, cd, val, lvec, rhs, aux, out, out2, \
+                                    st, lay));                                                                   \
     } while (0)
     switch (mode) {
         case SW_FWD_DIV: SSG_CL(SW_FWD_DIV); break;
@@ -322,29 +526,24 @@ static void launch_cluster(const Tri &tri, const T *val, int mode, const T *rhs,
 }
 
 template <typename T>
-void sweep_cluster(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *D, T *out, T *out2,
-                   const T *dinv, const KState *st, int group, cudaStream_t s) {
+void sweep_cluster(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *lvec, T *out, T *out2,
+                   const KState *st, int group, cudaStream_t s) {
     if (tri.n == 0) return;
     const int G = group ? group : sweep_group(tri);
     if (G == 8)
-        launch_cluster<T, 8>(tri, val, mode, rhs, aux, D, out, out2, dinv, st, s);
+        launch_cluster<T, 8>(tri, val, mode, rhs, aux, lvec, out, out2, st, s);
+    else if (G == 16)
+        launch_cluster<T, 16>(tri, val, mode, rhs, aux, lvec, out, out2, st, s);
     else if (G == 32)
-        launch_cluster<T, 32>(tri, val, mode, rhs, aux, D, out, out2, dinv, st, s);
-    else if (G == 4)
-        launch_cluster<T, 4>(tri, val, mode, rhs, aux, D, out, out2, dinv, st, s);
+        launch_cluster<T, 32>(tri, val, mode, rhs, aux, lvec, out, out2, st, s);
     else
-        launch_cluster<T, 16>(tri, val, mode, rhs, aux, D, out, out2, dinv, st, s);
+        launch_cluster<T, 4>(tri, val, mode, rhs, aux, lvec, out, out2, st, s);
     SSG_LAUNCHED();
 }
 
-int cluster_size_available() {
-    if (g_cluster_size < 0) g_cluster_size = probe_cluster<double>(96 * 1024);
-    return g_cluster_size;
-}
-
-#define SSG_INST(T)                                                                                              \
-    template void sweep_cluster<T>(const Tri &, const T *, int, const T *, const T *, const T *, T *, T *,       \
-                                   const T *, const KState *, int, cudaStream_t);
+#define SSG_INST(T)                                                                                        \
+    template void sweep_cluster<T>(const Tri &, const T *, int, const T *, const T *, const T *, T *, T *, \
+                                   const KState *, int, cudaStream_t);
 SSG_INST(double)
 SSG_INST(cplx)
 SSG_INST(float)

@@ -57,7 +57,7 @@ struct Tri {
     DBuf lptr_d;
     // cluster sweep plan (ss_cluster.cu)
     bool cl_ready = false;
-    int cl_C = 0, cl_S = 0, cl_elem = 0, cl_ring_bytes = 0;
+    int cl_C = 0, cl_S = 0, cl_elem = 0, cl_ring_bytes = 0, cl_cap_r = 0, cl_cap_e = 0;
     DBuf cl_code;                // per level-ordered entry: row id, or -1 - (owner << 20 | ring slot)
 };
 
@@ -115,9 +115,10 @@ int sweep_group(const Tri &tri);  // lanes per row from the mean row length
 int cluster_size_available();  // 16, 8 or 0
 void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBuf &tmp);
 struct KState;
+// lvec: per-row vector in this triangle's level order (1/diagonal, or D for SW_BWD_IC)
 template <typename T>
-void sweep_cluster(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *D, T *out, T *out2,
-                   const T *dinv, const KState *st, int group, cudaStream_t s);
+void sweep_cluster(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *lvec, T *out, T *out2,
+                   const KState *st, int group, cudaStream_t s);
 
 // ss_spmv_vec.cu -- see the Krylov state there
 struct KState;

@@ -242,6 +242,10 @@ void Handle::ensure_factor(double alpha, bool scaled) {
     }
     gather_values<T>(Ltb.psrc.as<int>(), Lval.as<T>(), Ltval.as<T>(), nnzL, stream);
     inv_diag<T>(Lf, Lval.as<T>(), invL.as<T>(), stream);
+    invL_lev.ensure(sizeof(T) * (size_t)(n + 1));
+    D_lev.ensure(sizeof(T) * (size_t)(n + 1));
+    gather_values<T>(Lf.perm.as<int>(), invL.as<T>(), invL_lev.as<T>(), n, stream);
+    gather_values<T>(Ltb.perm.as<int>(), Dvec.as<T>(), D_lev.as<T>(), n, stream);
     fac_valid = true;
     fac_version = version;
     fac_alpha_req = alpha;
@@ -261,6 +265,10 @@ void Handle::ensure_sgs() {
     invU.ensure(sizeof(T) * (size_t)(n + 1));
     inv_diag<T>(Lf, Cval.as<T>(), invC.as<T>(), stream);
     inv_diag<T>(Ub, Uval.as<T>(), invU.as<T>(), stream);
+    invC_lev.ensure(sizeof(T) * (size_t)(n + 1));
+    invU_lev.ensure(sizeof(T) * (size_t)(n + 1));
+    gather_values<T>(Lf.perm.as<int>(), invC.as<T>(), invC_lev.as<T>(), n, stream);
+    gather_values<T>(Ub.perm.as<int>(), invU.as<T>(), invU_lev.as<T>(), n, stream);
     sgs_valid = true;
     sgs_version = version;
 }
@@ -287,12 +295,12 @@ void Handle::apply_precond(const T *d_r, T *d_z, const KState *stp) {
     const size_t v = sizeof(T);
     if (cluster_ok(Lf, v) && cluster_ok(Ltb, v)) {
         timed(PC_FWD, tri_bytes(Lf, v, 2), [&] {
-            sweep_cluster<T>(Lf, Lval.as<T>(), SW_FWD_DIV, d_r, nullptr, nullptr, y, nullptr,
-                             use_inv_diag ? invL.as<T>() : nullptr, stp, swcfg.group, stream);
+            sweep_cluster<T>(Lf, Lval.as<T>(), SW_FWD_DIV, d_r, nullptr, use_inv_diag ? invL_lev.as<T>() : nullptr, y,
+                             nullptr, stp, cl_group, stream);
         });
         timed(PC_BWD, tri_bytes(Ltb, v, 3), [&] {
-            sweep_cluster<T>(Ltb, Ltval.as<T>(), SW_BWD_IC, nullptr, y, Dvec.as<T>(), d_z, nullptr, nullptr, stp,
-                             swcfg.group, stream);
+            sweep_cluster<T>(Ltb, Ltval.as<T>(), SW_BWD_IC, nullptr, y, D_lev.as<T>(), d_z, nullptr, stp, cl_group,
+                             stream);
         });
         return;
     }
@@ -380,8 +388,8 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
     if (sgs && n) {
         // rd = C^{-1} r (src/MatSolverMRTR_SGSver.cpp:118-132)
         if (cluster_ok(Lf, sizeof(T))) {
-            sweep_cluster<T>(Lf, Cval.as<T>(), SW_FWD_DIV, r, nullptr, nullptr, t1, nullptr,
-                             use_inv_diag ? invC.as<T>() : nullptr, nullptr, swcfg.group, s);
+            sweep_cluster<T>(Lf, Cval.as<T>(), SW_FWD_DIV, r, nullptr, use_inv_diag ? invC_lev.as<T>() : nullptr, t1,
+                             nullptr, nullptr, cl_group, s);
         } else {
             fill_sentinel_st<T>(t1, n, nullptr, s);
             sweep_st<T>(Lf, Cval.as<T>(), SW_FWD_DIV, r, nullptr, nullptr, t1, nullptr, ticket(), err(), nullptr, s,
@@ -491,12 +499,12 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
             // u = U^{-1} rd ; ARd = u + C^{-1}(rd - u)  (src/MatSolverMRTR_SGSver.cpp:184-189)
             if (sgs_cluster) {
                 timed(PC_BWD, tri_bytes(Ub, vb, 2), [&] {
-                    sweep_cluster<T>(Ub, Uval.as<T>(), SW_BWD_DIV, r, nullptr, nullptr, u, nullptr,
-                                     use_inv_diag ? invU.as<T>() : nullptr, st, swcfg.group, s);
+                    sweep_cluster<T>(Ub, Uval.as<T>(), SW_BWD_DIV, r, nullptr,
+                                     use_inv_diag ? invU_lev.as<T>() : nullptr, u, nullptr, st, cl_group, s);
                 });
                 timed(PC_FWD, tri_bytes(Lf, vb, 4), [&] {
-                    sweep_cluster<T>(Lf, Cval.as<T>(), SW_FWD_EIS, r, u, nullptr, t1, w,
-                                     use_inv_diag ? invC.as<T>() : nullptr, st, swcfg.group, s);
+                    sweep_cluster<T>(Lf, Cval.as<T>(), SW_FWD_EIS, r, u, use_inv_diag ? invC_lev.as<T>() : nullptr,
+                                     t1, w, st, cl_group, s);
                 });
             } else {
                 timed(PC_VEC, nv, [&] { fill_sentinel_st<T>(u, n, st, s); });

@@ -61,6 +61,7 @@ struct Handle {
     // ---- values
     DBuf Lval, Ltval, Cval, Uval, Dvec;  // factor (Lf / Ltb layouts), SGS triangles, 1/pivot
     DBuf invL, invC, invU;               // reciprocal diagonals (natural order) for the dividing sweeps
+    DBuf invL_lev, D_lev, invC_lev, invU_lev;  // the same in the level order of the sweep that reads them
     bool fac_valid = false;
     uint64_t fac_version = 0;
     double fac_alpha_req = 0.0, alpha_used = 0.0;
@@ -88,7 +89,8 @@ struct Handle {
     int fac_backoff_ns = 0;
     bool use_inv_diag = true;
     int sweep_mode = 1;            // 0 auto, 1 sync-free (default), 2 cluster
-    int cl_ring_bytes = 96 * 1024; // distributed shared-memory ring per CTA
+    int cl_ring_bytes = 32 * 1024; // distributed shared-memory ring per CTA
+    int cl_group = 4;              // lanes per row in the cluster sweep
     bool cluster_ok(Tri &t, size_t elem);
 
     Prof prof;

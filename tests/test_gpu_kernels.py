@@ -149,8 +149,13 @@ def test_cluster_and_syncfree_sweeps_agree(handle, name):
     if np.iscomplexobj(val):
         r = r + 0.5j * np.random.default_rng(4).standard_normal(n)
     out = {}
-    for mode in (1, 2):
-        handle.set_tuning(_capi.TUNE_SWEEP_MODE, mode)
-        out[mode] = handle.apply_precond(r)
-    handle.set_tuning(_capi.TUNE_SWEEP_MODE, 0)
-    assert np.array_equal(out[1], out[2])
+    for g in (4, 8):
+        handle.set_tuning(_capi.TUNE_SWEEP_GROUP, g)
+        handle.set_tuning(_capi.TUNE_CLUSTER_GROUP, g)
+        for mode in (1, 2):
+            handle.set_tuning(_capi.TUNE_SWEEP_MODE, mode)
+            out[mode, g] = handle.apply_precond(r)
+        assert np.array_equal(out[1, g], out[2, g])
+    handle.set_tuning(_capi.TUNE_SWEEP_MODE, 1)
+    handle.set_tuning(_capi.TUNE_SWEEP_GROUP, 0)
+    handle.set_tuning(_capi.TUNE_CLUSTER_GROUP, 4)

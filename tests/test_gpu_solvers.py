@@ -158,6 +158,23 @@ def test_zero_rhs_and_early_exit(handle, golden_cases):
     assert ok2 and iters2 == 0 and len(log2) == 0
 
 
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("key", ["cfg1/iccg", "cfg1/mrtr_ic", "cfg1/mrtr_sgs", "ec8/iccg"])
+def test_sweep_modes_solve_alike(handle, golden, golden_cases, key, mode):
+    """Both sweep schedules (sync-free and one-cluster) reach the reference's
+    iteration count."""
+    data, meta = golden
+    run = meta["runs"][key]
+    rp, ci, va, b = golden_cases[key.split("/")[0]]
+    handle.set_tuning(_capi.TUNE_SWEEP_MODE, mode)
+    try:
+        ok, x, log, iters = gpu_solve(handle, run["method"], rp, ci, va, b, Settings(**run["settings"]))
+    finally:
+        handle.set_tuning(_capi.TUNE_SWEEP_MODE, 1)
+    assert ok == run["converged"]
+    assert abs(iters - run["iters"]) <= iter_slack(run["iters"], np.iscomplexobj(va))
+
+
 def test_deterministic_and_factor_reuse(handle, golden_cases):
     rp, ci, va, b = golden_cases["cfg1"]
     s = Settings(accel_factor=1.1)
