@@ -35,8 +35,9 @@ namespace ssg {
 
 constexpr int CL_SLOT_BITS = 20;
 constexpr int CL_STORE_K = 8;   // store warp releases every K levels
-constexpr int CL_SPAN_BUFS = 4; // matrix span staged 3 levels ahead
+constexpr int CL_SPAN_BUFS = 5; // matrix span staged 4 levels ahead
 constexpr int CL_GATH_BUFS = 3; // gathered inputs staged 2 levels ahead
+constexpr int CL_PAD = 4;       // entries copied beyond a span to keep the 16-byte copies aligned
 
 __device__ __forceinline__ unsigned cluster_rank() {
     unsigned r;
@@ -77,6 +78,7 @@ __device__ __forceinline__ void cp_async(unsigned dst, const void *src) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 template <typename T>
 __device__ __forceinline__ T ld_dsmem(unsigned addr);
@@ -147,9 +149,9 @@ __host__ __device__ inline ClLayout cl_layout(int S, int cap_r, int cap_e, int e
     L.o_span = o;
     int so = 0;
     L.o_codes = so;
-    so += al16(cap_e * 4);
+    so += al16((cap_e + 2 * CL_PAD) * 4);
     L.o_vals = so;
-    so += al16(cap_e * elem);
+    so += al16((cap_e + 2 * CL_PAD) * elem);
     L.o_prp = so;
     so += al16((cap_r + 1) * 4);
     L.o_perm = so;
@@ -195,7 +197,11 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
     };
     auto span_base = [&](int l) { return Lay.o_span + (l % CL_SPAN_BUFS) * Lay.span_bytes; };
     auto gath_base = [&](int l) { return Lay.o_gath + (l % CL_GATH_BUFS) * Lay.gath_bytes; };
-    // stage the matrix span of level l: entry codes and values, row pointers, row ids, per-row vector
+    // stage the matrix span of level l: entry codes and values (16-byte copies of the
+    // aligned superset of [e0, e1); the arrays carry CL_PAD entries of padding), row
+    // pointers, row ids, per-row vector
+    constexpr int CPE = 16 / 4;              // codes per 16-byte copy
+    constexpr int VPE = VB >= 16 ? 1 : 16 / VB;  // values per 16-byte copy
     auto stage_span = [&](int l) {
         if (l >= nlev || is_store) return;
         int rs, re;
@@ -204,10 +210,11 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
         if (cnt <= 0) return;
         const int e0 = __ldg(prp + rs), e1 = __ldg(prp + re);
         const int sb = span_base(l);
-        for (int i = tid; i < e1 - e0; i += ncomp) {
-            cp_async<4>(sbase + sb + Lay.o_codes + 4 * i, code + e0 + i);
-            cp_async<VB>(sbase + sb + Lay.o_vals + VB * i, val + e0 + i);
-        }
+        const int c0 = e0 & ~(CPE - 1), v0 = e0 & ~(VPE - 1);
+        for (int i = tid; i * CPE < e1 - c0; i += ncomp)
+            cp_async<16>(sbase + sb + Lay.o_codes + 16 * i, code + c0 + CPE * i);
+        for (int i = tid; i * VPE < e1 - v0; i += ncomp)
+            cp_async<16>(sbase + sb + Lay.o_vals + 16 * i, val + v0 + VPE * i);
         for (int i = tid; i <= cnt; i += ncomp) cp_async<4>(sbase + sb + Lay.o_prp + 4 * i, prp + rs + i);
         for (int i = tid; i < cnt; i += ncomp) {
             cp_async<4>(sbase + sb + Lay.o_perm + 4 * i, perm + rs + i);
@@ -233,29 +240,32 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
         }
     };
 
-    // prologue: spans of levels 0..2, then gathers of levels 0..1
-    stage_span(0);
-    stage_span(1);
-    stage_span(2);
+    // prologue: spans of levels 0..3, then gathers of levels 0..1
+    for (int q = 0; q < CL_SPAN_BUFS - 1; ++q) stage_span(q);
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
     stage_gath(0);
     stage_gath(1);
     cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
 
     int produced = 0;  // values this CTA has written to its ring so far
     for (int l = 0; l < nlev; ++l) {
-        // A: everything staged for levels <= l+2 has landed and is visible CTA-wide
-        cp_async_wait_all();
+        // A: every copy group but the newest (the span of level l+3) has landed:
+        // the span of l+2 and the gathers of l are complete and visible CTA-wide
+        cp_async_wait_prev();
         __syncthreads();
         int rs, re;
         chunk_of(l, rs, re);
         const int cnt = re - rs;
         const unsigned char *sp = cl_smem + span_base(l);
-        const int *scode = (const int *)(sp + Lay.o_codes);
-        const T *sval = (const T *)(sp + Lay.o_vals);
         const int *sprp = (const int *)(sp + Lay.o_prp);
+        const int e0l = cnt > 0 ? sprp[0] : 0;
+        // entry k of the span (0-based from e0) sits at k + (e0 - aligned start) in the staged copies
+        const int *scode = (const int *)(sp + Lay.o_codes) + (e0l & (CPE - 1));
+        const T *sval = (const T *)(sp + Lay.o_vals) + (e0l & (VPE - 1));
         const int *sperm = (const int *)(sp + Lay.o_perm);
         const T *slvec = (const T *)(sp + Lay.o_lvec);
         const T *sg = (const T *)(cl_smem + gath_base(l));
@@ -268,6 +278,7 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
                 const int ob = fwd ? a : a + 1;
                 const int oe = fwd ? (e > a ? e - 1 : a) : e;
                 T acc = Sc<T>::zero();
+#pragma unroll 4
                 for (int k = ob + gl; k < oe; k += G) {
                     const int cd = scode[k];
                     T x;
@@ -304,9 +315,11 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
             // results are in the ring: let the store warp copy them out
             bar_arrive(1, nthreads);
             cluster_arrive_release();
-            // C: stage the span of level l+3 and the gathers of level l+2 while the barrier completes
-            stage_span(l + 3);
+            // C: stage the gathers of level l+2 (its span landed) and the span of level l+4
+            // while the barrier completes: two groups, the span one newest
             stage_gath(l + 2);
+            cp_async_commit();
+            stage_span(l + CL_SPAN_BUFS - 1);
             cp_async_commit();
             cluster_wait_acquire();
         } else {
@@ -448,6 +461,7 @@ void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBu
     const int elem = (int)elem_bytes;
     // sized for the fused Eisenstat sweep (second ring, two gathered inputs), the largest mode
     const ClLayout lay = cl_layout(ring_bytes / elem, cap_r, cap_e, elem, 1, 2);
+    if (T.nnz_pad < CL_PAD) return;  // the value arrays must carry padding for the aligned copies
     if (lay.total > CL_SMEM_MAX || lay.S >= (1 << CL_SLOT_BITS)) return;  // sync-free sweep instead
     const int S = lay.S;
     DBuf eo, owner, ord, inf;
@@ -460,7 +474,8 @@ void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBu
     k_cl_positions<<<div_up(T.n, 256), 256, 0, s>>>(T.n, T.perm.as<int>(), T.level.as<int>(), T.lptr_d.as<int>(),
                                                    eo.as<int>(), C, owner.as<unsigned char>(), ord.as<int>());
     SSG_LAUNCHED();
-    T.cl_code.ensure(sizeof(int) * (size_t)(T.nnz + 1));
+    T.cl_code.ensure(sizeof(int) * (size_t)(T.nnz + T.nnz_pad));
+    SSG_CUDA(cudaMemsetAsync(T.cl_code.p, 0, sizeof(int) * (size_t)(T.nnz + T.nnz_pad), s));
     k_cl_codes<<<div_up(T.n, 256), 256, 0, s>>>(T.n, T.perm.as<int>(), T.level.as<int>(), T.prp.as<int>(),
                                                 T.pci.as<int>(), T.ipos.as<int>(), owner.as<unsigned char>(),
                                                 ord.as<int>(), eo.as<int>(), C, S, CL_STORE_K, T.cl_code.as<int>(),

@@ -50,6 +50,7 @@ struct DBuf {
 // column order, column indices kept as original row ids.
 struct Tri {
     int n = 0, nnz = 0, nlev = 0;
+    int nnz_pad = 16;            // every per-entry array of this triangle (pci, psrc, codes, values) has nnz + nnz_pad slots
     bool lower = true;           // lower: deps j < i, diagonal last; upper: deps j > i, diagonal first
     DBuf level, perm, ipos;      // level[i], perm[t] = row, ipos[row] = t
     DBuf prp, pci, psrc;         // level-ordered CSR; psrc[k] = source value index

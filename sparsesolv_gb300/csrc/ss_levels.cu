@@ -234,26 +234,33 @@ void transpose_pattern(int n, int nnz, const int *rp, const int *ci, DBuf &trp, 
 }
 
 // ---------------------------------------------------------------- level sets
-// One warp per row; rows are claimed in dependency order through a ticket
-// (increasing for the forward triangle, decreasing for the backward one), so
-// every row a warp waits on was claimed earlier by a running warp and the
-// waits always end. Each wait is still bounded in time.
-constexpr int LV_ROWS_PER_TICKET = 4;
+// A group of LV_G lanes per row; a CTA claims LV_ROWS consecutive rows per
+// ticket, in dependency order (increasing row id for the forward triangle,
+// decreasing for the backward one), so every row a group waits on was claimed
+// earlier by a running group and the waits always end. Groups of one warp
+// reduce with group-local masks (one may wait on another). Each wait is also
+// bounded in time.
+constexpr int LV_G = 8;
+constexpr int LV_THREADS = 128;
+constexpr int LV_ROWS = LV_THREADS / LV_G;
 
-__global__ void k_levels(int n, const int *rp, const int *ci, int lower, int *level, int *ticket, int *nlev,
-                         int *err) {
-    const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(LV_THREADS) k_levels(int n, const int *rp, const int *ci, int lower, int *level,
+                                                       int *ticket, int *nlev, int *err) {
+    __shared__ int s_base;
+    const int g = threadIdx.x / LV_G, gl = threadIdx.x % LV_G;
+    const unsigned gm = group_mask(LV_G);
     int my_max = 0;
     for (;;) {
-        int t0 = 0;
-        if (lane == 0) t0 = atomicAdd(ticket, LV_ROWS_PER_TICKET);
-        t0 = __shfl_sync(0xffffffffu, t0, 0);
-        if (t0 >= n) break;
-        for (int q = 0; q < LV_ROWS_PER_TICKET && t0 + q < n; ++q) {
-            const int t = t0 + q;
+        if (threadIdx.x == 0) s_base = atomicAdd(ticket, LV_ROWS);
+        __syncthreads();
+        const int base = s_base;
+        __syncthreads();
+        if (base >= n) break;
+        const int t = base + g;
+        if (t < n) {
             const int row = lower ? t : n - 1 - t;
             int l = 0;
-            for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) {
+            for (int k = rp[row] + gl; k < rp[row + 1]; k += LV_G) {
                 const int c = ci[k];
                 if (lower ? (c < row) : (c > row)) {
                     const volatile int *pl = level + c;
@@ -277,12 +284,14 @@ __global__ void k_levels(int n, const int *rp, const int *ci, int lower, int *le
                 }
             }
 #pragma unroll
-            for (int m = 16; m >= 1; m >>= 1) l = max(l, __shfl_xor_sync(0xffffffffu, l, m));
-            if (lane == 0) *(volatile int *)(level + row) = l;
+            for (int m = LV_G / 2; m >= 1; m >>= 1) l = max(l, __shfl_xor_sync(gm, l, m));
+            if (gl == 0) *(volatile int *)(level + row) = l;
             my_max = max(my_max, l);
         }
     }
-    if (lane == 0) atomicMax(nlev, my_max + 1);
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) my_max = max(my_max, __shfl_xor_sync(0xffffffffu, my_max, m));
+    if ((threadIdx.x & 31) == 0) atomicMax(nlev, my_max + 1);
 }
 
 // histogram of levels per chunk of rows: cnt[l * nchunks + c]; one warp per chunk
@@ -370,10 +379,8 @@ void build_tri(Tri &T, int n, int nnz, const int *rp, const int *ci, const int *
         int dev = 0, sms = 0;
         SSG_CUDA(cudaGetDevice(&dev));
         SSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        // few enough warps that the spinning rows do not congest L2 (about one level's width in flight)
-        const int warps = min(div_up(n, LV_ROWS_PER_TICKET), sms * 4);
-        k_levels<<<div_up(warps * 32, 256), 256, 0, s>>>(n, rp, ci, lower ? 1 : 0, T.level.as<int>(), ticket, nlev_d,
-                                                         d_err);
+        const int blocks = min(div_up(n, LV_ROWS), sms * 2);
+        k_levels<<<blocks, LV_THREADS, 0, s>>>(n, rp, ci, lower ? 1 : 0, T.level.as<int>(), ticket, nlev_d, d_err);
         SSG_LAUNCHED();
     }
     int hv[2] = {0, 0};
@@ -414,8 +421,9 @@ void build_tri(Tri &T, int n, int nnz, const int *rp, const int *ci, const int *
     SSG_CUDA(cudaMemcpyAsync(T.lptr.data(), T.lptr_d.p, sizeof(int) * (size_t)(nlev + 1), cudaMemcpyDeviceToHost, s));
     // level-ordered copy of the rows
     T.prp.ensure(sizeof(int) * (size_t)(n + 1));
-    T.pci.ensure(sizeof(int) * (size_t)(nnz + 1));
-    T.psrc.ensure(sizeof(int) * (size_t)(nnz + 1));
+    T.pci.ensure(sizeof(int) * (size_t)(nnz + T.nnz_pad));
+    T.psrc.ensure(sizeof(int) * (size_t)(nnz + T.nnz_pad));
+    SSG_CUDA(cudaMemsetAsync(T.pci.p, 0, sizeof(int) * (size_t)(nnz + T.nnz_pad), s));
     k_perm_len<<<div_up(n + 1, 256), 256, 0, s>>>(n, T.perm.as<int>(), rp, T.prp.as<int>());
     SSG_LAUNCHED();
     scan_exclusive(T.prp.as<int>(), n + 1, nullptr, s, tmp);

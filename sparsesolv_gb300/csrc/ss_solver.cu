@@ -201,8 +201,9 @@ void Handle::ensure_factor(double alpha, bool scaled) {
         ensure_scaled<T>();
         aval = dad.as<T>();
     }
-    Lval.ensure(sizeof(T) * (size_t)(nnzL + 1));
-    Ltval.ensure(sizeof(T) * (size_t)(nnzL + 1));
+    // per-entry value arrays carry 16 slots of padding (aligned 16-byte staging in the cluster sweep)
+    Lval.ensure(sizeof(T) * (size_t)(nnzL + 16));
+    Ltval.ensure(sizeof(T) * (size_t)(nnzL + 16));
     Dvec.ensure(sizeof(T) * (size_t)(n + 1));
     invL.ensure(sizeof(T) * (size_t)(n + 1));
     done_buf.ensure(sizeof(int) * (size_t)(n + 1));
@@ -257,8 +258,8 @@ void Handle::ensure_sgs() {
     ensure_patterns(false, true);
     if (sgs_valid && sgs_version == version) return;
     ensure_scaled<T>();
-    Cval.ensure(sizeof(T) * (size_t)(nnzL + 1));
-    Uval.ensure(sizeof(T) * (size_t)(nnzU + 1));
+    Cval.ensure(sizeof(T) * (size_t)(nnzL + 16));
+    Uval.ensure(sizeof(T) * (size_t)(nnzU + 16));
     gather_values<T>(Lf.psrc.as<int>(), dad.as<T>(), Cval.as<T>(), nnzL, stream);
     gather_values<T>(Ub.psrc.as<int>(), dad.as<T>(), Uval.as<T>(), nnzU, stream);
     invC.ensure(sizeof(T) * (size_t)(n + 1));
