@@ -129,12 +129,12 @@ struct ClLayout {
     int ring2;  // second ring for the fused Eisenstat output (0/1)
     int ngath;  // gathered per-row inputs (1 or 2)
     // byte offsets
-    int o_ring, o_ring2, o_span, span_bytes, o_codes, o_vals, o_prp, o_perm, o_lvec, o_gath, gath_bytes, total;
+    int o_ring, o_ring2, o_span, span_bytes, o_codes, o_vals, o_prp, o_perm, o_lvec, o_gath, gath_bytes, o_tab, total;
 };
 
 __host__ __device__ inline int al16(int x) { return (x + 15) & ~15; }
 
-__host__ __device__ inline ClLayout cl_layout(int S, int cap_r, int cap_e, int elem, int ring2, int ngath) {
+__host__ __device__ inline ClLayout cl_layout(int S, int cap_r, int cap_e, int elem, int ring2, int ngath, int nlev) {
     ClLayout L;
     L.S = S;
     L.cap_r = cap_r;
@@ -163,6 +163,8 @@ __host__ __device__ inline ClLayout cl_layout(int S, int cap_r, int cap_e, int e
     L.o_gath = o;
     L.gath_bytes = al16(cap_r * elem * ngath);
     o += CL_GATH_BUFS * L.gath_bytes;
+    L.o_tab = o;  // per level: (rs, re, e0, e1) of this CTA's chunk
+    o += al16(nlev * 16);
     L.total = o;
     return L;
 }
@@ -172,7 +174,8 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
                                                         const int *__restrict__ perm, const int *__restrict__ prp,
                                                         const int *__restrict__ code, const T *__restrict__ val,
                                                         const T *__restrict__ lvec, const T *rhs, const T *aux, T *out,
-                                                        T *out2, const KState *st, ClLayout Lay) {
+                                                        T *out2, const KState *st, const int4 *__restrict__ tab,
+                                                        ClLayout Lay) {
     if (st && !st->active) return;  // uniform across the cluster
     extern __shared__ __align__(16) unsigned char cl_smem[];
     const unsigned sbase = (unsigned)__cvta_generic_to_shared(cl_smem);
@@ -189,11 +192,14 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
     constexpr bool eis = (MODE == SW_FWD_EIS);
     constexpr int VB = (int)sizeof(T);
 
+    // this CTA's chunk of every level, staged once: no global index loads inside the level loop
+    int4 *s_tab = (int4 *)(cl_smem + Lay.o_tab);
+    for (int q = tid; q < nlev; q += nthreads) s_tab[q] = __ldg(tab + (size_t)q * C + rank);
+    __syncthreads();
     auto chunk_of = [&](int l, int &rs, int &re) {
-        const int L0 = __ldg(lptr + l), L1 = __ldg(lptr + l + 1);
-        const int chunk = (L1 - L0 + C - 1) / C;
-        rs = min(L0 + rank * chunk, L1);
-        re = min(rs + chunk, L1);
+        const int4 c4 = s_tab[l];
+        rs = c4.x;
+        re = c4.y;
     };
     auto span_base = [&](int l) { return Lay.o_span + (l % CL_SPAN_BUFS) * Lay.span_bytes; };
     auto gath_base = [&](int l) { return Lay.o_gath + (l % CL_GATH_BUFS) * Lay.gath_bytes; };
@@ -208,7 +214,7 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
         chunk_of(l, rs, re);
         const int cnt = re - rs;
         if (cnt <= 0) return;
-        const int e0 = __ldg(prp + rs), e1 = __ldg(prp + re);
+        const int e0 = s_tab[l].z, e1 = s_tab[l].w;
         const int sb = span_base(l);
         const int c0 = e0 & ~(CPE - 1), v0 = e0 & ~(VPE - 1);
         for (int i = tid; i * CPE < e1 - c0; i += ncomp)
@@ -450,17 +456,19 @@ void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBu
     SSG_CUDA(cudaMemcpyAsync(prp.data(), T.prp.p, sizeof(int) * (size_t)(T.n + 1), cudaMemcpyDeviceToHost, s));
     SSG_CUDA(cudaStreamSynchronize(s));
     int cap_e = 1;
+    std::vector<int4> tab((size_t)nlev * C);
     for (int l = 0; l < nlev; ++l) {
         const int L0 = T.lptr[l], L1 = T.lptr[l + 1];
         const int chunk = (L1 - L0 + C - 1) / C;
         for (int c = 0; c < C; ++c) {
             const int rs = std::min(L0 + c * chunk, L1), re = std::min(rs + chunk, L1);
             cap_e = std::max(cap_e, prp[re] - prp[rs]);
+            tab[(size_t)l * C + c] = make_int4(rs, re, prp[rs], prp[re]);
         }
     }
     const int elem = (int)elem_bytes;
     // sized for the fused Eisenstat sweep (second ring, two gathered inputs), the largest mode
-    const ClLayout lay = cl_layout(ring_bytes / elem, cap_r, cap_e, elem, 1, 2);
+    const ClLayout lay = cl_layout(ring_bytes / elem, cap_r, cap_e, elem, 1, 2, nlev);
     if (T.nnz_pad < CL_PAD) return;  // the value arrays must carry padding for the aligned copies
     if (lay.total > CL_SMEM_MAX || lay.S >= (1 << CL_SLOT_BITS)) return;  // sync-free sweep instead
     const int S = lay.S;
@@ -474,6 +482,8 @@ void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBu
     k_cl_positions<<<div_up(T.n, 256), 256, 0, s>>>(T.n, T.perm.as<int>(), T.level.as<int>(), T.lptr_d.as<int>(),
                                                    eo.as<int>(), C, owner.as<unsigned char>(), ord.as<int>());
     SSG_LAUNCHED();
+    T.cl_tab.ensure(sizeof(int4) * tab.size());
+    SSG_CUDA(cudaMemcpyAsync(T.cl_tab.p, tab.data(), sizeof(int4) * tab.size(), cudaMemcpyHostToDevice, s));
     T.cl_code.ensure(sizeof(int) * (size_t)(T.nnz + T.nnz_pad));
     SSG_CUDA(cudaMemsetAsync(T.cl_code.p, 0, sizeof(int) * (size_t)(T.nnz + T.nnz_pad), s));
     k_cl_codes<<<div_up(T.n, 256), 256, 0, s>>>(T.n, T.perm.as<int>(), T.level.as<int>(), T.prp.as<int>(),
@@ -499,7 +509,7 @@ static void launch_cluster(const Tri &tri, const T *val, int mode, const T *rhs,
                            T *out2, const KState *st, cudaStream_t s) {
     const int elem = (int)sizeof(T);
     const ClLayout lay = cl_layout(tri.cl_S, tri.cl_cap_r, tri.cl_cap_e, elem, mode == SW_FWD_EIS ? 1 : 0,
-                                   mode == SW_FWD_EIS ? 2 : 1);
+                                   mode == SW_FWD_EIS ? 2 : 1, tri.nlev);
     // compute threads: enough groups for the widest chunk, 64..512, plus one store warp
     int ncomp = std::min(512, std::max(64, ((tri.cl_cap_r * G + 31) / 32) * 32));
     ncomp = (ncomp / G) * G;
@@ -529,7 +539,7 @@ static void launch_cluster(const Tri &tri, const T *val, int mode, const T *rhs,
             prepared = true;                                                                                     \
         }                                                                                                        \
         SSG_CUDA(cudaLaunchKernelEx(&cfg, kern, tri.nlev, ncomp, lp, pm, pr, cd, val, lvec, rhs, aux, out, out2, \
-                                    st, lay));                                                                   \
+                                    st, tri.cl_tab.as<int4>(), lay));                                            \
     } while (0)
     switch (mode) {
         case SW_FWD_DIV: SSG_CL(SW_FWD_DIV); break;

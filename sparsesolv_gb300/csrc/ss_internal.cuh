@@ -60,6 +60,7 @@ struct Tri {
     bool cl_ready = false;
     int cl_C = 0, cl_S = 0, cl_elem = 0, cl_ring_bytes = 0, cl_cap_r = 0, cl_cap_e = 0;
     DBuf cl_code;                // per level-ordered entry: row id, or -1 - (owner << 20 | ring slot)
+    DBuf cl_tab;                 // per (level, CTA): rows [rs, re) and entries [e0, e1) of the chunk
 };
 
 // ss_levels.cu
