@@ -78,7 +78,7 @@ __device__ __forceinline__ void cp_async(unsigned dst, const void *src) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev2() { asm volatile("cp.async.wait_group 2;" ::: "memory"); }
 
 template <typename T>
 __device__ __forceinline__ T ld_dsmem(unsigned addr);
@@ -259,9 +259,10 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
 
     int produced = 0;  // values this CTA has written to its ring so far
     for (int l = 0; l < nlev; ++l) {
-        // A: every copy group but the newest (the span of level l+3) has landed:
-        // the span of l+2 and the gathers of l are complete and visible CTA-wide
-        cp_async_wait_prev();
+        // A: every copy group but the two newest (the gathers of l+1 and the span of
+        // l+3, issued one level ago) has landed: the span of l+2 and the gathers of l
+        // are complete and visible CTA-wide
+        cp_async_wait_prev2();
         __syncthreads();
         int rs, re;
         chunk_of(l, rs, re);
