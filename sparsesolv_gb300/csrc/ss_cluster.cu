@@ -106,6 +106,43 @@ __device__ __forceinline__ cplxf ld_dsmem<cplxf>(unsigned addr) {
     asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
     return v;
 }
+// generic address of the same shared-memory location in CTA `rank` of the cluster
+__device__ __forceinline__ unsigned long long mapa_generic(const void *p, unsigned rank) {
+    unsigned long long r;
+    asm volatile("mapa.u64 %0, %1, %2;" : "=l"(r) : "l"(p), "r"(rank));
+    return r;
+}
+// one load for either a global address or a distributed shared-memory address;
+// relaxed at cluster scope, so a global line is never served stale from L1
+template <typename T>
+__device__ __forceinline__ T ld_rc(unsigned long long a);
+template <>
+__device__ __forceinline__ double ld_rc<double>(unsigned long long a) {
+    double v;
+    asm volatile("ld.relaxed.cluster.f64 %0, [%1];" : "=d"(v) : "l"(a) : "memory");
+    return v;
+}
+template <>
+__device__ __forceinline__ float ld_rc<float>(unsigned long long a) {
+    float v;
+    asm volatile("ld.relaxed.cluster.f32 %0, [%1];" : "=f"(v) : "l"(a) : "memory");
+    return v;
+}
+template <>
+__device__ __forceinline__ cplx ld_rc<cplx>(unsigned long long a) {
+    cplx v;
+    asm volatile("ld.relaxed.cluster.f64 %0, [%1];" : "=d"(v.x) : "l"(a) : "memory");
+    asm volatile("ld.relaxed.cluster.f64 %0, [%1];" : "=d"(v.y) : "l"(a + 8) : "memory");
+    return v;
+}
+template <>
+__device__ __forceinline__ cplxf ld_rc<cplxf>(unsigned long long a) {
+    cplxf v;
+    asm volatile("ld.relaxed.cluster.f32 %0, [%1];" : "=f"(v.x) : "l"(a) : "memory");
+    asm volatile("ld.relaxed.cluster.f32 %0, [%1];" : "=f"(v.y) : "l"(a + 4) : "memory");
+    return v;
+}
+
 template <typename T>
 __device__ __forceinline__ T ld_l2(const T *p) {
     return __ldcg(p);
@@ -285,19 +322,29 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
                 const int ob = fwd ? a : a + 1;
                 const int oe = fwd ? (e > a ? e - 1 : a) : e;
                 T acc = Sc<T>::zero();
-#pragma unroll 4
-                for (int k = ob + gl; k < oe; k += G) {
-                    const int cd = scode[k];
-                    T x;
-                    if (cd >= 0) {
-                        x = ld_l2(out + cd);
-                    } else {
-                        const int sl = -1 - cd;
-                        x = ld_dsmem<T>(map_shared(
-                            sbase + Lay.o_ring + (unsigned)((sl & ((1 << CL_SLOT_BITS) - 1)) * VB),
-                            (unsigned)(sl >> CL_SLOT_BITS)));
+                // four entries per step: all addresses first, then all loads, then the
+                // multiply-adds in entry order (the same order as the sync-free sweep)
+                for (int k0 = ob + gl; k0 < oe; k0 += 4 * G) {
+                    unsigned long long ad[4];
+                    T vv[4], xx[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int k = k0 + u * G;
+                        if (k < oe) {
+                            const int cd = scode[k];
+                            vv[u] = sval[k];
+                            const int sl = -1 - cd;
+                            ad[u] = cd >= 0 ? (unsigned long long)(out + cd)
+                                            : mapa_generic(ring + (sl & ((1 << CL_SLOT_BITS) - 1)),
+                                                           (unsigned)(sl >> CL_SLOT_BITS));
+                        }
                     }
-                    acc = acc + sval[k] * x;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (k0 + u * G < oe) xx[u] = ld_rc<T>(ad[u]);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (k0 + u * G < oe) acc = acc + vv[u] * xx[u];
                 }
 #pragma unroll
                 for (int m = G / 2; m >= 1; m >>= 1) acc = acc + gshfl_xor(acc, m, gm);
