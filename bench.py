@@ -11,7 +11,7 @@ and b resident in HBM; ``e2e`` is the same through the C ABI with host
 buffers (values, b and x0 copied in, x copied out inside the timed region).
 
     python bench.py [--steps K] [--warmup W] [--method iccg|sgs|mrtr_ic]
-                    [--workload cfg2|cfg1] [--impl reference]
+                    [--workload cfg2|cfg1] [--sweep-mode 0|1|2] [--impl reference]
 
 Under torchrun (--gpus N > 1) every rank solves its own replica (the path
 does not shard; "replicas only") and value sums the ranks' solves.
@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--method", default="iccg", choices=["iccg", "sgs", "mrtr_ic"])
     ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sweep-mode", type=int, default=0, choices=[0, 1, 2],
+                    help="triangular sweeps: 0 automatic, 1 sync-free, 2 one-cluster level-synchronous")
     return ap.parse_args()
 
 
@@ -235,6 +237,7 @@ def run_ours(args):
     o.precondition_type = pt
     o.is_save_residual_log = 1
     h.set_options(o)
+    h.set_tuning(_capi.TUNE_SWEEP_MODE, args.sweep_mode)
     h.set_matrix(rp, ci, val)
     stream = torch.cuda.ExternalStream(h.stream(), device=dev)
 
@@ -313,7 +316,8 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded voxel generator)",
         "config": {"workload": label, "n": n, "nnz": nnz, "method": mname, "alpha": ALPHA, "tolerance": TOL,
                    "iterations": iters, "parallelism": "replicas only" if ws > 1 else "single GPU",
-                   "factor": "recomputed every step", "level_schedule": "computed once per sparsity pattern",
+                   "factor": "recomputed every step",
+                   "sweep_mode": ["automatic", "sync-free", "one-cluster"][args.sweep_mode], "level_schedule": "computed once per sparsity pattern",
                    "l2": "inputs larger than L2 (matrix %.0f MB)" % ((12.0 * nnz) / 1e6),
                    "true_relative_residual": true_res},
         "time_to_tolerance_s": ms_max / args.steps / 1e3,

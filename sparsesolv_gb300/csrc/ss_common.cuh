@@ -19,11 +19,30 @@ struct cplxf {
     float x, y;
 };
 
+// Products rounded on their own (no fused multiply-add), so that a sum of two
+// products such as a.x*b.x - a.y*b.y gives the same bits in every kernel: with
+// contraction the compiler may fuse either product, and picks differently in
+// differently shaped loops. This is also the rounding of a CPU without FMA.
+__host__ __device__ __forceinline__ double mul_rn(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+__host__ __device__ __forceinline__ float mul_rn(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+
 __host__ __device__ __forceinline__ cplx operator+(cplx a, cplx b) { return {a.x + b.x, a.y + b.y}; }
 __host__ __device__ __forceinline__ cplx operator-(cplx a, cplx b) { return {a.x - b.x, a.y - b.y}; }
 __host__ __device__ __forceinline__ cplx operator-(cplx a) { return {-a.x, -a.y}; }
 __host__ __device__ __forceinline__ cplx operator*(cplx a, cplx b) {
-    return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+    return {mul_rn(a.x, b.x) - mul_rn(a.y, b.y), mul_rn(a.x, b.y) + mul_rn(a.y, b.x)};
 }
 __host__ __device__ __forceinline__ cplx operator*(double s, cplx a) { return {s * a.x, s * a.y}; }
 // Smith's algorithm (R. L. Smith, CACM 5(8), 1962) for robust complex division
@@ -39,7 +58,7 @@ __host__ __device__ __forceinline__ cplx operator/(cplx a, cplx b) {
 __host__ __device__ __forceinline__ cplxf operator+(cplxf a, cplxf b) { return {a.x + b.x, a.y + b.y}; }
 __host__ __device__ __forceinline__ cplxf operator-(cplxf a, cplxf b) { return {a.x - b.x, a.y - b.y}; }
 __host__ __device__ __forceinline__ cplxf operator*(cplxf a, cplxf b) {
-    return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+    return {mul_rn(a.x, b.x) - mul_rn(a.y, b.y), mul_rn(a.x, b.y) + mul_rn(a.y, b.x)};
 }
 __host__ __device__ __forceinline__ cplxf operator/(cplxf a, cplxf b) {
     if (fabsf(b.x) >= fabsf(b.y)) {

@@ -280,8 +280,14 @@ static double tri_bytes(const Tri &T, size_t v, int vecs) {
     return (4.0 + (double)v) * T.nnz + 4.0 * (T.n + 1) + (double)vecs * (double)v * T.n;
 }
 
+// mean rows per level above which the automatic mode keeps the sync-free sweep
+static constexpr double kAutoClusterRowsPerLevel = 4096.0;
+
 bool Handle::cluster_ok(Tri &t, size_t elem) {
     if (sweep_mode == 1 || t.n == 0) return false;
+    // automatic: one cluster wins while the levels are narrow enough that the
+    // per-level latency, not the row count, sets the pace
+    if (sweep_mode == 0 && (double)t.n > kAutoClusterRowsPerLevel * (double)t.nlev) return false;
     if (!t.cl_ready || t.cl_elem != (int)elem || t.cl_ring_bytes != cl_ring_bytes) {
         DBuf tmp;
         cluster_plan(t, elem, cl_ring_bytes, stream, tmp);

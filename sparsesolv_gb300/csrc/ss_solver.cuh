@@ -88,7 +88,7 @@ struct Handle {
     SweepCfg swcfg;
     int fac_backoff_ns = 0;
     bool use_inv_diag = true;
-    int sweep_mode = 1;            // 0 auto, 1 sync-free (default), 2 cluster
+    int sweep_mode = 0;            // 0 auto (default), 1 sync-free, 2 cluster
     int cl_ring_bytes = 16 * 1024; // distributed shared-memory ring per CTA
     int cl_group = 4;              // lanes per row in the cluster sweep
     bool cluster_ok(Tri &t, size_t elem);

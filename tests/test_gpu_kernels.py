@@ -156,6 +156,6 @@ def test_cluster_and_syncfree_sweeps_agree(handle, name):
             handle.set_tuning(_capi.TUNE_SWEEP_MODE, mode)
             out[mode, g] = handle.apply_precond(r)
         assert np.array_equal(out[1, g], out[2, g])
-    handle.set_tuning(_capi.TUNE_SWEEP_MODE, 1)
+    handle.set_tuning(_capi.TUNE_SWEEP_MODE, 0)
     handle.set_tuning(_capi.TUNE_SWEEP_GROUP, 0)
     handle.set_tuning(_capi.TUNE_CLUSTER_GROUP, 4)

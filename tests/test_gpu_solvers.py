@@ -170,7 +170,7 @@ def test_sweep_modes_solve_alike(handle, golden, golden_cases, key, mode):
     try:
         ok, x, log, iters = gpu_solve(handle, run["method"], rp, ci, va, b, Settings(**run["settings"]))
     finally:
-        handle.set_tuning(_capi.TUNE_SWEEP_MODE, 1)
+        handle.set_tuning(_capi.TUNE_SWEEP_MODE, 0)
     assert ok == run["converged"]
     assert abs(iters - run["iters"]) <= iter_slack(run["iters"], np.iscomplexobj(va))
 
