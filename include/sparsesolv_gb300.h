@@ -179,6 +179,39 @@ int ssg_spmv(ssg_handle h, const double *x, double *y);
  * number of levels in *nlev */
 int ssg_level_schedule(ssg_handle h, int lower, int32_t *level, int32_t *perm, int *nlev);
 
+/* ---- IC(0) factor that allocates nothing (no counterpart in the reference) ----
+ * For callers that may not call cudaMalloc: code that runs under an external
+ * memory manager which owns all device memory, or a real-time loop where an
+ * allocation's latency or failure is not allowed. Unlike ssg_create/
+ * ssg_set_matrix/ssg_factor it needs no handle and allocates no memory, host or
+ * device: its scratch (one flag per row, a row ticket, an error word) is a
+ * file-scope array of the library, (64 + SSG_NOALLOC_MAX_ROWS) ints = 8 MB, that
+ * every GPU which loads the library holds until the process exits.
+ *
+ * All pointers are device memory on the calling thread's current device:
+ *   lrp[n+1], lci[nnz]  lower triangle of A including the diagonal, CSR in
+ *                       natural row order, columns ascending, diagonal last in
+ *                       each row, at most 32 entries a row (the pattern
+ *                       ssg_factor returns)
+ *   lower_val[nnz]      A's values on that pattern (double, or interleaved
+ *                       complex for value_type SSG_COMPLEX)
+ *   lval[nnz], D[n]     outputs: L on the same pattern and D = 1/pivot, the
+ *                       shifted IC(0) of src/SprsPreconditioner.cpp:43-111;
+ *                       lval may be lower_val (factor in place)
+ *   alpha > 0           the shift (acceleration factor); no automatic search
+ * Work is queued on `stream` (NULL: the legacy default stream) and the call
+ * waits for it, so the result is ready on return. Returns SSG_OK,
+ * SSG_ERR_ARG (n > SSG_NOALLOC_MAX_ROWS, a bad argument, or a row longer than
+ * 32 entries), SSG_ERR_NO_DIAGONAL, SSG_ERR_TIMEOUT or SSG_ERR_CUDA.
+ * The first call on a device looks up the array's device address (once per
+ * device, cudaGetSymbolAddress); make that first call before any stream
+ * capture. All calls share the one array and it keeps the last call's
+ * contents (each call clears what it uses), so calls whose work overlaps on
+ * the GPU (other threads, other streams) race: serialise them. */
+#define SSG_NOALLOC_MAX_ROWS (1 << 21)
+int ssg_ic_factor_noalloc(int n, int nnz, const int32_t *lrp, const int32_t *lci, const void *lower_val, void *lval,
+                          void *D, double alpha, int value_type, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,8 +26,9 @@ EXPORTED = [
     "ssg_set_matrix_device", "ssg_solve", "ssg_solve_device", "ssg_get_residual_log", "ssg_get_iters",
     "ssg_get_accel_used", "ssg_get_timings", "ssg_factor", "ssg_apply_precond", "ssg_spmv", "ssg_level_schedule",
     "ssg_update_values", "ssg_update_values_device", "ssg_get_stream", "ssg_set_profiling", "ssg_get_kernel_stats",
-    "ssg_launch_count", "ssg_set_tuning",
+    "ssg_launch_count", "ssg_set_tuning", "ssg_ic_factor_noalloc",
 ]
+NOALLOC_MAX_ROWS = 1 << 21
 TUNE_SWEEP_CTA_PER_SM = 0
 TUNE_SWEEP_GROUP = 1
 TUNE_SWEEP_BACKOFF_NS = 2
@@ -79,6 +80,7 @@ def declare(lib):
         "ssg_get_kernel_stats": ([H, P, P, P, I], I),
         "ssg_launch_count": ([], ctypes.c_longlong),
         "ssg_set_tuning": ([H, I, I], I),
+        "ssg_ic_factor_noalloc": ([I, I, P, P, P, P, P, D, I, P], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -366,4 +366,9 @@ int ssg_level_schedule(ssg_handle hd, int lower, int32_t *level, int32_t *perm, 
     });
 }
 
+int ssg_ic_factor_noalloc(int n, int nnz, const int32_t *lrp, const int32_t *lci, const void *lower_val, void *lval,
+                          void *D, double alpha, int value_type, void *stream) {
+    return ssg::ic_factor_noalloc(n, nnz, lrp, lci, lower_val, lval, D, alpha, value_type, (cudaStream_t)stream);
+}
+
 }  // extern "C"

@@ -10,7 +10,9 @@
 // warp reductions. Rows are claimed in level order through a ticket, and a
 // row waits (bounded) for the rows it reads to publish their "done" flags.
 #include <cfloat>
+#include <mutex>
 
+#include "sparsesolv_gb300.h"
 #include "ss_internal.cuh"
 
 namespace ssg {
@@ -162,7 +164,9 @@ int factor_blocks_per_sm = 4;  // rows in flight: enough for a level, few enough
 template <typename T>
 __host__ __device__ constexpr int ff_warps() { return sizeof(T) == 8 ? 3 : 2; }  // static shared memory below 48 KB
 
-template <typename T>
+// NAT: rows in natural order (perm is the identity, a row's dependencies start
+// at prp[c]); dep and perm are then not read.
+template <typename T, bool NAT = false>
 __global__ void __launch_bounds__(ff_warps<T>() * 32) k_ic_factor_fast(int n, const int *perm, const int *prp,
                                                                        const int *pci, const int2 *dep, T *lval,
                                                                        T *D, int *done, double alpha, int *ticket,
@@ -176,13 +180,15 @@ __global__ void __launch_bounds__(ff_warps<T>() * 32) k_ic_factor_fast(int n, co
         if (lane == 0) t = atomicAdd(ticket, 1);
         t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= n) return;
-        const int i = perm[t];
+        const int i = NAT ? t : perm[t];
         const int a = prp[t], m = prp[t + 1] - a;
         const bool have = lane < m;
         const int c = have ? pci[a + lane] : INT_MAX;
         T v = have ? lval[a + lane] : Sc<T>::zero();
         const int last_c = __shfl_sync(0xffffffffu, c, (m - 1) & 31);
-        if (m < 1 || m > FF_MAXROW || last_c != i) {
+        // caller-given pattern (natural order): off-diagonal columns must lie in [0, i)
+        const bool bad_col = NAT && __any_sync(0xffffffffu, have && lane < m - 1 && (c < 0 || c >= i));
+        if (m < 1 || m > FF_MAXROW || last_c != i || bad_col) {
             // no diagonal last (src/SprsPreconditioner.cpp:88-94) or too long for this kernel
             if (lane == 0) {
                 atomicExch(err, m > FF_MAXROW ? ERR_ROW_TOO_LONG : ERR_NO_DIAG);
@@ -215,7 +221,8 @@ __global__ void __launch_bounds__(ff_warps<T>() * 32) k_ic_factor_fast(int n, co
             __threadfence();
             dk = ldcg(D + c);
             // row j = c without its diagonal (its last entry); the loads are independent
-            const int2 dj = dep[a + lane];  // (start, length) of row j in level order
+            // (start, length) of row j in level order
+            const int2 dj = NAT ? make_int2(prp[c], prp[c + 1] - prp[c]) : dep[a + lane];
             mj = min(dj.y - 1, FF_MAXROW - 1);
 #pragma unroll
             for (int l = 0; l < FF_MAXROW - 1; ++l) {
@@ -369,5 +376,79 @@ void all_pivots_positive(int n, const T *D, int *d_flag, cudaStream_t s) {
 SSG_INST(double)
 SSG_INST(cplx)
 #undef SSG_INST
+
+// ---------------------------------------------------------------- factor without allocation
+// For callers that may not allocate device memory (ssg_ic_factor_noalloc): the
+// row flags, the row ticket and the error word live in one file-scope array
+// that every device loading this library holds until the process exits.
+// Layout: [0] ticket, [1] error code, [NA_HEAD, NA_HEAD + n) row done flags.
+constexpr int NA_HEAD = 64;  // 256 bytes, keeps the flags 256-byte aligned
+static __device__ __align__(256) int g_noalloc_scratch[NA_HEAD + SSG_NOALLOC_MAX_ROWS];
+
+// Device address of the scratch array on device `dev`, which must be current.
+// The array's name in host code is only a stand-in; a kernel needs this
+// address. Looked up once per device and kept.
+static int noalloc_scratch(int dev, int **out) {
+    constexpr int MAX_DEV = 64;
+    static std::mutex mu;
+    static int *addr[MAX_DEV] = {};
+    if (dev < 0 || dev >= MAX_DEV) return SSG_ERR_ARG;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return SSG_ERR_CUDA;
+        addr[dev] = (int *)p;
+    }
+    *out = addr[dev];
+    return SSG_OK;
+}
+
+template <typename T>
+static cudaError_t noalloc_launch(int n, const int *lrp, const int *lci, void *lval, void *D, double alpha,
+                                  int *scr, int sms, cudaStream_t s) {
+    constexpr int W = ff_warps<T>();
+    const int blocks = min(div_up(n, W), sms * factor_blocks_per_sm);
+    k_ic_factor_fast<T, true><<<blocks, W * 32, 0, s>>>(n, nullptr, lrp, lci, nullptr, (T *)lval, (T *)D,
+                                                        scr + NA_HEAD, alpha, scr, scr + 1, 0);
+    return cudaGetLastError();
+}
+
+// Natural-order IC(0) with the scratch above. Every failure returns a code;
+// nothing here allocates, host or device, on the way to a result.
+int ic_factor_noalloc(int n, int nnz, const int *lrp, const int *lci, const void *val, void *lval, void *D,
+                      double alpha, int vtype, cudaStream_t s) {
+    if (n < 0 || nnz < 0 || n > SSG_NOALLOC_MAX_ROWS) return SSG_ERR_ARG;
+    if (!(alpha > 0.0) || (vtype != SSG_REAL && vtype != SSG_COMPLEX)) return SSG_ERR_ARG;
+    if (n == 0) return SSG_OK;
+    if (!lrp || !lci || !val || !lval || !D || nnz < n) return SSG_ERR_ARG;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return SSG_ERR_CUDA;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return SSG_ERR_CUDA;
+    int *scr = nullptr;
+    const int rc = noalloc_scratch(dev, &scr);
+    if (rc != SSG_OK) return rc;
+    const size_t vb = vtype == SSG_COMPLEX ? sizeof(cplx) : sizeof(double);
+    if (val != lval && cudaMemcpyAsync(lval, val, vb * (size_t)nnz, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        return SSG_ERR_CUDA;
+    // the ticket, the error word and the flags of this call's rows start at zero
+    if (cudaMemsetAsync(scr, 0, sizeof(int) * (NA_HEAD + (size_t)n), s) != cudaSuccess) return SSG_ERR_CUDA;
+    const cudaError_t le = vtype == SSG_COMPLEX ? noalloc_launch<cplx>(n, lrp, lci, lval, D, alpha, scr, sms, s)
+                                                : noalloc_launch<double>(n, lrp, lci, lval, D, alpha, scr, sms, s);
+    if (le != cudaSuccess) return SSG_ERR_CUDA;
+    try {
+        note_launch();
+    } catch (...) {
+        return SSG_ERR_CUDA;
+    }
+    int err = 0;
+    if (cudaMemcpyAsync(&err, scr + 1, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return SSG_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return SSG_ERR_CUDA;
+    switch (err) {
+        case ERR_NONE: return SSG_OK;
+        case ERR_TIMEOUT: return SSG_ERR_TIMEOUT;
+        case ERR_NO_DIAG: return SSG_ERR_NO_DIAGONAL;
+        default: return SSG_ERR_ARG;  // a row longer than the kernel's 32 entries
+    }
+}
 
 }  // namespace ssg

@@ -86,6 +86,9 @@ void factor_plan(const Tri &L, DBuf &dep, int &max_row, cudaStream_t s);
 template <typename T>
 void ic_factor(const Tri &L, T *lval, T *D, double alpha, int *d_err, int *d_ticket, cudaStream_t s,
                const int2 *dep, int max_row, int *done, int backoff_ns);
+// natural-order factor with library-owned scratch; returns an SSG_* code
+int ic_factor_noalloc(int n, int nnz, const int *lrp, const int *lci, const void *val, void *lval, void *D,
+                      double alpha, int vtype, cudaStream_t s);
 template <typename T>
 void diag_scaling(int n, const int *rp, const int *ci, const T *val, const T *b, T *d, T *bs, cudaStream_t s);
 template <typename T>
