@@ -152,7 +152,7 @@ def cpu_time_sample(rp, ci, val, b, method, pt, sample_iters, full_iters, use_re
     eng.solve(m, rp, ci, val, b, s, conv=TOL, maxit=sample_iters)
     t_sample = time.perf_counter() - t0
     per_iter = max(t_sample - t_setup, 1e-9) / sample_iters
-    return t_setup + per_iter * full_iters, t_setup, per_iter
+    return t_setup + per_iter * full_iters, t_setup, per_iter, eng.threads()
 
 
 def run_reference(args):
@@ -167,19 +167,20 @@ def run_reference(args):
     full_iters = reference_iterations(args, rp, ci, val, b, pt)
     times = []
     for k in range(args.warmup + args.steps):
-        t, ts, ti = cpu_time_sample(rp, ci, val, b, args.method, pt, CPU_SAMPLE_ITERS, full_iters, use_ref)
+        t, ts, ti, cores = cpu_time_sample(rp, ci, val, b, args.method, pt, CPU_SAMPLE_ITERS, full_iters, use_ref)
         if k >= args.warmup:
             times.append(t)
     sec = sum(times) / len(times)
     value = 1.0 / sec
     kind = "reference" if use_ref else "port"
     sample = ("%s: IC(0) factorisation + %d iterations of the %s per step, scaled to the %d iterations of a "
-              "full solve" % (label, CPU_SAMPLE_ITERS, mname, full_iters))
+              "full solve; SpMV row-parallel on %d OpenMP threads as in the reference, the rest serial"
+              % (label, CPU_SAMPLE_ITERS, mname, full_iters, cores))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded voxel generator)",
             "config": {"workload": label, "method": mname, "alpha": ALPHA, "tolerance": TOL},
-            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": 1, "kind": kind, "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -261,26 +262,30 @@ def run_ours(args):
         if ws > 1:
             torch.distributed.barrier()
 
-    # ---- device-resident timed region
+    # ---- device-resident timed region (one event pair per step for the latency percentiles)
     clocks = Clocks(local)
     clocks.start()
-    h.set_profiling(True)
     launches0 = h.launch_count()
     barrier()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev[0].record(stream)
     t_host0 = time.perf_counter()
-    for _ in range(args.steps):
+    for k in range(args.steps):
         ok = step_device() and ok
-    e1.record(stream)
+        ev[k + 1].record(stream)
     barrier()
     t_host = time.perf_counter() - t_host0
-    ms = e0.elapsed_time(e1)
+    ms = ev[0].elapsed_time(ev[-1])
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
     launches = h.launch_count() - launches0
+    clk = clocks.stop()
+    # ---- per-kernel-class times from the same steps run again with event profiling
+    h.set_profiling(True)
+    for _ in range(args.steps):
+        ok = step_device() and ok
+    barrier()
     stats = h.kernel_stats()
     h.set_profiling(False)
-    clk = clocks.stop()
     # ---- end-to-end through the C ABI with host buffers
     barrier()
     f0 = torch.cuda.Event(enable_timing=True)
@@ -293,14 +298,10 @@ def run_ours(args):
     ms_e2e = f0.elapsed_time(f1)
     true_res = float(np.linalg.norm(b - _spmv_host(rp, ci, val, x_h.numpy())) / np.linalg.norm(b))
 
-    ms_max = ms
-    ms_e2e_max = ms_e2e
-    if ws > 1:
-        t = torch.tensor([ms, ms_e2e], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_max, ms_e2e_max = float(t[0]), float(t[1])
-    value = ws * args.steps / (ms_max / 1e3)
-    e2e = ws * args.steps / (ms_e2e_max / 1e3)
+    from sparsesolv_gb300 import replicas
+    ms_max, ms_e2e_max = replicas.max_over_ranks([ms, ms_e2e])
+    value = replicas.whole_job_rate(args.steps, ws, ms_max)
+    e2e = replicas.whole_job_rate(args.steps, ws, ms_e2e_max)
 
     # roofline of the dominant kernel class
     dom = max(("forward sweep", "backward sweep", "spmv"), key=lambda k: stats[k][0])
@@ -321,6 +322,8 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (matrix %.0f MB)" % ((12.0 * nnz) / 1e6),
                    "true_relative_residual": true_res},
         "time_to_tolerance_s": ms_max / args.steps / 1e3,
+        "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
+                       "steps": len(step_ms)},
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": 8 * nnz + 16 * n,
                 "d2h_bytes_per_step": 8 * n},
         "gpu_launches": launches,
@@ -335,9 +338,10 @@ def run_ours(args):
         from oracle.oracle import Reference, build
         build()
         use_ref = Reference.available()
-        sec, ts, ti = cpu_time_sample(rp, ci, val, b, args.method, pt, CPU_SAMPLE_ITERS, iters, use_ref)
+        sec, ts, ti, cores = cpu_time_sample(rp, ci, val, b, args.method, pt, CPU_SAMPLE_ITERS, iters, use_ref)
         line["cpu_baseline"] = {
-            "value": 1.0 / sec, "unit": "solves/s", "cores": 1, "kind": "reference" if use_ref else "port",
+            "value": 1.0 / sec, "unit": "solves/s", "cores": cores,
+            "kind": "reference" if use_ref else "port",
             "sample": "IC(0) factorisation (%.2f s) + %d iterations (%.3f s each), scaled to %d iterations"
                       % (ts, CPU_SAMPLE_ITERS, ti, iters)}
     print(json.dumps(line), flush=True)

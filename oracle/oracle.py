@@ -114,6 +114,10 @@ class Oracle(_Base):
             build()
         self.lib = ctypes.CDLL(ORACLE_LIB)
 
+    def threads(self):
+        """Host threads of the row-parallel SpMV (1 when built without OpenMP)."""
+        return int(self.lib.or_threads())
+
     def solve(self, method, rp, ci, val, b, settings=None, x0=None, normB=None, conv=1e-8, maxit=10000):
         """method: 'iccg' or 'mrtr' (settings.precondition_type picks IC=0 / SGS=1)."""
         s = settings or Settings()
@@ -205,6 +209,11 @@ class Reference(_Base):
         if not os.path.exists(REF_LIB):
             raise RuntimeError("reference build %s is missing" % REF_LIB)
         self.lib = ctypes.CDLL(REF_LIB)
+
+    @staticmethod
+    def threads():
+        """OpenMP threads of the reference build (its Eigen SpMV is row-parallel)."""
+        return int(os.environ.get("OMP_NUM_THREADS") or os.cpu_count() or 1)
 
     def solve(self, method, rp, ci, val, b, settings=None, x0=None, normB=None, conv=1e-8, maxit=10000):
         s = settings or Settings()

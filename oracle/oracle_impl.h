@@ -17,8 +17,10 @@
 #define FN(name) CAT(name, SFX)
 
 /* y = A x, row by row in stored order (Eigen sparse*dense, row-major;
- * 000_thirdparty/Eigen/src/SparseCore/SparseDenseProduct.h). */
+ * 000_thirdparty/Eigen/src/SparseCore/SparseDenseProduct.h:48-56, whose rows
+ * are split over OpenMP threads; each row's sum is the same either way). */
 static void FN(spmv)(const or_csr *A, const T *restrict v, const T *x, T *y) {
+#pragma omp parallel for schedule(static) if (A->n > 20000)
     for (int i = 0; i < A->n; ++i) {
         T s = 0;
         for (int k = A->rp[i]; k < A->rp[i + 1]; ++k) s += v[k] * x[A->ci[k]];
