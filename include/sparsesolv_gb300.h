@@ -179,6 +179,41 @@ int ssg_spmv(ssg_handle h, const double *x, double *y);
  * number of levels in *nlev */
 int ssg_level_schedule(ssg_handle h, int lower, int32_t *level, int32_t *perm, int *nlev);
 
+/* ---- batches: many systems in shared launches (no counterpart in the reference) ----
+ * Independent systems of uneven sizes, each with one or more right-hand
+ * sides, solved together. Every (system, right-hand side) pair is an instance;
+ * the instances are concatenated into one block-diagonal matrix, so one
+ * launch of each kernel serves all of them, while every instance keeps its
+ * own Krylov scalars, convergence test and iteration count, as if it had been
+ * solved alone by MatSolverICCG / MatSolverMRTR (IC preconditioner) with x0 = 0,
+ * a fixed shift alpha, conv_normalize_type 0 and no diagonal scaling. An
+ * instance's results do not depend on the other instances of its batch.
+ * The systems of one batch are all real or all complex. A right-hand side of a
+ * system is stored as its own instance (the matrix is repeated per
+ * right-hand side). Host buffers; X and B hold n_rhs vectors of n values
+ * one after another (interleaved re, im for SSG_COMPLEX). */
+typedef struct ssg_batch_s *ssg_batch;
+int ssg_batch_create(ssg_batch *out, int device);
+int ssg_batch_destroy(ssg_batch b);
+const char *ssg_batch_last_error(ssg_batch b);
+/* adds a system (CSR as for ssg_set_matrix) and its right-hand sides; *index numbers it */
+int ssg_batch_add(ssg_batch b, int n, int nnz, const int32_t *row_ptr, const int32_t *col, const void *val,
+                  int value_type, int n_rhs, const void *B, int *index);
+int ssg_batch_clear(ssg_batch b);
+/* uploads the systems (first start after add/clear), factors every system with
+ * shift alpha and queues the first iterations; returns without waiting */
+int ssg_batch_start(ssg_batch b, int method, double alpha, double conv, int max_ite);
+/* non-blocking: queues further iterations when the previous ones finished; *done = 1 once every instance ended */
+int ssg_batch_poll(ssg_batch b, int *done);
+int ssg_batch_wait(ssg_batch b);
+/* solution, iteration counts and statuses (ST_* : 1 converged, 2 max_ite, 3 diverged) of system `index`;
+ * returns SSG_OK when all its right-hand sides converged, else SSG_NOT_CONVERGED */
+int ssg_batch_result(ssg_batch b, int index, void *X, int *iters, int *status);
+int ssg_batch_residual_log(ssg_batch b, int index, int rhs, double *log, int capacity, int *length);
+/* set-up and iteration time of the last solve (ms, CUDA events) */
+int ssg_batch_timings(ssg_batch b, double *ms2);
+int ssg_batch_stream(ssg_batch b, void **stream);
+
 /* ---- IC(0) factor that allocates nothing (no counterpart in the reference) ----
  * For callers that may not call cudaMalloc: code that runs under an external
  * memory manager which owns all device memory, or a real-time loop where an

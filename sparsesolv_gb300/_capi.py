@@ -26,7 +26,9 @@ EXPORTED = [
     "ssg_set_matrix_device", "ssg_solve", "ssg_solve_device", "ssg_get_residual_log", "ssg_get_iters",
     "ssg_get_accel_used", "ssg_get_timings", "ssg_factor", "ssg_apply_precond", "ssg_spmv", "ssg_level_schedule",
     "ssg_update_values", "ssg_update_values_device", "ssg_get_stream", "ssg_set_profiling", "ssg_get_kernel_stats",
-    "ssg_launch_count", "ssg_set_tuning", "ssg_ic_factor_noalloc",
+    "ssg_launch_count", "ssg_set_tuning", "ssg_ic_factor_noalloc", "ssg_batch_create", "ssg_batch_destroy",
+    "ssg_batch_last_error", "ssg_batch_add", "ssg_batch_clear", "ssg_batch_start", "ssg_batch_poll", "ssg_batch_wait",
+    "ssg_batch_result", "ssg_batch_residual_log", "ssg_batch_timings", "ssg_batch_stream",
 ]
 NOALLOC_MAX_ROWS = 1 << 21
 TUNE_SWEEP_CTA_PER_SM = 0
@@ -81,6 +83,18 @@ def declare(lib):
         "ssg_launch_count": ([], ctypes.c_longlong),
         "ssg_set_tuning": ([H, I, I], I),
         "ssg_ic_factor_noalloc": ([I, I, P, P, P, P, P, D, I, P], I),
+        "ssg_batch_create": ([ctypes.POINTER(ctypes.c_void_p), I], I),
+        "ssg_batch_destroy": ([H], I),
+        "ssg_batch_last_error": ([H], ctypes.c_char_p),
+        "ssg_batch_add": ([H, I, I, P, P, P, I, I, P, pI], I),
+        "ssg_batch_clear": ([H], I),
+        "ssg_batch_start": ([H, I, D, D, I], I),
+        "ssg_batch_poll": ([H, pI], I),
+        "ssg_batch_wait": ([H], I),
+        "ssg_batch_result": ([H, I, P, P, P], I),
+        "ssg_batch_residual_log": ([H, I, I, P, I, pI], I),
+        "ssg_batch_timings": ([H, P], I),
+        "ssg_batch_stream": ([H, ctypes.POINTER(ctypes.c_void_p)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -263,3 +277,94 @@ class Handle:
         self._check(self.lib.ssg_level_schedule(self.h, 1 if lower else 0, _p(level), _p(perm), ctypes.byref(nlev)),
                     "ssg_level_schedule")
         return level[:self.n], perm[:self.n], nlev.value
+
+
+class Batch:
+    """Many independent systems solved in shared launches (ssg_batch_*)."""
+
+    def __init__(self, device=0):
+        from ._native import load_solver
+        self.lib = load_solver()
+        b = ctypes.c_void_p()
+        rc = self.lib.ssg_batch_create(ctypes.byref(b), int(device))
+        if rc != SSG_OK:
+            raise SolverError(rc, "ssg_batch_create failed")
+        self.b = b
+        self.systems = []  # (n, nrhs, complex)
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.lib.ssg_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc < 0:
+            msg = self.lib.ssg_batch_last_error(self.b)
+            raise SolverError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+        return rc
+
+    def add(self, row_ptr, col, val, B):
+        """B: (n,) or (nrhs, n). Returns the system index."""
+        rp = np.ascontiguousarray(row_ptr, np.int32)
+        ci = np.ascontiguousarray(col, np.int32)
+        cplx = np.iscomplexobj(val) or np.iscomplexobj(B)
+        dt = np.complex128 if cplx else np.float64
+        v = np.ascontiguousarray(val, dt)
+        Bm = np.ascontiguousarray(np.atleast_2d(B), dt)
+        n = len(rp) - 1
+        assert Bm.shape[1] == n
+        idx = ctypes.c_int(-1)
+        self._check(self.lib.ssg_batch_add(self.b, n, len(ci), _p(rp), _p(ci), _p(v), COMPLEX if cplx else REAL,
+                                           Bm.shape[0], _p(Bm), ctypes.byref(idx)), "ssg_batch_add")
+        self.systems.append((n, Bm.shape[0], cplx))
+        return idx.value
+
+    def clear(self):
+        self._check(self.lib.ssg_batch_clear(self.b), "ssg_batch_clear")
+        self.systems = []
+
+    def start(self, method, alpha, conv=1e-8, max_ite=10000):
+        self._check(self.lib.ssg_batch_start(self.b, int(method), float(alpha), float(conv), int(max_ite)),
+                    "ssg_batch_start")
+
+    def poll(self):
+        d = ctypes.c_int(0)
+        self._check(self.lib.ssg_batch_poll(self.b, ctypes.byref(d)), "ssg_batch_poll")
+        return bool(d.value)
+
+    def wait(self):
+        self._check(self.lib.ssg_batch_wait(self.b), "ssg_batch_wait")
+
+    def result(self, index):
+        """(X (nrhs, n), iters (nrhs,), status (nrhs,), all converged)"""
+        n, nrhs, cplx = self.systems[index]
+        X = np.zeros((nrhs, n), np.complex128 if cplx else np.float64)
+        it = np.zeros(nrhs, np.int32)
+        stt = np.zeros(nrhs, np.int32)
+        rc = self._check(self.lib.ssg_batch_result(self.b, int(index), _p(X), _p(it), _p(stt)), "ssg_batch_result")
+        return X, it, stt, rc == SSG_OK
+
+    def residual_log(self, index, rhs=0):
+        ln = ctypes.c_int(0)
+        self._check(self.lib.ssg_batch_residual_log(self.b, int(index), int(rhs), None, 0, ctypes.byref(ln)),
+                    "ssg_batch_residual_log")
+        out = np.zeros(ln.value)
+        self._check(self.lib.ssg_batch_residual_log(self.b, int(index), int(rhs), _p(out), ln.value, ctypes.byref(ln)),
+                    "ssg_batch_residual_log")
+        return out
+
+    def timings(self):
+        t = np.zeros(2)
+        self._check(self.lib.ssg_batch_timings(self.b, _p(t)), "ssg_batch_timings")
+        return t
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        self._check(self.lib.ssg_batch_stream(self.b, ctypes.byref(s)), "ssg_batch_stream")
+        return s.value or 0

@@ -38,6 +38,7 @@ CUDA_SOURCES = [
     "ss_cluster.cu",
     "ss_spmv_vec.cu",
     "ss_solver.cu",
+    "ss_batch.cu",
     "ss_capi.cu",
 ]
 

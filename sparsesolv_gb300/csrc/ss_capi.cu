@@ -2,6 +2,7 @@
 #include <cstring>
 #include <new>
 
+#include "ss_batch.cuh"
 #include "ss_solver.cuh"
 
 using ssg::cplx;
@@ -35,6 +36,30 @@ int guarded(ssg_handle hd, F &&f) {
 }
 
 size_t vbytes(const Handle &h) { return h.vtype == SSG_COMPLEX ? 16 : 8; }
+
+}  // namespace
+
+struct ssg_batch_s {
+    ssg::Batch *b;
+    std::string err;
+};
+
+namespace {
+
+template <typename F>
+int bguarded(ssg_batch bd, F &&f) {
+    if (!bd || !bd->b) return SSG_ERR_ARG;
+    try {
+        SSG_CUDA(cudaSetDevice(bd->b->h.device));
+        return f(*bd->b);
+    } catch (const Error &e) {
+        bd->err = e.msg;
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        bd->err = "host allocation failed";
+        return SSG_ERR_NOMEM;
+    }
+}
 
 }  // namespace
 
@@ -362,6 +387,104 @@ int ssg_level_schedule(ssg_handle hd, int lower, int32_t *level, int32_t *perm, 
         if (perm && h.n)
             SSG_CUDA(cudaMemcpyAsync(perm, T.perm.p, sizeof(int) * (size_t)h.n, cudaMemcpyDeviceToHost, h.stream));
         SSG_CUDA(cudaStreamSynchronize(h.stream));
+        return SSG_OK;
+    });
+}
+
+int ssg_batch_create(ssg_batch *out, int device) {
+    if (!out) return SSG_ERR_ARG;
+    *out = nullptr;
+    ssg_batch_s *bd = new (std::nothrow) ssg_batch_s();
+    if (!bd) return SSG_ERR_NOMEM;
+    try {
+        bd->b = new ssg::Batch(device);
+    } catch (const Error &e) {
+        delete bd;
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        delete bd;
+        return SSG_ERR_NOMEM;
+    }
+    *out = bd;
+    return SSG_OK;
+}
+
+int ssg_batch_destroy(ssg_batch bd) {
+    if (!bd) return SSG_ERR_ARG;
+    if (bd->b) {
+        cudaSetDevice(bd->b->h.device);
+        if (bd->b->running) cudaStreamSynchronize(bd->b->h.stream);
+        delete bd->b;
+    }
+    delete bd;
+    return SSG_OK;
+}
+
+const char *ssg_batch_last_error(ssg_batch bd) { return bd ? bd->err.c_str() : "null batch"; }
+
+int ssg_batch_add(ssg_batch bd, int n, int nnz, const int32_t *rp, const int32_t *ci, const void *val, int value_type,
+                  int n_rhs, const void *B, int *index) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        const int i = b.add(n, nnz, rp, ci, (const double *)val, value_type, n_rhs, (const double *)B);
+        if (index) *index = i;
+        return SSG_OK;
+    });
+}
+
+int ssg_batch_clear(ssg_batch bd) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        b.clear();
+        return SSG_OK;
+    });
+}
+
+int ssg_batch_start(ssg_batch bd, int method, double alpha, double conv, int max_ite) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        if (b.sys.empty()) return SSG_ERR_STATE;
+        if (b.vtype == SSG_COMPLEX)
+            b.start<cplx>(method, alpha, conv, max_ite);
+        else
+            b.start<double>(method, alpha, conv, max_ite);
+        return SSG_OK;
+    });
+}
+
+int ssg_batch_poll(ssg_batch bd, int *done) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        const bool d = b.poll();
+        if (done) *done = d ? 1 : 0;
+        return SSG_OK;
+    });
+}
+
+int ssg_batch_wait(ssg_batch bd) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        b.wait();
+        return SSG_OK;
+    });
+}
+
+int ssg_batch_result(ssg_batch bd, int index, void *X, int *iters, int *status) {
+    return bguarded(bd, [&](ssg::Batch &b) { return b.result(index, (double *)X, iters, status); });
+}
+
+int ssg_batch_residual_log(ssg_batch bd, int index, int rhs, double *log, int capacity, int *length) {
+    return bguarded(bd, [&](ssg::Batch &b) { return b.residual_log(index, rhs, log, capacity, length); });
+}
+
+int ssg_batch_timings(ssg_batch bd, double *ms2) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        if (!ms2) return SSG_ERR_ARG;
+        ms2[0] = b.t_ms.size() > 0 ? b.t_ms[0] : 0.0;
+        ms2[1] = b.t_ms.size() > 1 ? b.t_ms[1] : 0.0;
+        return SSG_OK;
+    });
+}
+
+int ssg_batch_stream(ssg_batch bd, void **stream) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        if (!stream) return SSG_ERR_ARG;
+        *stream = (void *)b.h.stream;
         return SSG_OK;
     });
 }

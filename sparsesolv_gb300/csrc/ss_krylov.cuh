@@ -31,7 +31,7 @@ struct KState {
     int log_enabled;
     int quirks;       // reproduce the reference's IC-MRTR p update
     unsigned int red_count;  // last-block ticket of the fused reductions
-    int pad0;
+    int log_len;             // batched solves: residual-log entries, -1 for it + 1
     double conv_cri, abs_conv_cri, normalizer, best, bad_div_val;
     double last_norm;        // |r| of the latest iteration
     // scalars; complex values use [0] = re, [1] = im

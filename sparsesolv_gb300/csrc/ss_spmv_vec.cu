@@ -8,33 +8,12 @@
 // contiguous stretch of the value and column arrays.
 #include "ss_internal.cuh"
 #include "ss_krylov.cuh"
+#include "ss_kdev.cuh"
 
 namespace ssg {
 
 constexpr int RED_T = 256;
 constexpr int RED_MAXGRID = 2048;
-
-// scalars of KState as T
-template <typename T>
-__device__ __forceinline__ T getS(const double *a);
-template <>
-__device__ __forceinline__ double getS<double>(const double *a) { return a[0]; }
-template <>
-__device__ __forceinline__ cplx getS<cplx>(const double *a) { return {a[0], a[1]}; }
-template <typename T>
-__device__ __forceinline__ void putS(double *a, T v);
-template <>
-__device__ __forceinline__ void putS<double>(double *a, double v) { a[0] = v; a[1] = 0.0; }
-template <>
-__device__ __forceinline__ void putS<cplx>(double *a, cplx v) { a[0] = v.x; a[1] = v.y; }
-template <typename T>
-__device__ __forceinline__ void acc_parts(double *acc, T v);
-template <>
-__device__ __forceinline__ void acc_parts<double>(double *acc, double v) { acc[0] += v; }
-template <>
-__device__ __forceinline__ void acc_parts<cplx>(double *acc, cplx v) { acc[0] += v.x; acc[1] += v.y; }
-template <typename T>
-constexpr int nparts() { return Sc<T>::is_complex ? 2 : 1; }
 
 int red_grid(int n) {
     static int sms = 0;
@@ -104,39 +83,6 @@ __device__ bool grid_reduce(double (&v)[K], double *part, unsigned *counter, dou
     for (int k = 0; k < K; ++k) tot[k] = sh[k][0];
     if (threadIdx.x == 0) *counter = 0;
     return true;
-}
-
-// convergence test, best tracking and divergence judge of one iteration
-// (src/MatSolverICCG.cpp:267-305; identical in the MRTR loops)
-__device__ void decide(KState *st, double pure, double *log) {
-    const double normR = pure / st->normalizer;
-    const int it = st->it + 1;
-    st->it = it;
-    st->last_norm = pure;
-    if (st->log_enabled) log[it] = normR;
-    st->improved = 0;
-    if (normR < st->conv_cri || pure < st->abs_conv_cri) {
-        st->status = ST_CONVERGED;
-        st->active = 0;
-        return;
-    }
-    if (normR < st->best) {
-        st->best = normR;
-        st->improved = 1;
-    }
-    if (st->diverge_type == 1) {
-        if (normR < st->best * st->bad_div_val) st->bad_counter = 0;
-        if (normR >= st->best * st->bad_div_val) st->bad_counter++;
-        if (st->bad_counter >= st->bad_div_count_thres) {
-            st->status = ST_DIVERGED;
-            st->active = 0;
-            return;
-        }
-    }
-    if (it >= st->max_ite) {
-        st->status = ST_MAXIT;
-        st->active = 0;
-    }
 }
 
 // ---------------------------------------------------------------- SpMV
