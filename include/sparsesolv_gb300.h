@@ -156,7 +156,8 @@ int ssg_get_kernel_stats(ssg_handle h, double *ms, long long *launches, double *
 long long ssg_launch_count(void);
 
 /* launch tuning (new; results do not depend on it beyond last-bit rounding) */
-#define SSG_TUNE_SWEEP_CTA_PER_SM 0  /* resident CTAs per SM claiming sweep rows (default 2; 0 = 8) */
+#define SSG_TUNE_SWEEP_CTA_PER_SM 0  /* resident CTAs per SM claiming sweep rows (0, default: from the mean
+                                        level width, 2 for levels of about a thousand rows, up to 16) */
 #define SSG_TUNE_SWEEP_GROUP 1       /* lanes per row in the sweeps: 0 auto, 4, 8, 16, 32 */
 #define SSG_TUNE_SWEEP_BACKOFF_NS 2  /* sleep between polls of an unsolved entry */
 #define SSG_TUNE_FACTOR_BACKOFF_NS 3 /* sleep between polls of an unfinished factor row */
@@ -199,6 +200,8 @@ const char *ssg_batch_last_error(ssg_batch b);
 /* adds a system (CSR as for ssg_set_matrix) and its right-hand sides; *index numbers it */
 int ssg_batch_add(ssg_batch b, int n, int nnz, const int32_t *row_ptr, const int32_t *col, const void *val,
                   int value_type, int n_rhs, const void *B, int *index);
+/* replaces the n_rhs right-hand sides of system `index` for the next start (the others stay on the device) */
+int ssg_batch_set_rhs(ssg_batch b, int index, const void *B);
 int ssg_batch_clear(ssg_batch b);
 /* uploads the systems (first start after add/clear), factors every system with
  * shift alpha and queues the first iterations; returns without waiting */
@@ -213,6 +216,9 @@ int ssg_batch_residual_log(ssg_batch b, int index, int rhs, double *log, int cap
 /* set-up and iteration time of the last solve (ms, CUDA events) */
 int ssg_batch_timings(ssg_batch b, double *ms2);
 int ssg_batch_stream(ssg_batch b, void **stream);
+/* per-kernel-class event timing of the batch's solves, as ssg_set_profiling / ssg_get_kernel_stats */
+int ssg_batch_set_profiling(ssg_batch b, int enable);
+int ssg_batch_kernel_stats(ssg_batch b, double *ms, long long *launches, double *bytes, int capacity);
 
 /* ---- IC(0) factor that allocates nothing (no counterpart in the reference) ----
  * For callers that may not call cudaMalloc: code that runs under an external

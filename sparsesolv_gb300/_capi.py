@@ -27,8 +27,9 @@ EXPORTED = [
     "ssg_get_accel_used", "ssg_get_timings", "ssg_factor", "ssg_apply_precond", "ssg_spmv", "ssg_level_schedule",
     "ssg_update_values", "ssg_update_values_device", "ssg_get_stream", "ssg_set_profiling", "ssg_get_kernel_stats",
     "ssg_launch_count", "ssg_set_tuning", "ssg_ic_factor_noalloc", "ssg_batch_create", "ssg_batch_destroy",
-    "ssg_batch_last_error", "ssg_batch_add", "ssg_batch_clear", "ssg_batch_start", "ssg_batch_poll", "ssg_batch_wait",
+    "ssg_batch_last_error", "ssg_batch_add", "ssg_batch_set_rhs", "ssg_batch_clear", "ssg_batch_start", "ssg_batch_poll", "ssg_batch_wait",
     "ssg_batch_result", "ssg_batch_residual_log", "ssg_batch_timings", "ssg_batch_stream",
+    "ssg_batch_set_profiling", "ssg_batch_kernel_stats",
 ]
 NOALLOC_MAX_ROWS = 1 << 21
 TUNE_SWEEP_CTA_PER_SM = 0
@@ -87,6 +88,7 @@ def declare(lib):
         "ssg_batch_destroy": ([H], I),
         "ssg_batch_last_error": ([H], ctypes.c_char_p),
         "ssg_batch_add": ([H, I, I, P, P, P, I, I, P, pI], I),
+        "ssg_batch_set_rhs": ([H, I, P], I),
         "ssg_batch_clear": ([H], I),
         "ssg_batch_start": ([H, I, D, D, I], I),
         "ssg_batch_poll": ([H, pI], I),
@@ -95,6 +97,8 @@ def declare(lib):
         "ssg_batch_residual_log": ([H, I, I, P, I, pI], I),
         "ssg_batch_timings": ([H, P], I),
         "ssg_batch_stream": ([H, ctypes.POINTER(ctypes.c_void_p)], I),
+        "ssg_batch_set_profiling": ([H, I], I),
+        "ssg_batch_kernel_stats": ([H, P, P, P, I], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -325,6 +329,12 @@ class Batch:
         self.systems.append((n, Bm.shape[0], cplx))
         return idx.value
 
+    def set_rhs(self, index, B):
+        n, nrhs, cplx = self.systems[index]
+        Bm = np.ascontiguousarray(np.atleast_2d(B), np.complex128 if cplx else np.float64)
+        assert Bm.shape == (nrhs, n)
+        self._check(self.lib.ssg_batch_set_rhs(self.b, int(index), _p(Bm)), "ssg_batch_set_rhs")
+
     def clear(self):
         self._check(self.lib.ssg_batch_clear(self.b), "ssg_batch_clear")
         self.systems = []
@@ -368,3 +378,15 @@ class Batch:
         s = ctypes.c_void_p()
         self._check(self.lib.ssg_batch_stream(self.b, ctypes.byref(s)), "ssg_batch_stream")
         return s.value or 0
+
+    def set_profiling(self, on):
+        self._check(self.lib.ssg_batch_set_profiling(self.b, 1 if on else 0), "ssg_batch_set_profiling")
+
+    def kernel_stats(self):
+        """{class: (ms, launches, algorithmic bytes)} since profiling was switched on"""
+        k = len(KERNEL_CLASSES)
+        ms = np.zeros(k)
+        ln = np.zeros(k, np.int64)
+        by = np.zeros(k)
+        self._check(self.lib.ssg_batch_kernel_stats(self.b, _p(ms), _p(ln), _p(by), k), "ssg_batch_kernel_stats")
+        return {c: (float(ms[i]), int(ln[i]), float(by[i])) for i, c in enumerate(KERNEL_CLASSES)}

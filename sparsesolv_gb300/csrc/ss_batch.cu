@@ -390,7 +390,16 @@ int Batch::add(int n, int nnz, const int *rp, const int *ci, const double *val, 
     sys.push_back(std::move(S_));
     vtype = vt;
     assembled = false;
+    rhs_dirty = true;
     return (int)sys.size() - 1;
+}
+
+void Batch::set_rhs(int index, const double *B) {
+    if (running) throw Error{SSG_ERR_STATE, "batch is running"};
+    if (index < 0 || index >= (int)sys.size() || !B) throw Error{SSG_ERR_ARG, "bad system index"};
+    BatchSystem &q = sys[index];
+    std::memcpy(q.B.data(), B, sizeof(double) * q.B.size());
+    rhs_dirty = true;
 }
 
 void Batch::clear() {
@@ -499,8 +508,8 @@ void Batch::start(int method_, double alpha, double conv, int max_ite_) {
     d_logs.ensure(sizeof(double) * (size_t)S * (size_t)(max_ite + 2));
     T *b = h.vec[0].as<T>(), *r = h.vec[1].as<T>(), *p = h.vec[2].as<T>(), *z = h.vec[3].as<T>();
     T *u = h.vec[4].as<T>(), *y = h.vec[5].as<T>(), *x = h.vec[8].as<T>();
-    // right-hand sides of all instances, staged through pinned memory
-    {
+    // right-hand sides of all instances, uploaded when they changed (they stay resident otherwise)
+    if (rhs_dirty) {
         const int w = vtype == SSG_COMPLEX ? 2 : 1;
         std::vector<double> stage((size_t)w * n);
         for (int q = 0; q < S; ++q) {
@@ -510,6 +519,7 @@ void Batch::start(int method_, double alpha, double conv, int max_ite_) {
         }
         SSG_CUDA(cudaMemcpyAsync(b, stage.data(), sizeof(T) * (size_t)n, cudaMemcpyHostToDevice, s));
         SSG_CUDA(cudaStreamSynchronize(s));
+        rhs_dirty = false;
     }
     for (int q = 0; q < S; ++q) {
         KState &k = h_st[q];
@@ -533,13 +543,21 @@ void Batch::start(int method_, double alpha, double conv, int max_ite_) {
     SSG_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, s));
     BDev B = dev_view();
     const int grid = bgrid(NT);
-    k_bsetup<T><<<grid, BT, 0, s>>>(B, b);
-    SSG_LAUNCHED();
+    const double nv = (double)sizeof(T) * n;
+    h.prof.iter = 0;
+    h.prof.pre = true;
+    iter_no = 0;
+    h.timed(PC_VEC, nv, [&] {
+        k_bsetup<T><<<grid, BT, 0, s>>>(B, b);
+        SSG_LAUNCHED();
+    });
     if (method == SSG_METHOD_ICCG) {
         h.apply_precond<T>(r, z, ctl());
         SSG_CUDA(cudaMemcpyAsync(p, z, sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, s));
-        k_brur0<T><<<grid, BT, 0, s>>>(B, r, z);
-        SSG_LAUNCHED();
+        h.timed(PC_VEC, 2 * nv, [&] {
+            k_brur0<T><<<grid, BT, 0, s>>>(B, r, z);
+            SSG_LAUNCHED();
+        });
     } else {
         h.apply_precond<T>(r, u, ctl());
         vec_neg<T>(n, r, y, s);
@@ -564,30 +582,51 @@ void Batch::queue_chunk() {
     T *r = h.vec[1].as<T>(), *p = h.vec[2].as<T>(), *z = h.vec[3].as<T>(), *u = h.vec[4].as<T>();
     T *y = h.vec[5].as<T>(), *v = h.vec[6].as<T>(), *w = h.vec[7].as<T>(), *x = h.vec[8].as<T>();
     const int todo = std::min(chunk, max_ite - queued);
+    const double nv = (double)sizeof(T) * n;
+    const double spmv_bytes = (4.0 + sizeof(T)) * h.nnz + 4.0 * (n + 1) + 2.0 * nv;
     for (int c = 0; c < todo; ++c) {
+        h.prof.iter = ++iter_no;
+        h.prof.pre = true;
         if (method == SSG_METHOD_ICCG) {
-            k_bspmv<T, true><<<grid, BT, 0, s>>>(B, rp, ci, aval, p, v);
-            SSG_LAUNCHED();
-            k_biccg_update<T><<<grid, BT, 0, s>>>(B, x, r, p, v);
-            SSG_LAUNCHED();
+            h.timed(PC_SPMV, spmv_bytes, [&] {
+                k_bspmv<T, true><<<grid, BT, 0, s>>>(B, rp, ci, aval, p, v);
+                SSG_LAUNCHED();
+            });
+            h.timed(PC_VEC, 6 * nv, [&] {
+                k_biccg_update<T><<<grid, BT, 0, s>>>(B, x, r, p, v);
+                SSG_LAUNCHED();
+            });
+            h.prof.pre = false;
             h.apply_precond<T>(r, z, ctl());
-            k_biccg_beta<T><<<grid, BT, 0, s>>>(B, r, z);
-            SSG_LAUNCHED();
-            k_biccg_p<T><<<grid, BT, 0, s>>>(B, p, z);
-            SSG_LAUNCHED();
+            h.timed(PC_VEC, 2 * nv, [&] {
+                k_biccg_beta<T><<<grid, BT, 0, s>>>(B, r, z);
+                SSG_LAUNCHED();
+            });
+            h.timed(PC_VEC, 3 * nv, [&] {
+                k_biccg_p<T><<<grid, BT, 0, s>>>(B, p, z);
+                SSG_LAUNCHED();
+            });
         } else {
-            k_bspmv<T, false><<<grid, BT, 0, s>>>(B, rp, ci, aval, u, v);
-            SSG_LAUNCHED();
+            h.timed(PC_SPMV, spmv_bytes, [&] {
+                k_bspmv<T, false><<<grid, BT, 0, s>>>(B, rp, ci, aval, u, v);
+                SSG_LAUNCHED();
+            });
             h.apply_precond<T>(v, w, ctl());
-            k_bmrtr_dots<T><<<grid, BT, 0, s>>>(B, w, r, v, y);
-            SSG_LAUNCHED();
-            k_bmrtr_update<T><<<grid, BT, 0, s>>>(B, p, u, x, y, v, r);
-            SSG_LAUNCHED();
-            k_bmrtr_zu<T><<<grid, BT, 0, s>>>(B, z, w, u);
-            SSG_LAUNCHED();
+            h.timed(PC_VEC, 4 * nv, [&] {
+                k_bmrtr_dots<T><<<grid, BT, 0, s>>>(B, w, r, v, y);
+                SSG_LAUNCHED();
+            });
+            h.timed(PC_VEC, 10 * nv, [&] {
+                k_bmrtr_update<T><<<grid, BT, 0, s>>>(B, p, u, x, y, v, r);
+                SSG_LAUNCHED();
+            });
+            h.prof.pre = false;
+            h.timed(PC_VEC, 5 * nv, [&] {
+                k_bmrtr_zu<T><<<grid, BT, 0, s>>>(B, z, w, u);
+                SSG_LAUNCHED();
+            });
         }
     }
-    (void)n;
     queued += todo;
     chunk = std::min(chunk * 2, 32);
     SSG_CUDA(cudaMemcpyAsync(h_ctl, ctl(), sizeof(KState), cudaMemcpyDeviceToHost, s));
@@ -611,6 +650,10 @@ bool Batch::poll() {
     SSG_CUDA(cudaMemcpyAsync(h_st, d_st.p, sizeof(KState) * (size_t)S, cudaMemcpyDeviceToHost, s));
     SSG_CUDA(cudaEventRecord(ev[2], s));
     SSG_CUDA(cudaStreamSynchronize(s));
+    int most = 0;
+    for (int q = 0; q < S; ++q) most = std::max(most, h_st[q].it);
+    h.prof_flush(most);
+    h.prof.iter = 0;
     float a = 0.f, b = 0.f;
     cudaEventElapsedTime(&a, ev[0], ev[1]);
     cudaEventElapsedTime(&b, ev[1], ev[2]);

@@ -52,13 +52,14 @@ struct Batch {
     std::vector<int> inst_sys, inst_rhs, inst_row;  // per instance; inst_row has S + 1 entries
     int S = 0, NT = 0;
     bool assembled = false;
+    bool rhs_dirty = true;  // right-hand sides changed since the last upload
     DBuf d_tile, d_tile_sys, d_sys_tile, d_sys_row, d_st, d_part, d_logs, d_ctl_counter;
     KState *h_st = nullptr;   // pinned copy of the instance states
     KState *h_ctl = nullptr;  // pinned copy of the control state
     cudaEvent_t ev_chunk = nullptr;
     // the running solve
     int method = SSG_METHOD_ICCG;
-    int max_ite = 0, queued = 0, chunk = 2;
+    int max_ite = 0, queued = 0, chunk = 2, iter_no = 0;
     bool running = false, log_on = true;
     std::vector<double> t_ms;  // set-up, iterations (ms) of the last solve
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
@@ -67,6 +68,7 @@ struct Batch {
     ~Batch();
     int add(int n, int nnz, const int *rp, const int *ci, const double *val, int vt, int nrhs, const double *B);
     void clear();
+    void set_rhs(int index, const double *B);
     void assemble();
     BDev dev_view();
     KState *ctl();

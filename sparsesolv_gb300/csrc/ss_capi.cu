@@ -431,6 +431,13 @@ int ssg_batch_add(ssg_batch bd, int n, int nnz, const int32_t *rp, const int32_t
     });
 }
 
+int ssg_batch_set_rhs(ssg_batch bd, int index, const void *B) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        b.set_rhs(index, (const double *)B);
+        return SSG_OK;
+    });
+}
+
 int ssg_batch_clear(ssg_batch bd) {
     return bguarded(bd, [&](ssg::Batch &b) {
         b.clear();
@@ -477,6 +484,32 @@ int ssg_batch_timings(ssg_batch bd, double *ms2) {
         if (!ms2) return SSG_ERR_ARG;
         ms2[0] = b.t_ms.size() > 0 ? b.t_ms[0] : 0.0;
         ms2[1] = b.t_ms.size() > 1 ? b.t_ms[1] : 0.0;
+        return SSG_OK;
+    });
+}
+
+int ssg_batch_set_profiling(ssg_batch bd, int enable) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        Handle &h = b.h;
+        h.prof.on = enable != 0;
+        for (int c = 0; c < ssg::PC_N; ++c) {
+            h.prof.ms[c] = 0.0;
+            h.prof.launches[c] = 0;
+            h.prof.bytes[c] = 0.0;
+        }
+        h.prof.recs.clear();
+        h.prof.used = 0;
+        return SSG_OK;
+    });
+}
+
+int ssg_batch_kernel_stats(ssg_batch bd, double *ms, long long *launches, double *bytes, int cap) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        for (int c = 0; c < ssg::PC_N && c < cap; ++c) {
+            if (ms) ms[c] = b.h.prof.ms[c];
+            if (launches) launches[c] = b.h.prof.launches[c];
+            if (bytes) bytes[c] = b.h.prof.bytes[c];
+        }
         return SSG_OK;
     });
 }

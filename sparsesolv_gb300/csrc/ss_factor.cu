@@ -294,7 +294,10 @@ void ic_factor(const Tri &L, T *lval, T *D, double alpha, int *d_err, int *d_tic
     SSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     if (dep && max_row <= FF_MAXROW) {
         constexpr int W = ff_warps<T>();
-        const int blocks = min(div_up(L.n, W), sms * factor_blocks_per_sm);
+        // wide levels (batches of many systems) keep more rows in flight
+        const double width = L.nlev > 0 ? (double)L.n / L.nlev : (double)L.n;
+        const int per_sm = width >= 8192.0 ? 6 : factor_blocks_per_sm;
+        const int blocks = min(div_up(L.n, W), sms * per_sm);
         k_ic_factor_fast<T><<<blocks, W * 32, 0, s>>>(L.n, L.perm.as<int>(), L.prp.as<int>(), L.pci.as<int>(), dep,
                                                       lval, D, done, alpha, d_ticket, d_err, backoff_ns);
     } else {

@@ -108,7 +108,7 @@ void sweep(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, c
            int *d_ticket, int *d_err, cudaStream_t s);
 // launch shape of the sweeps (tunable; 0 = automatic)
 struct SweepCfg {
-    int cta_per_sm = 2;   // resident CTAs per SM claiming rows
+    int cta_per_sm = 0;   // resident CTAs per SM claiming rows (0: from the mean level width)
     int group = 0;        // lanes per row: 4, 8, 16 or 32 (0: from the mean row length)
     int backoff_ns = 0;   // __nanosleep between polls of an unsolved entry
 };

@@ -196,7 +196,15 @@ void sweep_st(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux
     if (tri.n == 0) return;
     SSG_CUDA(cudaMemsetAsync(d_ticket, 0, sizeof(int), s));
     const int G = cfg.group ? cfg.group : sweep_group(tri);
-    const int grid = sweep_grid(tri.n, SW_THREADS / G, cfg.cta_per_sm);
+    int cps = cfg.cta_per_sm;
+    if (cps <= 0) {
+        // rows in flight from the mean level width: two CTAs per SM (4,864 rows at
+        // G = 8) keep levels of about a thousand rows busy with the least polling;
+        // wide levels (batches of many systems) need more rows in flight
+        const double width = tri.nlev > 0 ? (double)tri.n / tri.nlev : (double)tri.n;
+        cps = width <= 1024.0 ? 2 : (width >= 8192.0 ? 16 : (int)(width / 512.0));
+    }
+    const int grid = sweep_grid(tri.n, SW_THREADS / G, cps);
     if (G == 8)
         launch_sweep<T, 8>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, dinv, cfg.backoff_ns, s);
     else if (G == 16)

@@ -147,6 +147,13 @@ def test_zero_rhs_and_repeated_start(gpu, systems):
             assert ok and it[1] == 0 and np.all(X[1] == 0)
             assert list(bt.residual_log(0, 1)) == [0.0]
             assert it[0] > 5
+        # swapped right-hand sides through set_rhs: the results swap with them
+        bt.set_rhs(0, B[::-1])
+        bt.start(_capi.METHOD_ICCG, ALPHA, conv=1e-8, max_ite=5000)
+        bt.wait()
+        X2, it2, _, ok2 = bt.result(0)
+        assert ok2 and it2[0] == 0 and np.all(X2[0] == 0)
+        assert np.array_equal(X2[1], X[0]) and it2[1] == it[0]
     finally:
         bt.close()
 
