@@ -50,7 +50,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--method", default="iccg", choices=["iccg", "sgs", "mrtr_ic"])
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg4"])
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="mixed: FP32 inner solves inside FP64 refinement on the true residual")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sweep-mode", type=int, default=0, choices=[0, 1, 2],
                     help="triangular sweeps: 0 automatic, 1 sync-free, 2 one-cluster level-synchronous")
@@ -61,6 +63,8 @@ def workload(name):
     from sparsesolv_gb300 import voxel
     if name == "cfg2":
         case, label = voxel.config2(), "curl-curl 80^3 voxels, 3 seeded iron blocks"
+    elif name == "cfg3":
+        case, label = voxel.config3(), "eddy-current K + j omega sigma M, 60^3 voxels, complex128"
     else:
         case, label = voxel.config1(), "curl-curl 20^3 voxels, 1 seeded iron block"
     rp, ci, val, b = case.assemble()
@@ -224,19 +228,22 @@ def run_ours(args):
     meth, pt, mname = method_args(args.method)
     n, nnz = len(rp) - 1, len(ci)
     dev = torch.device("cuda", local)
+    cplx = np.iscomplexobj(val)
+    tdt = torch.complex128 if cplx else torch.float64
     # device-resident inputs
     val_d = torch.from_numpy(val).to(dev)
     b_d = torch.from_numpy(b).to(dev)
-    x_d = torch.zeros(n, dtype=torch.float64, device=dev)
+    x_d = torch.zeros(n, dtype=tdt, device=dev)
     # pinned host buffers for the end-to-end path
     val_h = torch.from_numpy(val).pin_memory()
     b_h = torch.from_numpy(b).pin_memory()
-    x_h = torch.zeros(n, dtype=torch.float64).pin_memory()
+    x_h = torch.zeros(n, dtype=tdt).pin_memory()
     h = _capi.Handle(local)
     o = h.default_options()
     o.accel_factor = ALPHA
     o.precondition_type = pt
     o.is_save_residual_log = 1
+    o.precision = _capi.PREC_MIXED if args.precision == "mixed" else _capi.PREC_FP64
     h.set_options(o)
     h.set_tuning(_capi.TUNE_SWEEP_MODE, args.sweep_mode)
     h.set_matrix(rp, ci, val)
@@ -314,8 +321,11 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded voxel generator)",
+        "vs_baseline": None,
+        "dtype": ("c128" if cplx else "f64") + ("+fp32-inner" if args.precision == "mixed" else ""),
+        "data": "synthetic (seeded voxel generator)",
         "config": {"workload": label, "n": n, "nnz": nnz, "method": mname, "alpha": ALPHA, "tolerance": TOL,
+                   "precision": args.precision,
                    "iterations": iters, "parallelism": "replicas only" if ws > 1 else "single GPU",
                    "factor": "recomputed every step",
                    "sweep_mode": ["automatic", "sync-free", "one-cluster"][args.sweep_mode], "level_schedule": "computed once per sparsity pattern",
@@ -324,8 +334,8 @@ def run_ours(args):
         "time_to_tolerance_s": ms_max / args.steps / 1e3,
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
                        "steps": len(step_ms)},
-        "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": 8 * nnz + 16 * n,
-                "d2h_bytes_per_step": 8 * n},
+        "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": val.itemsize * nnz + 2 * b.itemsize * n,
+                "d2h_bytes_per_step": b.itemsize * n},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
@@ -369,6 +379,7 @@ def run_batch(args):
         case, coils = cases[i]
         systems.append(case.assemble(coils_list=coils))
     bt = _capi.Batch(local)
+    bt.set_precision(_capi.PREC_MIXED if args.precision == "mixed" else _capi.PREC_FP64)
     for rp, ci, va, B in systems:
         bt.add(rp, ci, va, B)
     inst = sum(len(B) for _, _, _, B in systems)
@@ -456,10 +467,12 @@ def run_batch(args):
         "metric": "batched solves/s (one solve = one system x right-hand side to 1e-8)", "value": value,
         "unit": "solves/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded voxel generator)",
+        "dtype": "f64" + ("+fp32-inner" if args.precision == "mixed" else ""),
+        "data": "synthetic (seeded voxel generator)",
         "config": {"workload": "256 curl-curl systems, N ~ U{8..32} voxels, 4 coil right-hand sides each",
                    "instances": total_inst, "rows": int(sum(len(B) * (len(rp) - 1) for rp, _, _, B in systems)),
                    "method": "shifted ICCG", "alpha": ALPHA, "tolerance": TOL, "converged": conv_all,
+                   "precision": args.precision,
                    "iterations": {"min": min(iters), "median": float(np.median(iters)), "max": max(iters)},
                    "factor": "recomputed every step", "pattern_analysis_s": t_first,
                    "parallelism": "replicas only" if ws > 1 else "single GPU"},

@@ -83,7 +83,17 @@ typedef struct ssg_handle_s *ssg_handle;
 /* precision modes (build addition; does not change the method) */
 #define SSG_PREC_FP64 0  /* everything in FP64, as the reference */
 #define SSG_PREC_MIXED 1 /* FP32 factor, SpMV and sweeps inside an inner loop,
-                            FP64 outer residual and iterative refinement */
+                            FP64 outer residual and iterative refinement: the IC factor
+                            and its shift are computed in FP64 and rounded; each inner
+                            ICCG / IC-MRTR (FP32 vectors, FP64 scalars) reduces the
+                            scaled residual r/|r| by 1e-4 (real) or 1e-2 (complex), or
+                            ends after 30 iterations without a 1% gain (FP32 rounding
+                            bounds what one inner solve can reach); x += |r| d and r = b - A x
+                            run in FP64 until |b - A x| / |b| < conv_cri (a true
+                            residual). ssg_solve: ICCG or IC-MRTR, accel_factor > 0,
+                            is_init = 1, conv_normalize_type 0, no diagonal scaling;
+                            iterations count inner iterations, the residual log holds
+                            |b - A x| / |b| after each refinement step. */
 
 /*
  * Settings with the reference's defaults (src/MatSolverBase.cpp:32-47,
@@ -215,6 +225,8 @@ int ssg_batch_result(ssg_batch b, int index, void *X, int *iters, int *status);
 int ssg_batch_residual_log(ssg_batch b, int index, int rhs, double *log, int capacity, int *length);
 /* set-up and iteration time of the last solve (ms, CUDA events) */
 int ssg_batch_timings(ssg_batch b, double *ms2);
+/* SSG_PREC_FP64 (default) or SSG_PREC_MIXED (see above) for the next start; inner_tol <= 0: 1e-4 real, 1e-2 complex */
+int ssg_batch_set_precision(ssg_batch b, int precision, double inner_tol);
 int ssg_batch_stream(ssg_batch b, void **stream);
 /* per-kernel-class event timing of the batch's solves, as ssg_set_profiling / ssg_get_kernel_stats */
 int ssg_batch_set_profiling(ssg_batch b, int enable);

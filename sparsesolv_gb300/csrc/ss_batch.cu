@@ -120,7 +120,7 @@ template <typename T>
 __global__ void __launch_bounds__(BT) k_brur0(BDev B, const T *r, const T *z) {
     if (!B.ctl->active) return;
     for (int t = blockIdx.x; t < B.NT; t += gridDim.x) {
-        if (!B.st[B.tile_sys[t]].active) continue;
+        if (!B.act[(size_t)B.tile_sys[t] * B.act_stride]) continue;
         const int2 tr = B.tile[t];
         double acc[2] = {0.0, 0.0};
         for (int i = tr.x + threadIdx.x; i < tr.y; i += BT) acc_parts<T>(acc, r[i] * z[i]);
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(BT) k_bspmv(BDev B, const int *__restrict__ rp
     constexpr int G = 8, RPB = BT / G;
     const int g = threadIdx.x / G, gl = threadIdx.x % G;
     for (int t = blockIdx.x; t < B.NT; t += gridDim.x) {
-        if (!B.st[B.tile_sys[t]].active) continue;
+        if (!B.act[(size_t)B.tile_sys[t] * B.act_stride]) continue;
         const int2 tr = B.tile[t];
         double acc2[2] = {0.0, 0.0};
         for (int row0 = tr.x; row0 < tr.y; row0 += RPB) {
@@ -176,7 +176,8 @@ __global__ void __launch_bounds__(BT) k_bspmv(BDev B, const int *__restrict__ rp
         inst_sum<2>(B, s, tot);
         st->dots[0] = tot[0];
         st->dots[1] = tot[1];
-        putS<T>(st->alpha, getS<T>(st->rur0) / getS<T>(tot));
+        using W = typename Wide<T>::type;
+        putS<W>(st->alpha, getS<W>(st->rur0) / getS<W>(tot));
     }
     __syncthreads();
     if (threadIdx.x == 0) *B.counter = 0u;
@@ -187,8 +188,8 @@ template <typename T>
 __global__ void __launch_bounds__(BT) k_biccg_update(BDev B, T *x, T *r, const T *p, const T *ap) {
     if (!B.ctl->active) return;
     for (int t = blockIdx.x; t < B.NT; t += gridDim.x) {
+        if (!B.act[(size_t)B.tile_sys[t] * B.act_stride]) continue;
         const KState *st = B.st + B.tile_sys[t];
-        if (!st->active) continue;
         const T alpha = getS<T>(st->alpha);
         const int2 tr = B.tile[t];
         double acc[1] = {0.0};
@@ -215,7 +216,7 @@ template <typename T>
 __global__ void __launch_bounds__(BT) k_biccg_beta(BDev B, const T *r, const T *z) {
     if (!B.ctl->active) return;
     for (int t = blockIdx.x; t < B.NT; t += gridDim.x) {
-        if (!B.st[B.tile_sys[t]].active) continue;
+        if (!B.act[(size_t)B.tile_sys[t] * B.act_stride]) continue;
         const int2 tr = B.tile[t];
         double acc[2] = {0.0, 0.0};
         for (int i = tr.x + threadIdx.x; i < tr.y; i += BT) acc_parts<T>(acc, r[i] * z[i]);
@@ -227,9 +228,10 @@ __global__ void __launch_bounds__(BT) k_biccg_beta(BDev B, const T *r, const T *
         if (!st->active) continue;
         double tot[2];
         inst_sum<2>(B, s, tot);
-        const T rur1 = getS<T>(tot);
-        putS<T>(st->beta, rur1 / getS<T>(st->rur0));
-        putS<T>(st->rur0, rur1);
+        using W = typename Wide<T>::type;
+        const W rur1 = getS<W>(tot);
+        putS<W>(st->beta, rur1 / getS<W>(st->rur0));
+        putS<W>(st->rur0, rur1);
     }
     __syncthreads();
     if (threadIdx.x == 0) *B.counter = 0u;
@@ -239,8 +241,8 @@ template <typename T>
 __global__ void __launch_bounds__(BT) k_biccg_p(BDev B, T *p, const T *z) {
     if (!B.ctl->active) return;
     for (int t = blockIdx.x; t < B.NT; t += gridDim.x) {
+        if (!B.act[(size_t)B.tile_sys[t] * B.act_stride]) continue;
         const KState *st = B.st + B.tile_sys[t];
-        if (!st->active) continue;
         const T beta = getS<T>(st->beta);
         const int2 tr = B.tile[t];
         for (int i = tr.x + threadIdx.x; i < tr.y; i += BT) p[i] = p[i] * beta + z[i];
@@ -252,7 +254,7 @@ template <typename T>
 __global__ void __launch_bounds__(BT) k_bmrtr_dots(BDev B, const T *a, const T *b, const T *c, const T *y) {
     if (!B.ctl->active) return;
     for (int t = blockIdx.x; t < B.NT; t += gridDim.x) {
-        if (!B.st[B.tile_sys[t]].active) continue;
+        if (!B.act[(size_t)B.tile_sys[t] * B.act_stride]) continue;
         const int2 tr = B.tile[t];
         double acc[6] = {0, 0, 0, 0, 0, 0};
         for (int i = tr.x + threadIdx.x; i < tr.y; i += BT) {
@@ -269,26 +271,27 @@ __global__ void __launch_bounds__(BT) k_bmrtr_dots(BDev B, const T *a, const T *
         if (!st->active) continue;
         double tot[6];
         inst_sum<6>(B, s, tot);
-        const T wr = getS<T>(tot + 0), vw = getS<T>(tot + 2), wy = getS<T>(tot + 4);
+        using W = typename Wide<T>::type;
+        const W wr = getS<W>(tot + 0), vw = getS<W>(tot + 2), wy = getS<W>(tot + 4);
         for (int k = 0; k < 6; ++k) st->dots[k] = tot[k];
-        T zeta, eta, nu = getS<T>(st->nu), zeta_old = getS<T>(st->zeta_old);
+        W zeta, eta, nu = getS<W>(st->nu), zeta_old = getS<W>(st->zeta_old);
         if (st->it == 0) {
             zeta = wr / vw;
             zeta_old = zeta;
-            eta = Sc<T>::zero();
+            eta = Sc<W>::zero();
         } else {
-            const T temp0 = Sc<T>::one() / (nu * vw - wy * wy);
+            const W temp0 = Sc<W>::one() / (nu * vw - wy * wy);
             zeta = nu * wr * temp0;
             eta = (-1.0 * wy) * wr * temp0;
         }
         nu = zeta * wr;
-        const T ptemp = eta * zeta_old / zeta;
+        const W ptemp = eta * zeta_old / zeta;
         zeta_old = zeta;
-        putS<T>(st->zeta, zeta);
-        putS<T>(st->eta, eta);
-        putS<T>(st->nu, nu);
-        putS<T>(st->ptemp, ptemp);
-        putS<T>(st->zeta_old, zeta_old);
+        putS<W>(st->zeta, zeta);
+        putS<W>(st->eta, eta);
+        putS<W>(st->nu, nu);
+        putS<W>(st->ptemp, ptemp);
+        putS<W>(st->zeta_old, zeta_old);
     }
     __syncthreads();
     if (threadIdx.x == 0) *B.counter = 0u;
@@ -298,8 +301,8 @@ template <typename T>
 __global__ void __launch_bounds__(BT) k_bmrtr_update(BDev B, T *p, const T *u, T *x, T *y, const T *v, T *r) {
     if (!B.ctl->active) return;
     for (int t = blockIdx.x; t < B.NT; t += gridDim.x) {
+        if (!B.act[(size_t)B.tile_sys[t] * B.act_stride]) continue;
         const KState *st = B.st + B.tile_sys[t];
-        if (!st->active) continue;
         const T zeta = getS<T>(st->zeta), eta = getS<T>(st->eta), pt = getS<T>(st->ptemp);
         const int2 tr = B.tile[t];
         double acc[1] = {0.0};
@@ -330,8 +333,8 @@ template <typename T>
 __global__ void __launch_bounds__(BT) k_bmrtr_zu(BDev B, T *z, const T *w, T *u) {
     if (!B.ctl->active) return;
     for (int t = blockIdx.x; t < B.NT; t += gridDim.x) {
+        if (!B.act[(size_t)B.tile_sys[t] * B.act_stride]) continue;
         const KState *st = B.st + B.tile_sys[t];
-        if (!st->active) continue;
         const T zeta = getS<T>(st->zeta), eta = getS<T>(st->eta);
         const int2 tr = B.tile[t];
         for (int i = tr.x + threadIdx.x; i < tr.y; i += BT) {
@@ -339,6 +342,153 @@ __global__ void __launch_bounds__(BT) k_bmrtr_zu(BDev B, T *z, const T *w, T *u)
             z[i] = zi;
             u[i] = u[i] - zi;
         }
+    }
+}
+
+// ---------------------------------------------------------------- mixed precision
+// FP64 refinement around FP32 inner solves: per instance, r = b - A x in FP64,
+// the inner solver (ICCG or IC-MRTR on FP32 copies of A and of the IC factor,
+// FP32 vectors, FP64 scalars) reduces the scaled residual r / |r| by the inner
+// tolerance, and x += |r| d in FP64, until |b - A x| / |b| reaches the
+// tolerance. The factor and its shift are computed in FP64 and then rounded.
+constexpr int MAX_OUTER = 40;
+
+template <typename T, typename Ti>
+__global__ void k_narrow(size_t n, const T *src, Ti *dst) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = to_lo(src[i]);
+}
+
+__device__ __forceinline__ void inner_reset(KState *st, double eta, int inner_max) {
+    st->active = inner_max > 0 ? 1 : 0;
+    st->status = inner_max > 0 ? ST_RUNNING : ST_MAXIT;
+    st->it = 0;
+    st->conv_cri = eta;
+    st->normalizer = 1.0;  // the inner right-hand side is scaled to unit norm
+    st->abs_conv_cri = 0.0;
+    st->max_ite = inner_max;
+    st->log_enabled = 0;
+    st->best = 1.0e+6;
+    st->bad_counter = 0;
+    st->improved = 0;
+    st->zeta[0] = st->zeta_old[0] = st->nu[0] = 1.0;
+    st->zeta[1] = st->zeta_old[1] = st->nu[1] = 0.0;
+    st->rur0[0] = st->rur0[1] = 0.0;
+    // FP32 cannot take every inner solve to eta (the rounding of A and of the factor bounds
+    // what one solve can gain); a stalled inner solve ends and the refinement continues
+    st->stall_limit = 30;
+    st->stall = 0;
+    st->stall_best = 1.0e+300;
+}
+
+// after k_bsetup (one block): refinement state of every instance, first inner solve armed
+__global__ void k_bmix_begin(BDev B, OState *O, KState *octl, double eta, int inner_max) {
+    int any = 0;
+    for (int s = threadIdx.x; s < B.S; s += blockDim.x) {
+        KState *st = B.st + s;
+        OState *o = O + s;
+        o->active = st->active;
+        o->status = st->status;
+        o->outer_it = 0;
+        o->inner_total = 0;
+        o->normB = o->norm = o->scale = st->normalizer;
+        if (st->active) {
+            inner_reset(st, eta, inner_max);
+            any = 1;
+        }
+    }
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) {
+        octl->active = any;
+        B.ctl->active = any;
+    }
+}
+
+// inner right-hand side r / |r| in FP32 and a zero inner solution (outer-active instances)
+template <typename T, typename Ti>
+__global__ void __launch_bounds__(BT) k_bscale(BDev Bo, const OState *O, const T *r, Ti *rin, Ti *d) {
+    if (!Bo.ctl->active) return;
+    for (int t = blockIdx.x; t < Bo.NT; t += gridDim.x) {
+        const int s = Bo.tile_sys[t];
+        if (!Bo.act[(size_t)s * Bo.act_stride]) continue;
+        const double inv = 1.0 / O[s].scale;
+        const int2 tr = Bo.tile[t];
+        for (int i = tr.x + threadIdx.x; i < tr.y; i += BT) {
+            rin[i] = to_lo(inv * r[i]);
+            d[i] = Sc<Ti>::zero();
+        }
+    }
+}
+
+// x += |r| d in FP64
+template <typename T, typename Ti>
+__global__ void __launch_bounds__(BT) k_bouter_update(BDev Bo, const OState *O, T *x, const Ti *d) {
+    if (!Bo.ctl->active) return;
+    for (int t = blockIdx.x; t < Bo.NT; t += gridDim.x) {
+        const int s = Bo.tile_sys[t];
+        if (!Bo.act[(size_t)s * Bo.act_stride]) continue;
+        const double sc = O[s].scale;
+        const int2 tr = Bo.tile[t];
+        for (int i = tr.x + threadIdx.x; i < tr.y; i += BT) x[i] = x[i] + sc * to_hi(d[i]);
+    }
+}
+
+// r = b - A x (v = A x), |r| per instance, the refinement decision; a continuing
+// instance gets its next inner solve armed
+template <typename T>
+__global__ void __launch_bounds__(BT) k_bresid(BDev Bo, OState *O, KState *ictl, const T *b, const T *v, T *r,
+                                               double tol, int max_ite, double eta) {
+    if (!Bo.ctl->active) return;
+    for (int t = blockIdx.x; t < Bo.NT; t += gridDim.x) {
+        if (!Bo.act[(size_t)Bo.tile_sys[t] * Bo.act_stride]) continue;
+        const int2 tr = Bo.tile[t];
+        double acc[1] = {0.0};
+        for (int i = tr.x + threadIdx.x; i < tr.y; i += BT) {
+            const T ri = b[i] - v[i];
+            r[i] = ri;
+            acc[0] += Sc<T>::abs2(ri);
+        }
+        block_partial<1>(acc, Bo.part + (size_t)t * BATCH_PARTS);
+    }
+    if (!last_block(Bo.counter)) return;
+    int any = 0;
+    for (int s = threadIdx.x; s < Bo.S; s += BT) {
+        OState *o = O + s;
+        if (!o->active) continue;
+        KState *st = Bo.st + s;
+        double tot[1];
+        inst_sum<1>(Bo, s, tot);
+        const double norm = sqrt(tot[0]);
+        o->outer_it += 1;
+        o->inner_total += st->it;
+        inst_log(Bo, s)[o->outer_it] = norm / o->normB;
+        if (norm / o->normB < tol) {
+            o->active = 0;
+            o->status = ST_CONVERGED;
+        } else if (o->inner_total >= max_ite || o->outer_it >= MAX_OUTER) {
+            o->active = 0;
+            o->status = ST_MAXIT;
+        } else {
+            o->norm = o->scale = norm;
+            inner_reset(st, eta, max_ite - o->inner_total);
+            any = 1;
+        }
+    }
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) {
+        Bo.ctl->active = any;
+        ictl->active = any;
+        *Bo.counter = 0u;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BT) k_bneg(BDev B, const T *a, T *out) {
+    if (!B.ctl->active) return;
+    for (int t = blockIdx.x; t < B.NT; t += gridDim.x) {
+        if (!B.act[(size_t)B.tile_sys[t] * B.act_stride]) continue;
+        const int2 tr = B.tile[t];
+        for (int i = tr.x + threadIdx.x; i < tr.y; i += BT) out[i] = Sc<T>::zero() - a[i];
     }
 }
 
@@ -367,6 +517,8 @@ Batch::~Batch() {
     cudaSetDevice(h.device);
     if (h_st) cudaFreeHost(h_st);
     if (h_ctl) cudaFreeHost(h_ctl);
+    if (h_octl) cudaFreeHost(h_octl);
+    if (h_ost) cudaFreeHost(h_ost);
     if (ev_chunk) cudaEventDestroy(ev_chunk);
     for (auto &e : ev)
         if (e) cudaEventDestroy(e);
@@ -402,6 +554,40 @@ void Batch::set_rhs(int index, const double *B) {
     rhs_dirty = true;
 }
 
+void Batch::set_rhs_device(int index, const void *dB) {
+    if (running) throw Error{SSG_ERR_STATE, "batch is running"};
+    if (index < 0 || index >= (int)sys.size() || !dB) throw Error{SSG_ERR_ARG, "bad system index"};
+    dev_rhs.resize(sys.size(), nullptr);
+    dev_rhs[index] = dB;
+}
+
+void Batch::result_device(int index, void *dX) {
+    if (running) throw Error{SSG_ERR_STATE, "batch is running"};
+    if (index < 0 || index >= (int)sys.size() || !dX) throw Error{SSG_ERR_ARG, "bad system index"};
+    const size_t vb = vtype == SSG_COMPLEX ? 16 : 8;
+    for (int q = 0; q < S; ++q) {
+        if (inst_sys[q] != index) continue;
+        const int n = sys[index].n;
+        SSG_CUDA(cudaMemcpyAsync((char *)dX + vb * (size_t)n * inst_rhs[q], h.vec[8].as<char>() + vb * (size_t)inst_row[q],
+                                 vb * (size_t)n, cudaMemcpyDeviceToDevice, h.stream));
+    }
+    SSG_CUDA(cudaStreamSynchronize(h.stream));
+}
+
+void Batch::update_values_device(int index, const void *dval) {
+    if (running) throw Error{SSG_ERR_STATE, "batch is running"};
+    if (index < 0 || index >= (int)sys.size() || !dval) throw Error{SSG_ERR_ARG, "bad system index"};
+    if (!assembled) throw Error{SSG_ERR_STATE, "batch not assembled"};
+    const size_t vb = vtype == SSG_COMPLEX ? 16 : 8;
+    for (int q = 0; q < S; ++q) {
+        if (inst_sys[q] != index) continue;
+        SSG_CUDA(cudaMemcpyAsync(h.A_val.as<char>() + vb * (size_t)inst_entry[q], dval, vb * (size_t)sys[index].nnz,
+                                 cudaMemcpyDeviceToDevice, h.stream));
+    }
+    SSG_CUDA(cudaStreamSynchronize(h.stream));
+    h.values_changed();
+}
+
 void Batch::clear() {
     if (running) throw Error{SSG_ERR_STATE, "batch is running"};
     sys.clear();
@@ -416,11 +602,13 @@ void Batch::assemble() {
     inst_sys.clear();
     inst_rhs.clear();
     inst_row.assign(1, 0);
+    inst_entry.clear();
     long long N = 0, NNZ = 0;
     for (size_t q = 0; q < sys.size(); ++q)
         for (int j = 0; j < sys[q].nrhs; ++j) {
             inst_sys.push_back((int)q);
             inst_rhs.push_back(j);
+            inst_entry.push_back(NNZ);
             N += sys[q].n;
             NNZ += sys[q].nnz;
             if (N >= (1ll << 31) - 1 || NNZ >= (1ll << 31) - 1)
@@ -466,6 +654,12 @@ void Batch::assemble() {
     h_st = nullptr;
     SSG_CUDA(cudaMallocHost((void **)&h_st, sizeof(KState) * (size_t)S));
     if (!h_ctl) SSG_CUDA(cudaMallocHost((void **)&h_ctl, sizeof(KState)));
+    if (!h_octl) SSG_CUDA(cudaMallocHost((void **)&h_octl, sizeof(KState)));
+    if (h_ost) cudaFreeHost(h_ost);
+    h_ost = nullptr;
+    SSG_CUDA(cudaMallocHost((void **)&h_ost, sizeof(OState) * (size_t)S));
+    d_ost.ensure(sizeof(OState) * (size_t)S);
+    d_octl.ensure(sizeof(KState));
     SSG_CUDA(cudaStreamSynchronize(st));
     assembled = true;
 }
@@ -481,11 +675,13 @@ BDev Batch::dev_view() {
     B.sys_tile = d_sys_tile.as<int>();
     B.sys_row = d_sys_row.as<int>();
     B.st = d_st.as<KState>();
+    B.act = &d_st.as<KState>()->active;
+    B.act_stride = (int)(sizeof(KState) / sizeof(int));
     B.ctl = ctl();
     B.part = d_part.as<double>();
     B.counter = (unsigned *)(d_ctl_counter.as<char>() + sizeof(KState));
     B.logs = d_logs.as<double>();
-    B.log_stride = max_ite + 2;
+    B.log_stride = max_ite + 2 + MAX_OUTER;
     return B;
 }
 
@@ -505,7 +701,7 @@ void Batch::start(int method_, double alpha, double conv, int max_ite_) {
     h.fac_valid = false;
     h.ensure_factor<T>(alpha, false);
     h.ensure_work(sizeof(T));
-    d_logs.ensure(sizeof(double) * (size_t)S * (size_t)(max_ite + 2));
+    d_logs.ensure(sizeof(double) * (size_t)S * (size_t)(max_ite + 2 + MAX_OUTER));
     T *b = h.vec[0].as<T>(), *r = h.vec[1].as<T>(), *p = h.vec[2].as<T>(), *z = h.vec[3].as<T>();
     T *u = h.vec[4].as<T>(), *y = h.vec[5].as<T>(), *x = h.vec[8].as<T>();
     // right-hand sides of all instances, uploaded when they changed (they stay resident otherwise)
@@ -520,6 +716,17 @@ void Batch::start(int method_, double alpha, double conv, int max_ite_) {
         SSG_CUDA(cudaMemcpyAsync(b, stage.data(), sizeof(T) * (size_t)n, cudaMemcpyHostToDevice, s));
         SSG_CUDA(cudaStreamSynchronize(s));
         rhs_dirty = false;
+    }
+    // right-hand sides given in device memory
+    for (size_t i = 0; i < dev_rhs.size(); ++i) {
+        if (!dev_rhs[i]) continue;
+        for (int q = 0; q < S; ++q) {
+            if (inst_sys[q] != (int)i) continue;
+            const int ns = sys[i].n;
+            SSG_CUDA(cudaMemcpyAsync(b + inst_row[q], (const T *)dev_rhs[i] + (size_t)ns * inst_rhs[q],
+                                     sizeof(T) * (size_t)ns, cudaMemcpyDeviceToDevice, s));
+        }
+        dev_rhs[i] = nullptr;
     }
     for (int q = 0; q < S; ++q) {
         KState &k = h_st[q];
@@ -551,6 +758,17 @@ void Batch::start(int method_, double alpha, double conv, int max_ite_) {
         k_bsetup<T><<<grid, BT, 0, s>>>(B, b);
         SSG_LAUNCHED();
     });
+    conv_cri = conv;
+    if (precision == SSG_PREC_MIXED) {
+        using Ti = typename Lo<T>::type;
+        start_mixed<T, Ti>(alpha, conv);
+        SSG_CUDA(cudaEventRecord(ev[1], s));
+        queued = 0;
+        chunk = 2;
+        running = true;
+        queue_inner<T, Ti>(chunk);
+        return;
+    }
     if (method == SSG_METHOD_ICCG) {
         h.apply_precond<T>(r, z, ctl());
         SSG_CUDA(cudaMemcpyAsync(p, z, sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, s));
@@ -639,7 +857,28 @@ bool Batch::poll() {
     if (q == cudaErrorNotReady) return false;
     SSG_CUDA(q);
     h.check_err("batched iterations");
-    if (h_ctl->active && queued < max_ite) {
+    if (precision == SSG_PREC_MIXED) {
+        const bool cx = vtype == SSG_COMPLEX;
+        if (h_ctl->active && queued < max_ite) {
+            if (cx)
+                queue_inner<cplx, cplxf>(chunk);
+            else
+                queue_inner<double, float>(chunk);
+            return false;
+        }
+        if (h_octl->active) {
+            queued = 0;
+            chunk = 2;
+            if (cx) {
+                queue_outer_step<cplx, cplxf>();
+                queue_inner<cplx, cplxf>(chunk);
+            } else {
+                queue_outer_step<double, float>();
+                queue_inner<double, float>(chunk);
+            }
+            return false;
+        }
+    } else if (h_ctl->active && queued < max_ite) {
         if (vtype == SSG_COMPLEX)
             queue_chunk<cplx>();
         else
@@ -648,10 +887,13 @@ bool Batch::poll() {
     }
     cudaStream_t s = h.stream;
     SSG_CUDA(cudaMemcpyAsync(h_st, d_st.p, sizeof(KState) * (size_t)S, cudaMemcpyDeviceToHost, s));
+    if (precision == SSG_PREC_MIXED)
+        SSG_CUDA(cudaMemcpyAsync(h_ost, d_ost.p, sizeof(OState) * (size_t)S, cudaMemcpyDeviceToHost, s));
     SSG_CUDA(cudaEventRecord(ev[2], s));
     SSG_CUDA(cudaStreamSynchronize(s));
     int most = 0;
     for (int q = 0; q < S; ++q) most = std::max(most, h_st[q].it);
+    if (precision == SSG_PREC_MIXED) most = 1 << 30;  // every profiled launch of a refinement did work
     h.prof_flush(most);
     h.prof.iter = 0;
     float a = 0.f, b = 0.f;
@@ -678,9 +920,12 @@ int Batch::result(int index, double *X, int *iters, int *status) {
         if (X)
             SSG_CUDA(cudaMemcpyAsync((char *)X + vb * (size_t)n * j, h.vec[8].as<char>() + vb * (size_t)inst_row[q],
                                      vb * (size_t)n, cudaMemcpyDeviceToHost, h.stream));
-        if (iters) iters[j] = h_st[q].it;
-        if (status) status[j] = h_st[q].status;
-        if (h_st[q].status != ST_CONVERGED) rc = SSG_NOT_CONVERGED;
+        const bool mixed = precision == SSG_PREC_MIXED;
+        const int it = mixed ? h_ost[q].inner_total : h_st[q].it;
+        const int stt = mixed ? h_ost[q].status : h_st[q].status;
+        if (iters) iters[j] = it;
+        if (status) status[j] = stt;
+        if (stt != ST_CONVERGED) rc = SSG_NOT_CONVERGED;
     }
     SSG_CUDA(cudaStreamSynchronize(h.stream));
     return rc;
@@ -697,15 +942,265 @@ int Batch::residual_log(int index, int rhs, double *out, int capacity, int *leng
     if (!assembled || t_ms.empty()) throw Error{SSG_ERR_STATE, "no finished solve"};
     const int q = instance(index, rhs);
     if (q < 0) throw Error{SSG_ERR_ARG, "bad system index or right-hand side"};
-    const int len = h_st[q].log_len >= 0 ? h_st[q].log_len : h_st[q].it + 1;
+    // mixed precision: the log holds |b - A x| / |b| after each refinement step
+    const int len = h_st[q].log_len >= 0 ? h_st[q].log_len
+                    : (precision == SSG_PREC_MIXED ? h_ost[q].outer_it + 1 : h_st[q].it + 1);
     if (length) *length = len;
     if (out && capacity > 0) {
         const int m = std::min(capacity, len);
         if (m > 0)
-            SSG_CUDA(cudaMemcpy(out, d_logs.as<double>() + (size_t)q * (max_ite + 2), sizeof(double) * (size_t)m,
+            SSG_CUDA(cudaMemcpy(out, d_logs.as<double>() + (size_t)q * (max_ite + 2 + MAX_OUTER), sizeof(double) * (size_t)m,
                                 cudaMemcpyDeviceToHost));
     }
     return SSG_OK;
+}
+
+// ---------------------------------------------------------------- mixed precision, host side
+BDev Batch::outer_view() {
+    BDev B = dev_view();
+    B.act = &d_ost.as<OState>()->active;
+    B.act_stride = (int)(sizeof(OState) / sizeof(int));
+    B.ctl = octl();
+    return B;
+}
+
+// z = (L D L^T)^{-1} r with the FP32 copy of the factor (the schedule choice of Handle::apply_precond)
+template <typename Ti>
+void Batch::precond32(const Ti *r, Ti *z, const KState *stp) {
+    cudaStream_t s = h.stream;
+    const size_t v = sizeof(Ti);
+    const int n = h.n;
+    Ti *y = v32[10].as<Ti>();
+    const double fb = (4.0 + v) * h.Lf.nnz + 4.0 * (n + 1) + 2.0 * v * n;
+    if (h.cluster_ok(h.Lf, v) && h.cluster_ok(h.Ltb, v)) {
+        h.timed(PC_FWD, fb, [&] {
+            sweep_cluster<Ti>(h.Lf, L32.as<Ti>(), SW_FWD_DIV, r, nullptr, h.use_inv_diag ? invL32_lev.as<Ti>() : nullptr,
+                              y, nullptr, stp, h.cl_group, s);
+        });
+        h.timed(PC_BWD, fb + v * n, [&] {
+            sweep_cluster<Ti>(h.Ltb, Lt32.as<Ti>(), SW_BWD_IC, nullptr, y, D32_lev.as<Ti>(), z, nullptr, stp,
+                              h.cl_group, s);
+        });
+        return;
+    }
+    // all bits set is the sentinel of every value type
+    SSG_CUDA(cudaMemsetAsync(y, 0xFF, v * (size_t)n, s));
+    h.timed(PC_FWD, fb, [&] {
+        sweep_st<Ti>(h.Lf, L32.as<Ti>(), SW_FWD_DIV, r, nullptr, nullptr, y, nullptr, h.ticket(), h.err(), stp, s,
+                     h.swcfg, h.use_inv_diag ? invL32.as<Ti>() : nullptr);
+    });
+    SSG_CUDA(cudaMemsetAsync(z, 0xFF, v * (size_t)n, s));
+    h.timed(PC_BWD, fb + v * n, [&] {
+        sweep_st<Ti>(h.Ltb, Lt32.as<Ti>(), SW_BWD_IC, nullptr, y, D32.as<Ti>(), z, nullptr, h.ticket() + 1, h.err(),
+                     stp, s, h.swcfg, (const Ti *)nullptr);
+    });
+}
+
+template <typename Ti>
+void Batch::inner_setup() {
+    cudaStream_t s = h.stream;
+    const int n = h.n;
+    BDev B = dev_view();
+    const int grid = bgrid(NT);
+    Ti *rin = v32[1].as<Ti>(), *p = v32[2].as<Ti>(), *z = v32[3].as<Ti>(), *u = v32[4].as<Ti>(),
+       *y = v32[5].as<Ti>();
+    if (method == SSG_METHOD_ICCG) {
+        precond32<Ti>(rin, z, ctl());
+        SSG_CUDA(cudaMemcpyAsync(p, z, sizeof(Ti) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+        k_brur0<Ti><<<grid, BT, 0, s>>>(B, rin, z);
+        SSG_LAUNCHED();
+    } else {
+        precond32<Ti>(rin, u, ctl());
+        k_bneg<Ti><<<grid, BT, 0, s>>>(B, rin, y);
+        SSG_LAUNCHED();
+        precond32<Ti>(y, z, ctl());
+        SSG_CUDA(cudaMemsetAsync(p, 0, sizeof(Ti) * (size_t)n, s));
+    }
+}
+
+template <typename T, typename Ti>
+void Batch::start_mixed(double alpha, double conv) {
+    (void)alpha;
+    (void)conv;
+    cudaStream_t s = h.stream;
+    const int n = h.n;
+    const int nnzL = h.Lf.nnz;
+    // FP32 copies of A and of the FP64 factor (value arrays keep the 16 padding entries)
+    A32.ensure(sizeof(Ti) * (size_t)(h.nnz + 16));
+    L32.ensure(sizeof(Ti) * (size_t)(nnzL + 16));
+    Lt32.ensure(sizeof(Ti) * (size_t)(nnzL + 16));
+    for (DBuf *d : {&invL32, &invL32_lev, &D32, &D32_lev}) d->ensure(sizeof(Ti) * (size_t)(n + 1));
+    for (auto &v : v32) v.ensure(sizeof(Ti) * (size_t)(n + 1));
+    auto narrow_copy = [&](const DBuf &src, DBuf &dst, size_t count) {
+        if (!count) return;
+        const int g = (int)std::min<size_t>(div_up((int)std::min<size_t>(count, 1u << 30), 256), 4096);
+        k_narrow<T, Ti><<<g, 256, 0, s>>>(count, src.as<T>(), dst.as<Ti>());
+        SSG_LAUNCHED();
+    };
+    h.timed(PC_VEC, (double)(sizeof(T) + sizeof(Ti)) * (h.nnz + 2.0 * nnzL + 4.0 * n), [&] {
+        narrow_copy(h.A_val, A32, (size_t)h.nnz);
+        narrow_copy(h.Lval, L32, (size_t)nnzL);
+        narrow_copy(h.Ltval, Lt32, (size_t)nnzL);
+        narrow_copy(h.invL, invL32, (size_t)n);
+        narrow_copy(h.invL_lev, invL32_lev, (size_t)n);
+        narrow_copy(h.Dvec, D32, (size_t)n);
+        narrow_copy(h.D_lev, D32_lev, (size_t)n);
+    });
+    BDev B = dev_view();
+    k_bmix_begin<<<1, BT, 0, s>>>(B, d_ost.as<OState>(), octl(), eff_inner_tol(), max_ite);
+    SSG_LAUNCHED();
+    BDev Bo = outer_view();
+    const int grid = bgrid(NT);
+    k_bscale<T, Ti><<<grid, BT, 0, s>>>(Bo, d_ost.as<OState>(), h.vec[1].as<T>(), v32[1].as<Ti>(), v32[0].as<Ti>());
+    SSG_LAUNCHED();
+    inner_setup<Ti>();
+}
+
+template <typename T, typename Ti>
+void Batch::queue_inner(int todo) {
+    cudaStream_t s = h.stream;
+    const int n = h.n;
+    BDev B = dev_view();
+    const int grid = bgrid(NT);
+    const int *rp = h.A_rp.as<int>(), *ci = h.A_ci.as<int>();
+    const Ti *aval = A32.as<Ti>();
+    Ti *d = v32[0].as<Ti>(), *r = v32[1].as<Ti>(), *p = v32[2].as<Ti>(), *z = v32[3].as<Ti>(), *u = v32[4].as<Ti>();
+    Ti *y = v32[5].as<Ti>(), *v = v32[6].as<Ti>(), *w = v32[7].as<Ti>();
+    todo = std::min(todo, max_ite - queued);
+    const double nv = (double)sizeof(Ti) * n;
+    const double spmv_bytes = (4.0 + sizeof(Ti)) * h.nnz + 4.0 * (n + 1) + 2.0 * nv;
+    for (int c = 0; c < todo; ++c) {
+        h.prof.iter = ++iter_no;
+        h.prof.pre = true;
+        if (method == SSG_METHOD_ICCG) {
+            h.timed(PC_SPMV, spmv_bytes, [&] {
+                k_bspmv<Ti, true><<<grid, BT, 0, s>>>(B, rp, ci, aval, p, v);
+                SSG_LAUNCHED();
+            });
+            h.timed(PC_VEC, 6 * nv, [&] {
+                k_biccg_update<Ti><<<grid, BT, 0, s>>>(B, d, r, p, v);
+                SSG_LAUNCHED();
+            });
+            precond32<Ti>(r, z, ctl());
+            h.timed(PC_VEC, 2 * nv, [&] {
+                k_biccg_beta<Ti><<<grid, BT, 0, s>>>(B, r, z);
+                SSG_LAUNCHED();
+            });
+            h.timed(PC_VEC, 3 * nv, [&] {
+                k_biccg_p<Ti><<<grid, BT, 0, s>>>(B, p, z);
+                SSG_LAUNCHED();
+            });
+        } else {
+            h.timed(PC_SPMV, spmv_bytes, [&] {
+                k_bspmv<Ti, false><<<grid, BT, 0, s>>>(B, rp, ci, aval, u, v);
+                SSG_LAUNCHED();
+            });
+            precond32<Ti>(v, w, ctl());
+            h.timed(PC_VEC, 4 * nv, [&] {
+                k_bmrtr_dots<Ti><<<grid, BT, 0, s>>>(B, w, r, v, y);
+                SSG_LAUNCHED();
+            });
+            h.timed(PC_VEC, 10 * nv, [&] {
+                k_bmrtr_update<Ti><<<grid, BT, 0, s>>>(B, p, u, d, y, v, r);
+                SSG_LAUNCHED();
+            });
+            h.timed(PC_VEC, 5 * nv, [&] {
+                k_bmrtr_zu<Ti><<<grid, BT, 0, s>>>(B, z, w, u);
+                SSG_LAUNCHED();
+            });
+        }
+    }
+    queued += todo;
+    chunk = std::min(chunk * 2, 32);
+    SSG_CUDA(cudaMemcpyAsync(h_ctl, ctl(), sizeof(KState), cudaMemcpyDeviceToHost, s));
+    SSG_CUDA(cudaMemcpyAsync(h_octl, octl(), sizeof(KState), cudaMemcpyDeviceToHost, s));
+    SSG_CUDA(cudaEventRecord(ev_chunk, s));
+}
+
+template <typename T, typename Ti>
+void Batch::queue_outer_step() {
+    cudaStream_t s = h.stream;
+    BDev Bo = outer_view();
+    const int grid = bgrid(NT);
+    OState *O = d_ost.as<OState>();
+    T *b = h.vec[0].as<T>(), *r = h.vec[1].as<T>(), *v = h.vec[6].as<T>(), *x = h.vec[8].as<T>();
+    const double nv = (double)sizeof(T) * h.n;
+    h.timed(PC_VEC, 2 * nv + (double)sizeof(Ti) * h.n, [&] {
+        k_bouter_update<T, Ti><<<grid, BT, 0, s>>>(Bo, O, x, v32[0].as<Ti>());
+        SSG_LAUNCHED();
+    });
+    h.timed(PC_SPMV, (4.0 + sizeof(T)) * h.nnz + 4.0 * (h.n + 1) + 2.0 * nv, [&] {
+        k_bspmv<T, false><<<grid, BT, 0, s>>>(Bo, h.A_rp.as<int>(), h.A_ci.as<int>(), h.A_val.as<T>(), x, v);
+        SSG_LAUNCHED();
+    });
+    h.timed(PC_VEC, 3 * nv, [&] {
+        k_bresid<T><<<grid, BT, 0, s>>>(Bo, O, ctl(), b, v, r, conv_cri, max_ite, eff_inner_tol());
+        SSG_LAUNCHED();
+    });
+    k_bscale<T, Ti><<<grid, BT, 0, s>>>(Bo, O, r, v32[1].as<Ti>(), v32[0].as<Ti>());
+    SSG_LAUNCHED();
+    inner_setup<Ti>();
+}
+
+int solve_mixed(Handle &h, Batch *&mb, uint64_t &mver, uint64_t &mpat, int method, double conv, int max_ite,
+                const void *d_b, void *d_x) {
+    const ssg_options &o = h.opt;
+    if (o.is_diag_scale || (method == SSG_METHOD_MRTR && o.precondition_type != 0) || !(o.accel_factor > 0.0) ||
+        !o.is_init || o.conv_normalize_type != 0)
+        throw Error{SSG_ERR_ARG,
+                    "mixed precision solves ICCG or IC-MRTR with a fixed accel_factor > 0, x0 = 0, the |b| "
+                    "normaliser and no diagonal scaling"};
+    if (h.vtype < 0) throw Error{SSG_ERR_STATE, "no matrix set"};
+    if (h.n == 0) {
+        h.iters = 0;
+        h.residual_log.clear();
+        return SSG_OK;
+    }
+    if (!mb) mb = new Batch(h.device);
+    mb->h.prof.on = h.prof.on;  // profiling follows the owning handle
+    const int w = h.vtype == SSG_COMPLEX ? 2 : 1;
+    if (mver != h.version && mpat == h.pattern_id && mb->assembled && !mb->sys.empty() && mb->vtype == h.vtype) {
+        // values-only update: the batch keeps its pattern analysis
+        SSG_CUDA(cudaStreamSynchronize(h.stream));
+        mb->update_values_device(0, h.A_val.p);
+        mver = h.version;
+    }
+    if (mver != h.version || mb->sys.empty()) {
+        // the handle's matrix, through the host once per matrix version
+        std::vector<int> rp((size_t)h.n + 1), ci((size_t)h.nnz);
+        std::vector<double> val((size_t)w * h.nnz), B((size_t)w * h.n, 0.0);
+        SSG_CUDA(cudaMemcpyAsync(rp.data(), h.A_rp.p, sizeof(int) * rp.size(), cudaMemcpyDeviceToHost, h.stream));
+        SSG_CUDA(cudaMemcpyAsync(ci.data(), h.A_ci.p, sizeof(int) * ci.size(), cudaMemcpyDeviceToHost, h.stream));
+        SSG_CUDA(cudaMemcpyAsync(val.data(), h.A_val.p, sizeof(double) * val.size(), cudaMemcpyDeviceToHost, h.stream));
+        SSG_CUDA(cudaStreamSynchronize(h.stream));
+        mb->clear();
+        mb->add(h.n, h.nnz, rp.data(), ci.data(), val.data(), h.vtype, 1, B.data());
+        mver = h.version;
+        mpat = h.pattern_id;
+    }
+    SSG_CUDA(cudaStreamSynchronize(h.stream));  // d_b may come from work queued on the handle's stream
+    mb->precision = SSG_PREC_MIXED;
+    mb->set_rhs_device(0, d_b);
+    if (h.vtype == SSG_COMPLEX)
+        mb->start<cplx>(method, o.accel_factor, conv, max_ite);
+    else
+        mb->start<double>(method, o.accel_factor, conv, max_ite);
+    mb->wait();
+    mb->result_device(0, d_x);
+    int it = 0, stt = 0;
+    const int rc = mb->result(0, nullptr, &it, &stt);
+    h.iters = it;
+    h.alpha_used = o.accel_factor;
+    h.residual_log.clear();
+    if (o.is_save_residual_log) {
+        int len = 0;
+        mb->residual_log(0, 0, nullptr, 0, &len);
+        h.residual_log.resize((size_t)len);
+        if (len) mb->residual_log(0, 0, h.residual_log.data(), len, &len);
+    }
+    h.t_setup_ms = mb->t_ms.size() > 0 ? mb->t_ms[0] : 0.0;
+    h.t_iter_ms = mb->t_ms.size() > 1 ? mb->t_ms[1] : 0.0;
+    return rc;
 }
 
 template void Batch::start<double>(int, double, double, int);

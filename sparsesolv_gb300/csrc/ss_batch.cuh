@@ -30,11 +30,21 @@ struct BDev {
     const int *sys_tile;  // [S + 1] first tile of each instance
     const int *sys_row;   // [S + 1] first row of each instance
     KState *st;           // [S] per-instance state
+    const int *act;       // per-instance activity mask: act[s * act_stride] (the state the launch follows)
+    int act_stride;
     KState *ctl;          // batch control: active while any instance is
     double *part;         // [NT * BATCH_PARTS]
     unsigned *counter;    // last-block ticket
     double *logs;         // [S * log_stride] residual logs
     int log_stride;
+};
+
+// mixed precision: per-instance state of the FP64 refinement around the FP32 inner solves
+struct OState {
+    int active, status;
+    int outer_it;     // refinement steps done
+    int inner_total;  // inner iterations over all steps
+    double normB, norm, scale, pad;
 };
 
 struct BatchSystem {
@@ -50,6 +60,7 @@ struct Batch {
     std::vector<BatchSystem> sys;
     // instances
     std::vector<int> inst_sys, inst_rhs, inst_row;  // per instance; inst_row has S + 1 entries
+    std::vector<long long> inst_entry;              // first entry of each instance in the block-diagonal matrix
     int S = 0, NT = 0;
     bool assembled = false;
     bool rhs_dirty = true;  // right-hand sides changed since the last upload
@@ -61,6 +72,26 @@ struct Batch {
     int method = SSG_METHOD_ICCG;
     int max_ite = 0, queued = 0, chunk = 2, iter_no = 0;
     bool running = false, log_on = true;
+    // mixed precision (SSG_PREC_MIXED): FP32 copies of A and of the factor, FP32 inner vectors
+    int precision = SSG_PREC_FP64;
+    double inner_tol = 0.0;  // inner solves reduce the scaled residual by this factor (0: 1e-4 real, 1e-2 complex)
+    double eff_inner_tol() const { return inner_tol > 0.0 ? inner_tol : (vtype == SSG_COMPLEX ? 1.0e-2 : 1.0e-4); }
+    DBuf d_ost, d_octl, A32, L32, Lt32, invL32, invL32_lev, D32, D32_lev, v32[11];
+    OState *h_ost = nullptr;
+    KState *h_octl = nullptr;
+    KState *octl() { return d_octl.as<KState>(); }
+    BDev outer_view();
+    template <typename T, typename Ti>
+    void start_mixed(double alpha, double conv);
+    template <typename T, typename Ti>
+    void queue_inner(int todo);
+    template <typename T, typename Ti>
+    void queue_outer_step();
+    template <typename Ti>
+    void inner_setup();
+    template <typename Ti>
+    void precond32(const Ti *r, Ti *z, const KState *st);
+    double conv_cri = 1.0e-8;
     std::vector<double> t_ms;  // set-up, iterations (ms) of the last solve
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
 
@@ -69,6 +100,10 @@ struct Batch {
     int add(int n, int nnz, const int *rp, const int *ci, const double *val, int vt, int nrhs, const double *B);
     void clear();
     void set_rhs(int index, const double *B);
+    std::vector<const void *> dev_rhs;  // right-hand sides to take from device memory at the next start
+    void set_rhs_device(int index, const void *dB);
+    void result_device(int index, void *dX);
+    void update_values_device(int index, const void *dval);  // same pattern, new values (device memory)
     void assemble();
     BDev dev_view();
     KState *ctl();
@@ -82,5 +117,10 @@ struct Batch {
     int residual_log(int index, int rhs, double *out, int capacity, int *length);
     int instance(int index, int rhs) const;
 };
+
+// ssg_solve / ssg_solve_device with precision SSG_PREC_MIXED: a one-system batch
+// built from the handle's matrix (kept while the matrix version is unchanged)
+int solve_mixed(Handle &h, Batch *&mb, uint64_t &mver, uint64_t &mpat, int method, double conv, int max_ite,
+                const void *d_b, void *d_x);
 
 }  // namespace ssg

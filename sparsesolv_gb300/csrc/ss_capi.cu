@@ -16,6 +16,8 @@ long long launch_count();
 struct ssg_handle_s {
     Handle *h;
     ssg::DBuf io_b, io_x;
+    ssg::Batch *mixed = nullptr;  // precision SSG_PREC_MIXED: one-system batch over this handle's matrix
+    uint64_t mixed_version = ~0ull, mixed_pattern = ~0ull;
 };
 
 namespace {
@@ -108,6 +110,7 @@ int ssg_destroy(ssg_handle hd) {
     if (hd->h) cudaSetDevice(hd->h->device);
     hd->io_b.release();
     hd->io_x.release();
+    delete hd->mixed;
     delete hd->h;
     delete hd;
     return SSG_OK;
@@ -120,6 +123,7 @@ const char *ssg_last_error(ssg_handle hd) {
 
 int ssg_set_options(ssg_handle hd, const ssg_options *o) {
     if (!o) return SSG_ERR_ARG;
+    if (o->precision != SSG_PREC_FP64 && o->precision != SSG_PREC_MIXED) return SSG_ERR_ARG;
     return guarded(hd, [&](Handle &h) {
         h.opt = *o;
         return SSG_OK;
@@ -157,6 +161,8 @@ int ssg_solve_device(ssg_handle hd, int method, double conv_cri, int max_ite, do
         const int rc = check_solve_args(h, method, max_ite);
         if (rc) return rc;
         if (h.n > 0 && (!d_b || !d_x)) return SSG_ERR_ARG;
+        if (h.opt.precision == SSG_PREC_MIXED)
+            return ssg::solve_mixed(h, hd->mixed, hd->mixed_version, hd->mixed_pattern, method, conv_cri, max_ite, d_b, d_x);
         if (h.vtype == SSG_COMPLEX) return h.solve<cplx>(method, conv_cri, max_ite, normB, (const cplx *)d_b, (cplx *)d_x);
         return h.solve<double>(method, conv_cri, max_ite, normB, d_b, d_x);
     });
@@ -175,7 +181,9 @@ int ssg_solve(ssg_handle hd, int method, double conv_cri, int max_ite, double no
             SSG_CUDA(cudaMemcpyAsync(hd->io_x.p, x, bytes, cudaMemcpyHostToDevice, h.stream));
         }
         int res;
-        if (h.vtype == SSG_COMPLEX)
+        if (h.opt.precision == SSG_PREC_MIXED)
+            res = ssg::solve_mixed(h, hd->mixed, hd->mixed_version, hd->mixed_pattern, method, conv_cri, max_ite, hd->io_b.p, hd->io_x.p);
+        else if (h.vtype == SSG_COMPLEX)
             res = h.solve<cplx>(method, conv_cri, max_ite, normB, hd->io_b.as<cplx>(), hd->io_x.as<cplx>());
         else
             res = h.solve<double>(method, conv_cri, max_ite, normB, hd->io_b.as<double>(), hd->io_x.as<double>());
@@ -209,26 +217,33 @@ int ssg_get_stream(ssg_handle hd, void **stream) {
     });
 }
 
+static void prof_reset(Handle &h, bool on) {
+    h.prof.on = on;
+    for (int c = 0; c < ssg::PC_N; ++c) {
+        h.prof.ms[c] = 0.0;
+        h.prof.launches[c] = 0;
+        h.prof.bytes[c] = 0.0;
+    }
+    h.prof.recs.clear();
+    h.prof.used = 0;
+}
+
 int ssg_set_profiling(ssg_handle hd, int enable) {
     return guarded(hd, [&](Handle &h) {
-        h.prof.on = enable != 0;
-        for (int c = 0; c < ssg::PC_N; ++c) {
-            h.prof.ms[c] = 0.0;
-            h.prof.launches[c] = 0;
-            h.prof.bytes[c] = 0.0;
-        }
-        h.prof.recs.clear();
-        h.prof.used = 0;
+        prof_reset(h, enable != 0);
+        if (hd->mixed) prof_reset(hd->mixed->h, enable != 0);
         return SSG_OK;
     });
 }
 
 int ssg_get_kernel_stats(ssg_handle hd, double *ms, long long *launches, double *bytes, int cap) {
     return guarded(hd, [&](Handle &h) {
+        // a mixed-precision solve runs in the handle's internal batch: its launches count too
+        const Handle *mh = hd->mixed ? &hd->mixed->h : nullptr;
         for (int c = 0; c < ssg::PC_N && c < cap; ++c) {
-            if (ms) ms[c] = h.prof.ms[c];
-            if (launches) launches[c] = h.prof.launches[c];
-            if (bytes) bytes[c] = h.prof.bytes[c];
+            if (ms) ms[c] = h.prof.ms[c] + (mh ? mh->prof.ms[c] : 0.0);
+            if (launches) launches[c] = h.prof.launches[c] + (mh ? mh->prof.launches[c] : 0);
+            if (bytes) bytes[c] = h.prof.bytes[c] + (mh ? mh->prof.bytes[c] : 0.0);
         }
         return SSG_OK;
     });
@@ -484,6 +499,17 @@ int ssg_batch_timings(ssg_batch bd, double *ms2) {
         if (!ms2) return SSG_ERR_ARG;
         ms2[0] = b.t_ms.size() > 0 ? b.t_ms[0] : 0.0;
         ms2[1] = b.t_ms.size() > 1 ? b.t_ms[1] : 0.0;
+        return SSG_OK;
+    });
+}
+
+int ssg_batch_set_precision(ssg_batch bd, int precision, double inner_tol) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        if (precision != SSG_PREC_FP64 && precision != SSG_PREC_MIXED) return SSG_ERR_ARG;
+        if (b.running) return SSG_ERR_STATE;
+        if (inner_tol >= 1.0) return SSG_ERR_ARG;
+        b.precision = precision;
+        b.inner_tol = inner_tol > 0.0 ? inner_tol : 0.0;
         return SSG_OK;
     });
 }

@@ -38,6 +38,10 @@ struct KState {
     double rur0[2], alpha[2], beta[2];
     double zeta[2], zeta_old[2], eta[2], nu[2], ptemp[2];
     double dots[8];          // latest fused dot products (for the host's diagnostics)
+    // inner solves of the mixed-precision refinement: end when the residual has not
+    // fallen below 0.99 x its best for stall_limit iterations (0: rule off)
+    int stall_limit, stall;
+    double stall_best;
 };
 
 }  // namespace ssg

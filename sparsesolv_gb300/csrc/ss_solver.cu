@@ -127,6 +127,7 @@ void Handle::set_matrix(int n_, int nnz_, const int32_t *rp, const int32_t *ci, 
     SSG_CUDA(cudaStreamSynchronize(stream));
     ++version;
     if (!same_pattern) {
+        ++pattern_id;
         pat_version = ~0ull;
         ltb_ready = ub_ready = false;
     } else {
@@ -140,6 +141,10 @@ void Handle::update_values(const double *val, cudaMemcpyKind kind) {
     const size_t vb = (vtype == SSG_COMPLEX ? 16 : 8);
     if (nnz) SSG_CUDA(cudaMemcpyAsync(A_val.p, val, vb * (size_t)nnz, kind, stream));
     SSG_CUDA(cudaStreamSynchronize(stream));
+    values_changed();
+}
+
+void Handle::values_changed() {
     const bool pat_ok = (pat_version == version);
     ++version;
     if (pat_ok) pat_version = version;  // the pattern and its schedules stay valid

@@ -39,7 +39,8 @@ struct Handle {
 
     // ---- the matrix, natural order (SparseMat's CSR)
     int n = 0, nnz = 0, vtype = -1;
-    uint64_t version = 0;  // bumps on every set_matrix
+    uint64_t version = 0;     // bumps on every set_matrix and values update
+    uint64_t pattern_id = 0;  // bumps when set_matrix brings a different sparsity pattern
     DBuf A_rp, A_ci, A_val;
 
     // ---- patterns and level schedules (depend on the sparsity pattern)
@@ -114,6 +115,7 @@ struct Handle {
     void set_matrix(int n_, int nnz_, const int32_t *rp, const int32_t *ci, const double *val, int vt,
                     cudaMemcpyKind kind);
     void update_values(const double *val, cudaMemcpyKind kind);
+    void values_changed();  // A_val was rewritten in place: keep the pattern, drop the factors
     void ensure_patterns(bool need_ltb, bool need_ub);
     void check_err(const char *where);
     template <typename T>
