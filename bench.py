@@ -50,9 +50,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--method", default="iccg", choices=["iccg", "sgs", "mrtr_ic"])
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
-                    help="mixed: FP32 inner solves inside FP64 refinement on the true residual")
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5"])
+    ap.add_argument("--requests", type=int, default=32, help="cfg5: requests per stream")
+    ap.add_argument("--precision", default=None, choices=["fp64", "mixed"],
+                    help="mixed: FP32 inner solves inside FP64 refinement on the true residual "
+                         "(default: mixed for the serving stream, fp64 otherwise)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sweep-mode", type=int, default=0, choices=[0, 1, 2],
                     help="triangular sweeps: 0 automatic, 1 sync-free, 2 one-cluster level-synchronous")
@@ -491,6 +493,97 @@ def run_batch(args):
         torch.distributed.destroy_process_group()
 
 
+def run_serving(args):
+    """Serving stream: requests log-uniform over 1k-500k unknowns, 70% real
+    ICCG / 30% complex IC-MRTR, continuous batching in mixed precision to 1e-8.
+    value = solves/s with every request queued at t = 0 (saturation); the rate
+    sweep replays the same requests as Poisson arrivals at fractions of that
+    rate and reports p50/p99 latency. The plain FP64 GPU path solves the same
+    requests one after another through a handle."""
+    import torch
+    from sparsesolv_gb300 import _capi, serving
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return  # one GPU serves the stream; replicas would split it by request
+    torch.cuda.set_device(local)
+    base = serving.synthetic_stream(args.requests, rate=0.0, seed=11)
+    kinds = [r.kind for r in base]
+    be = serving.GpuBackend(local, precision=_capi.PREC_MIXED if args.precision != "fp64" else _capi.PREC_FP64)
+
+    def fresh(rate, seed):
+        rng = np.random.default_rng(seed)
+        t, out = 0.0, []
+        for r in base:
+            if rate > 0:
+                t += rng.exponential(1.0 / rate)
+            out.append(serving.Request(r.rid, t, r.row_ptr, r.col, r.val, r.b, r.kind))
+        return out
+
+    def check(reqs):
+        import scipy.sparse as sp
+        worst = 0.0
+        for r in reqs:
+            A = sp.csr_matrix((r.val, r.col, r.row_ptr))
+            worst = max(worst, float(np.linalg.norm(r.b - A @ r.x) / np.linalg.norm(r.b)))
+        return worst
+
+    srv = serving.Server(be)
+    for _ in range(max(1, args.warmup - 2)):  # warm the slots (buffers, modules)
+        srv.run(fresh(0.0, 0))
+    sat = srv.run(fresh(0.0, 0))
+    st_sat = serving.latency_stats(sat)
+    worst = check(sat)
+    sweep = []
+    for frac in (0.25, 0.5, 1.0):
+        rate = frac * st_sat["solves_per_s"]
+        reqs = srv.run(fresh(rate, 1 + int(frac * 100)))
+        st = serving.latency_stats(reqs)
+        st["arrival_rate"] = rate
+        sweep.append(st)
+        worst = max(worst, check(reqs))
+    srv.close()
+    # plain FP64 GPU path: one request after another through a handle
+    h = _capi.Handle(local)
+    o = h.default_options()
+    o.accel_factor = 1.1
+    o.precondition_type = 0
+    h.set_options(o)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain_lat = []
+    for r in base:
+        t1 = time.perf_counter()
+        h.set_matrix(r.row_ptr, r.col, r.val)
+        x = np.zeros_like(r.b)
+        meth = _capi.METHOD_ICCG if r.kind == serving.KIND_REAL_ICCG else _capi.METHOD_MRTR
+        h.solve(meth, np.ascontiguousarray(r.b), x, conv=TOL, max_ite=20000)
+        plain_lat.append(time.perf_counter() - t1)
+    t_plain = time.perf_counter() - t0
+    h.close()
+    plain_rate = len(base) / t_plain
+    line = {
+        "metric": "serving solves/s at saturation, p50/p99 latency (ms) over a rate sweep", "value": st_sat["solves_per_s"],
+        "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "strong", "vs_baseline": None,
+        "dtype": "f64/c128" + ("+fp32-inner" if args.precision != "fp64" else ""),
+        "data": "synthetic (seeded voxel generator)",
+        "config": {"workload": "request stream, sizes log-uniform 1k-500k unknowns, 70% real curl-curl ICCG, "
+                               "30% complex eddy-current IC-MRTR", "requests": len(base),
+                   "real": kinds.count(serving.KIND_REAL_ICCG), "complex": kinds.count(serving.KIND_COMPLEX_MRTR),
+                   "rows": int(sum(r.n for r in base)), "tolerance": TOL, "alpha": 1.1,
+                   "precision": "mixed" if args.precision != "fp64" else "fp64",
+                   "slots": {k: v for k, v in srv.cfg.slots.items()},
+                   "worst_true_relative_residual": worst},
+        "latency_ms": {"p50": st_sat["p50_ms"], "p99": st_sat["p99_ms"]},
+        "rate_sweep": sweep,
+        "plain_gpu_sequential": {"value": plain_rate, "unit": "solves/s",
+                                 "p50_ms": float(np.percentile(plain_lat, 50) * 1e3),
+                                 "p99_ms": float(np.percentile(plain_lat, 99) * 1e3),
+                                 "ratio": st_sat["solves_per_s"] / plain_rate},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def _spmv_host(rp, ci, val, x):
     import scipy.sparse as sp
     return sp.csr_matrix((val, ci, rp), shape=(len(rp) - 1, len(rp) - 1)) @ x
@@ -498,10 +591,14 @@ def _spmv_host(rp, ci, val, x):
 
 def main():
     args = parse()
+    if args.precision is None:
+        args.precision = "mixed" if args.workload == "cfg5" else "fp64"
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "cfg4":
         run_batch(args)
+    elif args.workload == "cfg5":
+        run_serving(args)
     else:
         run_ours(args)
 
