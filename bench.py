@@ -43,6 +43,16 @@ ALPHA = 1.1
 CPU_SAMPLE_ITERS = 10
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel, from one ncu
+# capture of the same workload: profiles/k_sweep_cluster_80cube.md (cluster sweeps, the automatic mode's choice
+# here) and profiles/k_sweep_fwd_80cube.md (sync-free forward sweep)
+NCU_TRAFFIC = {
+    ("cfg2", "fp64", "cluster", "forward sweep"): 348.0e6,
+    ("cfg2", "fp64", "cluster", "backward sweep"): 348.7e6,
+    ("cfg2", "fp64", "sync-free", "forward sweep"): 360.6e6,
+}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -342,7 +352,10 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_kind == "measured" else "fallback 6.8 TB/s",
-                     "traffic": None, "launch_ms": dms / max(dlaunch, 1), "launches": dlaunch},
+                     "traffic": NCU_TRAFFIC.get((args.workload, args.precision,
+                                                 "sync-free" if args.sweep_mode == 1 else "cluster", dom)),
+                     "traffic_source": "ncu capture in profiles/ (per launch)", "algorithmic_bytes": dbytes / max(dlaunch, 1),
+                     "launch_ms": dms / max(dlaunch, 1), "launches": dlaunch},
         "kernel_ms_per_step": {k: v[0] / args.steps for k, v in stats.items()},
         "clocks": clk, "host_s": t_host,
     }
@@ -508,7 +521,8 @@ def run_serving(args):
     torch.cuda.set_device(local)
     base = serving.synthetic_stream(args.requests, rate=0.0, seed=11)
     kinds = [r.kind for r in base]
-    be = serving.GpuBackend(local, precision=_capi.PREC_MIXED if args.precision != "fp64" else _capi.PREC_FP64)
+    # mixed: per kind (real ICCG mixed, complex IC-MRTR FP64, see serving.GpuBackend); fp64: everything FP64
+    be = serving.GpuBackend(local, precision=None if args.precision != "fp64" else _capi.PREC_FP64)
 
     def fresh(rate, seed):
         rng = np.random.default_rng(seed)
@@ -571,7 +585,7 @@ def run_serving(args):
                                "30% complex eddy-current IC-MRTR", "requests": len(base),
                    "real": kinds.count(serving.KIND_REAL_ICCG), "complex": kinds.count(serving.KIND_COMPLEX_MRTR),
                    "rows": int(sum(r.n for r in base)), "tolerance": TOL, "alpha": 1.1,
-                   "precision": "mixed" if args.precision != "fp64" else "fp64",
+                   "precision": ("real ICCG mixed, complex IC-MRTR fp64" if args.precision != "fp64" else "fp64"),
                    "slots": {k: v for k, v in srv.cfg.slots.items()},
                    "worst_true_relative_residual": worst},
         "latency_ms": {"p50": st_sat["p50_ms"], "p99": st_sat["p99_ms"]},

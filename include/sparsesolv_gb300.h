@@ -219,7 +219,13 @@ int ssg_batch_start(ssg_batch b, int method, double alpha, double conv, int max_
 /* non-blocking: queues further iterations when the previous ones finished; *done = 1 once every instance ended */
 int ssg_batch_poll(ssg_batch b, int *done);
 int ssg_batch_wait(ssg_batch b);
-/* solution, iteration counts and statuses (ST_* : 1 converged, 2 max_ite, 3 diverged) of system `index`;
+/* blocking for the iterations in flight only, then as ssg_batch_poll */
+int ssg_batch_step(ssg_batch b, int *done);
+/* *finished = 1 once every right-hand side of system `index` ended, as of the last
+ * completed iterations; its ssg_batch_result is then available while the batch runs on */
+int ssg_batch_finished(ssg_batch b, int index, int *finished);
+/* solution, iteration counts and statuses (ST_* : 1 converged, 2 max_ite, 3 diverged) of system `index`,
+ * after the batch ended or once ssg_batch_finished reports the system;
  * returns SSG_OK when all its right-hand sides converged, else SSG_NOT_CONVERGED */
 int ssg_batch_result(ssg_batch b, int index, void *X, int *iters, int *status);
 int ssg_batch_residual_log(ssg_batch b, int index, int rhs, double *log, int capacity, int *length);

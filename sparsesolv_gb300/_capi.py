@@ -27,7 +27,7 @@ EXPORTED = [
     "ssg_get_accel_used", "ssg_get_timings", "ssg_factor", "ssg_apply_precond", "ssg_spmv", "ssg_level_schedule",
     "ssg_update_values", "ssg_update_values_device", "ssg_get_stream", "ssg_set_profiling", "ssg_get_kernel_stats",
     "ssg_launch_count", "ssg_set_tuning", "ssg_ic_factor_noalloc", "ssg_batch_create", "ssg_batch_destroy",
-    "ssg_batch_last_error", "ssg_batch_add", "ssg_batch_set_rhs", "ssg_batch_clear", "ssg_batch_start", "ssg_batch_poll", "ssg_batch_wait",
+    "ssg_batch_last_error", "ssg_batch_add", "ssg_batch_set_rhs", "ssg_batch_clear", "ssg_batch_start", "ssg_batch_poll", "ssg_batch_wait", "ssg_batch_step", "ssg_batch_finished",
     "ssg_batch_result", "ssg_batch_residual_log", "ssg_batch_timings", "ssg_batch_stream",
     "ssg_batch_set_profiling", "ssg_batch_kernel_stats", "ssg_batch_set_precision",
 ]
@@ -93,6 +93,8 @@ def declare(lib):
         "ssg_batch_start": ([H, I, D, D, I], I),
         "ssg_batch_poll": ([H, pI], I),
         "ssg_batch_wait": ([H], I),
+        "ssg_batch_step": ([H, pI], I),
+        "ssg_batch_finished": ([H, I, pI], I),
         "ssg_batch_result": ([H, I, P, P, P], I),
         "ssg_batch_residual_log": ([H, I, I, P, I, pI], I),
         "ssg_batch_timings": ([H, P], I),
@@ -351,6 +353,17 @@ class Batch:
 
     def wait(self):
         self._check(self.lib.ssg_batch_wait(self.b), "ssg_batch_wait")
+
+    def step(self):
+        """Wait for the iterations in flight, queue more; True once every instance ended."""
+        d = ctypes.c_int(0)
+        self._check(self.lib.ssg_batch_step(self.b, ctypes.byref(d)), "ssg_batch_step")
+        return bool(d.value)
+
+    def finished(self, index):
+        f = ctypes.c_int(0)
+        self._check(self.lib.ssg_batch_finished(self.b, int(index), ctypes.byref(f)), "ssg_batch_finished")
+        return bool(f.value)
 
     def result(self, index):
         """(X (nrhs, n), iters (nrhs,), status (nrhs,), all converged)"""

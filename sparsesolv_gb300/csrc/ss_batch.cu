@@ -511,6 +511,7 @@ Batch::Batch(int dev) : h(dev) {
     h.cl_group = 8;
     SSG_CUDA(cudaEventCreateWithFlags(&ev_chunk, cudaEventDisableTiming));
     for (auto &e : ev) SSG_CUDA(cudaEventCreate(&e));
+    SSG_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
 }
 
 Batch::~Batch() {
@@ -520,6 +521,7 @@ Batch::~Batch() {
     if (h_octl) cudaFreeHost(h_octl);
     if (h_ost) cudaFreeHost(h_ost);
     if (ev_chunk) cudaEventDestroy(ev_chunk);
+    if (side) cudaStreamDestroy(side);
     for (auto &e : ev)
         if (e) cudaEventDestroy(e);
 }
@@ -744,6 +746,8 @@ void Batch::start(int method_, double alpha, double conv, int max_ite_) {
     }
     std::memset(h_ctl, 0, sizeof(KState));
     h_ctl->active = 1;
+    seen_st.clear();
+    seen_ost.clear();
     SSG_CUDA(cudaMemcpyAsync(d_st.p, h_st, sizeof(KState) * (size_t)S, cudaMemcpyHostToDevice, s));
     SSG_CUDA(cudaMemcpyAsync(ctl(), h_ctl, sizeof(KState), cudaMemcpyHostToDevice, s));
     SSG_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * (size_t)n, s));
@@ -848,6 +852,7 @@ void Batch::queue_chunk() {
     queued += todo;
     chunk = std::min(chunk * 2, 32);
     SSG_CUDA(cudaMemcpyAsync(h_ctl, ctl(), sizeof(KState), cudaMemcpyDeviceToHost, s));
+    SSG_CUDA(cudaMemcpyAsync(h_st, d_st.p, sizeof(KState) * (size_t)S, cudaMemcpyDeviceToHost, s));
     SSG_CUDA(cudaEventRecord(ev_chunk, s));
 }
 
@@ -857,6 +862,8 @@ bool Batch::poll() {
     if (q == cudaErrorNotReady) return false;
     SSG_CUDA(q);
     h.check_err("batched iterations");
+    seen_st.assign(h_st, h_st + S);
+    if (precision == SSG_PREC_MIXED) seen_ost.assign(h_ost, h_ost + S);
     if (precision == SSG_PREC_MIXED) {
         const bool cx = vtype == SSG_COMPLEX;
         if (h_ctl->active && queued < max_ite) {
@@ -894,6 +901,8 @@ bool Batch::poll() {
     int most = 0;
     for (int q = 0; q < S; ++q) most = std::max(most, h_st[q].it);
     if (precision == SSG_PREC_MIXED) most = 1 << 30;  // every profiled launch of a refinement did work
+    seen_st.assign(h_st, h_st + S);
+    if (precision == SSG_PREC_MIXED) seen_ost.assign(h_ost, h_ost + S);
     h.prof_flush(most);
     h.prof.iter = 0;
     float a = 0.f, b = 0.f;
@@ -908,10 +917,29 @@ void Batch::wait() {
     while (!poll()) SSG_CUDA(cudaEventSynchronize(ev_chunk));
 }
 
-int Batch::result(int index, double *X, int *iters, int *status) {
-    if (running) throw Error{SSG_ERR_STATE, "batch is running"};
+bool Batch::step() {
+    if (!running) return true;
+    SSG_CUDA(cudaEventSynchronize(ev_chunk));
+    return poll();
+}
+
+bool Batch::finished(int index) const {
     if (index < 0 || index >= (int)sys.size()) throw Error{SSG_ERR_ARG, "bad system index"};
-    if (!assembled || t_ms.empty()) throw Error{SSG_ERR_STATE, "no finished solve"};
+    if (!running) return !t_ms.empty();
+    const bool mixed = precision == SSG_PREC_MIXED;
+    if ((int)seen_st.size() != S || (mixed && (int)seen_ost.size() != S)) return false;
+    for (int q = 0; q < S; ++q)
+        if (inst_sys[q] == index && (mixed ? seen_ost[q].active : seen_st[q].active)) return false;
+    return true;
+}
+
+// Allowed while the batch runs once the system's instances ended: their rows of
+// x are no longer written (every update kernel skips ended instances).
+int Batch::result(int index, double *X, int *iters, int *status) {
+    if (index < 0 || index >= (int)sys.size()) throw Error{SSG_ERR_ARG, "bad system index"};
+    if (!assembled || (!running && t_ms.empty())) throw Error{SSG_ERR_STATE, "no finished solve"};
+    if (running && !finished(index)) throw Error{SSG_ERR_STATE, "system still running"};
+    cudaStream_t cs = running ? side : h.stream;
     const size_t vb = vtype == SSG_COMPLEX ? 16 : 8;
     int rc = SSG_OK;
     for (int q = 0; q < S; ++q) {
@@ -919,15 +947,15 @@ int Batch::result(int index, double *X, int *iters, int *status) {
         const int j = inst_rhs[q], n = sys[index].n;
         if (X)
             SSG_CUDA(cudaMemcpyAsync((char *)X + vb * (size_t)n * j, h.vec[8].as<char>() + vb * (size_t)inst_row[q],
-                                     vb * (size_t)n, cudaMemcpyDeviceToHost, h.stream));
+                                     vb * (size_t)n, cudaMemcpyDeviceToHost, cs));
         const bool mixed = precision == SSG_PREC_MIXED;
-        const int it = mixed ? h_ost[q].inner_total : h_st[q].it;
-        const int stt = mixed ? h_ost[q].status : h_st[q].status;
+        const int it = mixed ? seen_ost[q].inner_total : seen_st[q].it;
+        const int stt = mixed ? seen_ost[q].status : seen_st[q].status;
         if (iters) iters[j] = it;
         if (status) status[j] = stt;
         if (stt != ST_CONVERGED) rc = SSG_NOT_CONVERGED;
     }
-    SSG_CUDA(cudaStreamSynchronize(h.stream));
+    SSG_CUDA(cudaStreamSynchronize(cs));
     return rc;
 }
 
@@ -943,8 +971,8 @@ int Batch::residual_log(int index, int rhs, double *out, int capacity, int *leng
     const int q = instance(index, rhs);
     if (q < 0) throw Error{SSG_ERR_ARG, "bad system index or right-hand side"};
     // mixed precision: the log holds |b - A x| / |b| after each refinement step
-    const int len = h_st[q].log_len >= 0 ? h_st[q].log_len
-                    : (precision == SSG_PREC_MIXED ? h_ost[q].outer_it + 1 : h_st[q].it + 1);
+    const int len = seen_st[q].log_len >= 0 ? seen_st[q].log_len
+                    : (precision == SSG_PREC_MIXED ? seen_ost[q].outer_it + 1 : seen_st[q].it + 1);
     if (length) *length = len;
     if (out && capacity > 0) {
         const int m = std::min(capacity, len);
@@ -1114,6 +1142,8 @@ void Batch::queue_inner(int todo) {
     chunk = std::min(chunk * 2, 32);
     SSG_CUDA(cudaMemcpyAsync(h_ctl, ctl(), sizeof(KState), cudaMemcpyDeviceToHost, s));
     SSG_CUDA(cudaMemcpyAsync(h_octl, octl(), sizeof(KState), cudaMemcpyDeviceToHost, s));
+    SSG_CUDA(cudaMemcpyAsync(h_st, d_st.p, sizeof(KState) * (size_t)S, cudaMemcpyDeviceToHost, s));
+    SSG_CUDA(cudaMemcpyAsync(h_ost, d_ost.p, sizeof(OState) * (size_t)S, cudaMemcpyDeviceToHost, s));
     SSG_CUDA(cudaEventRecord(ev_chunk, s));
 }
 

@@ -113,6 +113,12 @@ struct Batch {
     void queue_chunk();
     bool poll();  // true when finished
     void wait();
+    bool step();  // waits for the iterations in flight, queues more; true when finished
+    bool finished(int index) const;  // every instance of system `index` ended (as of the last completed chunk)
+    // instance states as of the last completed chunk (the pinned copies are refilled by the next one)
+    std::vector<KState> seen_st;
+    std::vector<OState> seen_ost;
+    cudaStream_t side = nullptr;  // copies of finished results while the batch runs
     int result(int index, double *X, int *iters, int *status);
     int residual_log(int index, int rhs, double *out, int capacity, int *length);
     int instance(int index, int rhs) const;

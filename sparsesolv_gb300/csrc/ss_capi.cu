@@ -479,6 +479,22 @@ int ssg_batch_poll(ssg_batch bd, int *done) {
     });
 }
 
+int ssg_batch_step(ssg_batch bd, int *done) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        const bool d = b.step();
+        if (done) *done = d ? 1 : 0;
+        return SSG_OK;
+    });
+}
+
+int ssg_batch_finished(ssg_batch bd, int index, int *finished) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        const bool f = b.finished(index);
+        if (finished) *finished = f ? 1 : 0;
+        return SSG_OK;
+    });
+}
+
 int ssg_batch_wait(ssg_batch bd) {
     return bguarded(bd, [&](ssg::Batch &b) {
         b.wait();

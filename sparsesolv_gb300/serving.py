@@ -3,10 +3,12 @@
 Requests of one kind (real ICCG, complex IC-MRTR) wait in that kind's queue.
 Each kind has a few slots; a slot is a reusable batch (its own CUDA stream,
 device buffers kept between uses and between streams) served by one worker
-thread. A free slot takes the oldest waiting request of its kind together
-with the waiting requests of similar size, as many as fit its row budget and
+thread. A free slot takes the waiting requests of its kind in arrival order
+(optionally only those of similar size), as many as fit its row budget and
 the free device memory, solves them in shared launches and hands each result
-back. Requests that arrive while others are on the GPU are
+back as soon as that request's own solve has ended. A batch costs about the
+depth x iterations of its largest system, so smaller systems ride along
+nearly free, and early delivery keeps their latency their own. Requests that arrive while others are on the GPU are
 admitted by the next slot that frees up, so the work of several batches
 overlaps on the device (the C calls release the GIL).
 
@@ -58,18 +60,29 @@ class Request:
 
 
 class GpuBackend:
-    """Slots are ssg_batch objects; free memory from the CUDA runtime."""
+    """Slots are ssg_batch objects; free memory from the CUDA runtime.
+
+    precision None picks per kind, by measurement: real curl-curl ICCG in mixed
+    precision (two refinement steps, faster at every size), complex
+    eddy-current IC-MRTR in FP64 (FP32 rounding of these systems lets one inner
+    solve gain little, so large ones need dozens of refinement steps and run
+    slower than FP64)."""
 
     def __init__(self, device=0, precision=None, alpha=1.1, tol=1e-8, max_ite=5000):
         from . import _capi
         self.capi = _capi
         self.device = device
-        self.precision = _capi.PREC_MIXED if precision is None else precision
+        self.precision = precision
         self.alpha, self.tol, self.max_ite = alpha, tol, max_ite
+
+    def precision_of(self, kind):
+        if self.precision is not None:
+            return self.precision
+        return self.capi.PREC_MIXED if kind == KIND_REAL_ICCG else self.capi.PREC_FP64
 
     def new_slot(self, kind):
         bt = self.capi.Batch(self.device)
-        bt.set_precision(self.precision)
+        bt.set_precision(self.precision_of(kind))
         return bt
 
     def free_bytes(self):
@@ -77,17 +90,24 @@ class GpuBackend:
         free, _ = torch.cuda.mem_get_info(self.device)
         return int(free)
 
-    def solve(self, slot, kind, reqs):
-        """Blocking: solve reqs in one batch on slot; fills x, iters, converged."""
+    def solve(self, slot, kind, reqs, deliver=None):
+        """Blocking: solve reqs in one batch on slot; fills x, iters, converged
+        and calls deliver(r) for each request as soon as its own solve ended."""
         slot.clear()
         for r in reqs:
             slot.add(r.row_ptr, r.col, r.val, r.b)
         meth = self.capi.METHOD_ICCG if kind == KIND_REAL_ICCG else self.capi.METHOD_MRTR
         slot.start(meth, self.alpha, conv=self.tol, max_ite=self.max_ite)
-        slot.wait()
-        for k, r in enumerate(reqs):
-            X, it, _, ok = slot.result(k)
-            r.x, r.iters, r.converged = X[0], int(it[0]), bool(ok)
+        pending = list(range(len(reqs)))
+        while pending:
+            done = slot.step()
+            for k in [k for k in pending if done or slot.finished(k)]:
+                X, it, _, ok = slot.result(k)
+                r = reqs[k]
+                r.x, r.iters, r.converged = X[0], int(it[0]), bool(ok)
+                pending.remove(k)
+                if deliver:
+                    deliver(r)
 
     def close_slot(self, slot):
         slot.close()
@@ -97,7 +117,7 @@ class GpuBackend:
 class ServerConfig:
     slots: dict = field(default_factory=lambda: {KIND_REAL_ICCG: 3, KIND_COMPLEX_MRTR: 2})
     max_rows_per_batch: int = 3_000_000
-    size_ratio: float = 2.0            # a batch groups requests within this factor of its oldest one
+    size_ratio: float = 0.0            # > 1: a batch only groups requests within this factor of its oldest one
     bytes_per_nnz: float = 96.0        # device bytes a request needs per matrix entry (estimate)
     memory_reserve: int = 2 << 30      # left free for everything else
 
@@ -134,7 +154,8 @@ class Server:
         if self._need(head) > free and self.reserved > 0:
             return []  # wait for memory held by running batches
         out, rows, need = [head], head.n, self._need(head)
-        lo, hi = head.n / self.cfg.size_ratio, head.n * self.cfg.size_ratio
+        ratio = self.cfg.size_ratio if self.cfg.size_ratio > 1.0 else float("inf")
+        lo, hi = head.n / ratio, head.n * ratio
         for r in list(q)[1:]:
             if not lo <= r.n <= hi:
                 continue
@@ -175,14 +196,19 @@ class Server:
             for r in reqs:
                 r.admitted = now
                 r.batch_size = len(reqs)
+
+            def deliver(r):
+                r.done = self.clock() - self.t0
+
             try:
-                self.backend.solve(slot, kind, reqs)
+                self.backend.solve(slot, kind, reqs, deliver)
             except Exception as e:  # recorded; the requests stay unsolved
                 self.errors.append(e)
             done = self.clock() - self.t0
             with self.lock:
                 for r in reqs:
-                    r.done = done
+                    if r.done < 0:
+                        r.done = done
                 self.reserved -= sum(self._need(r) for r in reqs)
                 self.lock.notify_all()
 

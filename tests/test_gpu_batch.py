@@ -171,3 +171,36 @@ def test_batch_argument_errors(gpu, systems):
             bt.start(_capi.METHOD_ICCG, -1.0)  # no automatic shift in batches
     finally:
         bt.close()
+
+
+def test_finished_system_result_while_batch_runs(gpu):
+    """A small system's result can be taken as soon as it ends; it equals the
+    result read after the whole batch ended."""
+    small = voxel.curl_curl_case(6, seed=1, iron_size=2).assemble()
+    large = voxel.curl_curl_case(24, seed=2, iron_size=6).assemble()
+    bt = _capi.Batch(0)
+    try:
+        bt.add(*small)
+        bt.add(*large)
+        bt.start(_capi.METHOD_ICCG, ALPHA, conv=1e-8, max_ite=5000)
+        early = None
+        done = False
+        while not done:
+            done = bt.step()
+            if early is None and bt.finished(0):
+                early = bt.result(0)
+                seen_running = not done
+        assert early is not None and seen_running
+        late = bt.result(0)
+        assert np.array_equal(early[0], late[0]) and np.array_equal(early[1], late[1])
+        with pytest.raises(_capi.SolverError):  # a running system's result is refused
+            bt.start(_capi.METHOD_ICCG, ALPHA, conv=1e-8, max_ite=5000)
+            try:
+                if not bt.finished(1):
+                    bt.result(1)
+                else:
+                    raise _capi.SolverError(-6, "large system ended before the check")
+            finally:
+                bt.wait()
+    finally:
+        bt.close()

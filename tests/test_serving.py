@@ -31,7 +31,7 @@ class FakeBackend:
     def free_bytes(self):
         return self.free
 
-    def solve(self, slot, kind, reqs):
+    def solve(self, slot, kind, reqs, deliver=None):
         with self.lock:
             self.batches.append((kind, [r.rid for r in reqs]))
             self.active += 1
@@ -40,6 +40,8 @@ class FakeBackend:
         for r in reqs:
             r.x = np.full(r.n, float(r.rid))
             r.iters, r.converged = 1, True
+            if deliver:
+                deliver(r)
         with self.lock:
             self.active -= 1
 
@@ -52,7 +54,8 @@ def req(rid, arrival, n, kind=KIND_REAL_ICCG, nnz_per_row=33):
 
 def test_all_requests_complete_in_kind_and_arrival_order():
     be = FakeBackend()
-    cfg = ServerConfig(slots={KIND_REAL_ICCG: 2, KIND_COMPLEX_MRTR: 1}, max_rows_per_batch=50_000, memory_reserve=0)
+    cfg = ServerConfig(slots={KIND_REAL_ICCG: 2, KIND_COMPLEX_MRTR: 1}, max_rows_per_batch=50_000, memory_reserve=0,
+                       size_ratio=2.0)
     rng = np.random.default_rng(0)
     reqs = [req(i, 0.002 * i, int(rng.integers(1_000, 20_000)),
                 KIND_COMPLEX_MRTR if i % 3 == 0 else KIND_REAL_ICCG) for i in range(40)]
@@ -71,6 +74,18 @@ def test_all_requests_complete_in_kind_and_arrival_order():
             assert ids == sorted(ids)
             assert all(reqs[ids[0]].n / cfg.size_ratio <= reqs[i].n <= reqs[ids[0]].n * cfg.size_ratio for i in ids)
         assert sorted(i for ids in mine for i in ids) == [r.rid for r in reqs if r.kind == kind]
+
+
+def test_default_batches_fill_in_arrival_order():
+    be = FakeBackend()
+    cfg = ServerConfig(slots={KIND_REAL_ICCG: 1}, max_rows_per_batch=25_000, memory_reserve=0)
+    rng = np.random.default_rng(1)
+    reqs = [req(i, 0.0, int(rng.integers(1_000, 20_000))) for i in range(20)]
+    Server(be, cfg).run(reqs)
+    order = [i for _, ids in be.batches for i in ids]
+    assert order == list(range(20))  # one slot: batches are consecutive runs of the queue
+    for _, ids in be.batches:
+        assert len(ids) == 1 or sum(reqs[i].n for i in ids) <= cfg.max_rows_per_batch
 
 
 def test_free_memory_limits_admission():
