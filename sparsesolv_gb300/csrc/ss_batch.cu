@@ -652,14 +652,19 @@ void Batch::assemble() {
     SSG_CUDA(cudaMemcpyAsync(d_sys_tile.p, sys_tile.data(), sizeof(int) * (size_t)(S + 1), cudaMemcpyHostToDevice, st));
     SSG_CUDA(cudaMemcpyAsync(d_sys_row.p, inst_row.data(), sizeof(int) * (size_t)(S + 1), cudaMemcpyHostToDevice, st));
     SSG_CUDA(cudaMemsetAsync(d_ctl_counter.p, 0, sizeof(KState) + 64, st));
-    if (h_st) cudaFreeHost(h_st);
-    h_st = nullptr;
-    SSG_CUDA(cudaMallocHost((void **)&h_st, sizeof(KState) * (size_t)S));
+    // pinned copies grow only: freeing pinned memory waits for the whole device
+    if (S > h_cap) {
+        if (h_st) cudaFreeHost(h_st);
+        if (h_ost) cudaFreeHost(h_ost);
+        h_st = nullptr;
+        h_ost = nullptr;
+        const int cap = std::max(S, 2 * h_cap);
+        SSG_CUDA(cudaMallocHost((void **)&h_st, sizeof(KState) * (size_t)cap));
+        SSG_CUDA(cudaMallocHost((void **)&h_ost, sizeof(OState) * (size_t)cap));
+        h_cap = cap;
+    }
     if (!h_ctl) SSG_CUDA(cudaMallocHost((void **)&h_ctl, sizeof(KState)));
     if (!h_octl) SSG_CUDA(cudaMallocHost((void **)&h_octl, sizeof(KState)));
-    if (h_ost) cudaFreeHost(h_ost);
-    h_ost = nullptr;
-    SSG_CUDA(cudaMallocHost((void **)&h_ost, sizeof(OState) * (size_t)S));
     d_ost.ensure(sizeof(OState) * (size_t)S);
     d_octl.ensure(sizeof(KState));
     SSG_CUDA(cudaStreamSynchronize(st));
@@ -1000,14 +1005,14 @@ void Batch::precond32(const Ti *r, Ti *z, const KState *stp) {
     const int n = h.n;
     Ti *y = v32[10].as<Ti>();
     const double fb = (4.0 + v) * h.Lf.nnz + 4.0 * (n + 1) + 2.0 * v * n;
-    if (h.cluster_ok(h.Lf, v) && h.cluster_ok(h.Ltb, v)) {
+    if (h.cluster_ok(h.Lf, v, true) && h.cluster_ok(h.Ltb, v, true)) {
         h.timed(PC_FWD, fb, [&] {
             sweep_cluster<Ti>(h.Lf, L32.as<Ti>(), SW_FWD_DIV, r, nullptr, h.use_inv_diag ? invL32_lev.as<Ti>() : nullptr,
-                              y, nullptr, stp, h.cl_group, s);
+                              y, nullptr, stp, h.cl_group, h.err(), s);
         });
         h.timed(PC_BWD, fb + v * n, [&] {
             sweep_cluster<Ti>(h.Ltb, Lt32.as<Ti>(), SW_BWD_IC, nullptr, y, D32_lev.as<Ti>(), z, nullptr, stp,
-                              h.cl_group, s);
+                              h.cl_group, h.err(), s);
         });
         return;
     }
@@ -1188,6 +1193,7 @@ int solve_mixed(Handle &h, Batch *&mb, uint64_t &mver, uint64_t &mpat, int metho
     }
     if (!mb) mb = new Batch(h.device);
     mb->h.prof.on = h.prof.on;  // profiling follows the owning handle
+    AllocStream as(mb->h.stream);  // the batch's buffers are ordered on its own stream
     const int w = h.vtype == SSG_COMPLEX ? 2 : 1;
     if (mver != h.version && mpat == h.pattern_id && mb->assembled && !mb->sys.empty() && mb->vtype == h.vtype) {
         // values-only update: the batch keeps its pattern analysis

@@ -66,6 +66,7 @@ struct Batch {
     bool rhs_dirty = true;  // right-hand sides changed since the last upload
     DBuf d_tile, d_tile_sys, d_sys_tile, d_sys_row, d_st, d_part, d_logs, d_ctl_counter;
     KState *h_st = nullptr;   // pinned copy of the instance states
+    int h_cap = 0;            // instances the pinned copies hold
     KState *h_ctl = nullptr;  // pinned copy of the control state
     cudaEvent_t ev_chunk = nullptr;
     // the running solve

@@ -27,6 +27,7 @@ int guarded(ssg_handle hd, F &&f) {
     if (!hd || !hd->h) return SSG_ERR_ARG;
     try {
         SSG_CUDA(cudaSetDevice(hd->h->device));
+        ssg::AllocStream as(hd->h->stream);
         return f(*hd->h);
     } catch (const Error &e) {
         hd->h->last_error = e.msg;
@@ -53,6 +54,7 @@ int bguarded(ssg_batch bd, F &&f) {
     if (!bd || !bd->b) return SSG_ERR_ARG;
     try {
         SSG_CUDA(cudaSetDevice(bd->b->h.device));
+        ssg::AllocStream as(bd->b->h.stream);
         return f(*bd->b);
     } catch (const Error &e) {
         bd->err = e.msg;
@@ -108,7 +110,7 @@ int ssg_create(ssg_handle *out, int device) {
 int ssg_destroy(ssg_handle hd) {
     if (!hd) return SSG_ERR_ARG;
     if (hd->h) cudaSetDevice(hd->h->device);
-    hd->io_b.release();
+    hd->io_b.release();  // freed on the handle's stream, which lives until delete hd->h
     hd->io_x.release();
     delete hd->mixed;
     delete hd->h;
@@ -274,7 +276,7 @@ int ssg_set_tuning(ssg_handle hd, int key, int value) {
                 h.use_inv_diag = value != 0;
                 break;
             case SSG_TUNE_SWEEP_MODE:
-                if (value < 0 || value > 2) return SSG_ERR_ARG;
+                if (value < 0 || value > 3) return SSG_ERR_ARG;
                 h.sweep_mode = value;
                 break;
             case SSG_TUNE_CLUSTER_RING_KB:

@@ -28,6 +28,7 @@
 // number of times by every thread.
 #include <algorithm>
 
+#include "sparsesolv_gb300.h"
 #include "ss_internal.cuh"
 #include "ss_krylov.cuh"
 
@@ -38,6 +39,7 @@ constexpr int CL_STORE_K = 8;   // store warp releases every K levels
 constexpr int CL_SPAN_BUFS = 5; // matrix span staged 4 levels ahead
 constexpr int CL_GATH_BUFS = 3; // gathered inputs staged 2 levels ahead
 constexpr int CL_PAD = 4;       // entries copied beyond a span to keep the 16-byte copies aligned
+constexpr int CL_LEAD = 4;      // neighbour-synchronised sweep: levels a CTA may run ahead of every other
 
 __device__ __forceinline__ unsigned cluster_rank() {
     unsigned r;
@@ -68,6 +70,15 @@ __device__ __forceinline__ void bar_arrive(int id, int count) {
 }
 __device__ __forceinline__ void bar_sync(int id, int count) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+// progress word of the neighbour-synchronised sweep: levels this CTA has completed
+__device__ __forceinline__ void st_release_progress(unsigned local_addr, unsigned v) {
+    asm volatile("st.release.cluster.shared::cta.u32 [%0], %1;" ::"r"(local_addr), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire_progress(unsigned cluster_addr) {
+    unsigned v;
+    asm volatile("ld.acquire.cluster.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(cluster_addr) : "memory");
+    return v;
 }
 template <int BYTES>
 __device__ __forceinline__ void cp_async(unsigned dst, const void *src) {
@@ -166,7 +177,8 @@ struct ClLayout {
     int ring2;  // second ring for the fused Eisenstat output (0/1)
     int ngath;  // gathered per-row inputs (1 or 2)
     // byte offsets
-    int o_ring, o_ring2, o_span, span_bytes, o_codes, o_vals, o_prp, o_perm, o_lvec, o_gath, gath_bytes, o_tab, total;
+    int o_ring, o_ring2, o_span, span_bytes, o_codes, o_vals, o_prp, o_perm, o_lvec, o_gath, gath_bytes, o_tab, o_prog,
+        total;
 };
 
 __host__ __device__ inline int al16(int x) { return (x + 15) & ~15; }
@@ -200,19 +212,25 @@ __host__ __device__ inline ClLayout cl_layout(int S, int cap_r, int cap_e, int e
     L.o_gath = o;
     L.gath_bytes = al16(cap_r * elem * ngath);
     o += CL_GATH_BUFS * L.gath_bytes;
-    L.o_tab = o;  // per level: (rs, re, e0, e1) of this CTA's chunk
+    L.o_tab = o;  // per level: this CTA's chunk (see cluster_plan for the packing)
     o += al16(nlev * 16);
+    L.o_prog = o;  // neighbour-synchronised sweep: progress word
+    o += 16;
     L.total = o;
     return L;
 }
 
-template <typename T, int G, int MODE>
+// P2P: neighbour-synchronised. No cluster barrier per level: the store warp
+// publishes the CTA's progress (a release on a shared-memory word) and, before
+// the next level, waits (bounded) until every CTA this chunk reads from has
+// published the levels it needs and no CTA is more than CL_LEAD levels behind.
+template <typename T, int G, int MODE, bool P2P>
 __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, const int *__restrict__ lptr,
                                                         const int *__restrict__ perm, const int *__restrict__ prp,
                                                         const int *__restrict__ code, const T *__restrict__ val,
                                                         const T *__restrict__ lvec, const T *rhs, const T *aux, T *out,
                                                         T *out2, const KState *st, const int4 *__restrict__ tab,
-                                                        ClLayout Lay) {
+                                                        int *err, ClLayout Lay) {
     if (st && !st->active) return;  // uniform across the cluster
     extern __shared__ __align__(16) unsigned char cl_smem[];
     const unsigned sbase = (unsigned)__cvta_generic_to_shared(cl_smem);
@@ -233,10 +251,12 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
     int4 *s_tab = (int4 *)(cl_smem + Lay.o_tab);
     for (int q = tid; q < nlev; q += nthreads) s_tab[q] = __ldg(tab + (size_t)q * C + rank);
     __syncthreads();
+    // table entry: x = first row, y = rows | producer mask << 16, z = first entry,
+    // w = entries | (level - required progress) << 16 (signed)
     auto chunk_of = [&](int l, int &rs, int &re) {
         const int4 c4 = s_tab[l];
         rs = c4.x;
-        re = c4.y;
+        re = c4.x + (c4.y & 0xFFFF);
     };
     auto span_base = [&](int l) { return Lay.o_span + (l % CL_SPAN_BUFS) * Lay.span_bytes; };
     auto gath_base = [&](int l) { return Lay.o_gath + (l % CL_GATH_BUFS) * Lay.gath_bytes; };
@@ -251,7 +271,7 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
         chunk_of(l, rs, re);
         const int cnt = re - rs;
         if (cnt <= 0) return;
-        const int e0 = s_tab[l].z, e1 = s_tab[l].w;
+        const int e0 = s_tab[l].z, e1 = s_tab[l].z + (s_tab[l].w & 0xFFFF);
         const int sb = span_base(l);
         const int c0 = e0 & ~(CPE - 1), v0 = e0 & ~(VPE - 1);
         for (int i = tid; i * CPE < e1 - c0; i += ncomp)
@@ -283,6 +303,12 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
         }
     };
 
+    if (P2P) {
+        // every CTA's progress word is zero before any CTA reads another's
+        if (tid == 0) *(volatile unsigned *)(cl_smem + Lay.o_prog) = 0u;
+        cluster_arrive_release();
+        cluster_wait_acquire();
+    }
     // prologue: spans of levels 0..3, then gathers of levels 0..1
     for (int q = 0; q < CL_SPAN_BUFS - 1; ++q) stage_span(q);
     cp_async_commit();
@@ -368,27 +394,72 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
             }
             // results are in the ring: let the store warp copy them out
             bar_arrive(1, nthreads);
-            cluster_arrive_release();
+            if (P2P) {
+                // publish: the compute warps have only shared-memory stores pending,
+                // so this release is short
+                bar_sync(2, ncomp);
+                if (tid == 0) st_release_progress(sbase + Lay.o_prog, (unsigned)(l + 1));
+            } else {
+                cluster_arrive_release();
+            }
             // C: stage the gathers of level l+2 (its span landed) and the span of level l+4
             // while the barrier completes: two groups, the span one newest
             stage_gath(l + 2);
             cp_async_commit();
             stage_span(l + CL_SPAN_BUFS - 1);
             cp_async_commit();
-            cluster_wait_acquire();
+            if (!P2P) cluster_wait_acquire();
         } else {
             bar_sync(1, nthreads);
-            // release at every K-th level publishes the stores of the earlier levels
-            if (l % CL_STORE_K == 0) cluster_arrive_release();
-            else cluster_arrive_relaxed();
+            if (!P2P) {
+                // release at every K-th level publishes the stores of the earlier levels
+                if (l % CL_STORE_K == 0) cluster_arrive_release();
+                else cluster_arrive_relaxed();
+            }
             for (int i = tid - ncomp; i < cnt; i += nthreads - ncomp) {
                 const int r = sperm[i];
                 out[r] = ring[(produced + i) % Lay.S];
                 if (eis) out2[r] = ring2[(produced + i) % Lay.S];
             }
-            cluster_wait_acquire();
+            if (!P2P) {
+                cluster_wait_acquire();
+            } else if (l + 1 < nlev) {
+                // before level l+1: the CTAs it reads from have published what it needs,
+                // and no CTA is more than CL_LEAD levels behind (its ring entries stay
+                // valid); lane q watches CTA q, bounded in time
+                const int q = tid - ncomp;
+                if (q < C && q != rank) {
+                    const int4 nx = s_tab[l + 1];
+                    const int mask = (nx.y >> 16) & 0xFFFF;
+                    const int delta = nx.w >> 16;  // level - required progress (signed)
+                    int req = ((mask >> q) & 1) ? (l + 1) - delta : 0;
+                    req = max(req, (l + 1) - CL_LEAD);
+                    if (req > 0) {
+                        const unsigned ra = map_shared(sbase + Lay.o_prog, (unsigned)q);
+                        if ((int)ld_acquire_progress(ra) < req) {
+                            const unsigned long long t0 = gtimer();
+                            int polls = 0;
+                            while ((int)ld_acquire_progress(ra) < req) {
+                                if ((++polls & 63) == 0) {
+                                    if (*(volatile int *)err) break;
+                                    if (gtimer() - t0 > SPIN_LIMIT_NS) {
+                                        atomicExch(err, ERR_TIMEOUT);
+                                        break;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
+            }
         }
         produced += cnt;
+    }
+    if (P2P) {
+        // no CTA leaves while another may still read its shared memory
+        cluster_arrive_release();
+        cluster_wait_acquire();
     }
 }
 
@@ -437,11 +508,51 @@ __global__ void k_cl_codes(int n, const int *perm, const int *level, const int *
     }
 }
 
+// neighbour-synchronised plan: every dependency on another CTA must sit in that
+// CTA's ring even when the producer is CL_LEAD levels ahead (else infeasible);
+// own values older than the ring are read from memory (stored by this CTA's
+// store warp before any later level starts). Per (level, CTA): the producers
+// read (mask) and the progress they must have published (the largest level read + 1).
+__global__ void k_cl_codes_p2p(int n, const int *perm, const int *level, const int *prp, const int *pci,
+                               const int *ipos, const unsigned char *owner, const int *ord, const int *end_ord, int C,
+                               int S, int nlev, int *code, int *needmask, int *needreq, int *infeasible) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int lt = level[perm[t]];
+    const int cons = owner[t];
+    for (int k = prp[t]; k < prp[t + 1]; ++k) {
+        const int j = pci[k];
+        const int lj = level[j];
+        if (lj >= lt) {
+            code[k] = j;
+            continue;
+        }
+        const int p = ipos[j];
+        const int c = owner[p];
+        const int o = ord[p];
+        if (c == cons) {
+            const int written = end_ord[lt * C + c];
+            code[k] = (written - o <= S) ? -1 - ((c << CL_SLOT_BITS) | (o % S)) : j;
+        } else {
+            const int lk = min(lt + CL_LEAD, nlev - 1);
+            const int written = end_ord[lk * C + c];
+            if (written - o <= S) {
+                code[k] = -1 - ((c << CL_SLOT_BITS) | (o % S));
+                atomicOr(needmask + lt * C + cons, 1 << c);
+                atomicMax(needreq + lt * C + cons, lj + 1);
+            } else {
+                code[k] = j;
+                atomicExch(infeasible, 1);
+            }
+        }
+    }
+}
+
 static int g_cluster_size = -1;
 
 template <typename T>
 static int probe_cluster(int smem) {
-    auto kern = k_sweep_cluster<T, 4, SW_FWD_DIV>;
+    auto kern = k_sweep_cluster<T, 4, SW_FWD_DIV, false>;
     for (int C : {16, 8}) {
         if (C > 8) {
             if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
@@ -478,7 +589,7 @@ int cluster_size_available() {
     return g_cluster_size;
 }
 
-void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBuf &tmp) {
+void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBuf &tmp, bool p2p) {
     (void)tmp;
     T.cl_ready = false;
     if (T.n == 0) return;
@@ -503,6 +614,9 @@ void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBu
     std::vector<int> prp(T.n + 1);
     SSG_CUDA(cudaMemcpyAsync(prp.data(), T.prp.p, sizeof(int) * (size_t)(T.n + 1), cudaMemcpyDeviceToHost, s));
     SSG_CUDA(cudaStreamSynchronize(s));
+    // table entry per (level, CTA): x = first row, y = rows | producer mask << 16,
+    // z = first entry, w = entries | (level - required progress) << 16; the mask and
+    // the requirement are filled for the neighbour-synchronised sweep
     int cap_e = 1;
     std::vector<int4> tab((size_t)nlev * C);
     for (int l = 0; l < nlev; ++l) {
@@ -511,12 +625,15 @@ void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBu
         for (int c = 0; c < C; ++c) {
             const int rs = std::min(L0 + c * chunk, L1), re = std::min(rs + chunk, L1);
             cap_e = std::max(cap_e, prp[re] - prp[rs]);
-            tab[(size_t)l * C + c] = make_int4(rs, re, prp[rs], prp[re]);
+            tab[(size_t)l * C + c] = make_int4(rs, re - rs, prp[rs], prp[re] - prp[rs]);
         }
     }
+    if (cap_r > 0xFFFF || cap_e > 0xFFFF) return;  // the packed table holds 16-bit counts
     const int elem = (int)elem_bytes;
-    // sized for the fused Eisenstat sweep (second ring, two gathered inputs), the largest mode
-    const ClLayout lay = cl_layout(ring_bytes / elem, cap_r, cap_e, elem, 1, 2, nlev);
+    // sized for the fused Eisenstat sweep (second ring, two gathered inputs), the largest
+    // mode; the neighbour-synchronised plan serves the IC sweeps only
+    const ClLayout lay = p2p ? cl_layout(ring_bytes / elem, cap_r, cap_e, elem, 0, 1, nlev)
+                             : cl_layout(ring_bytes / elem, cap_r, cap_e, elem, 1, 2, nlev);
     if (T.nnz_pad < CL_PAD) return;  // the value arrays must carry padding for the aligned copies
     if (lay.total > CL_SMEM_MAX || lay.S >= (1 << CL_SLOT_BITS)) return;  // sync-free sweep instead
     const int S = lay.S;
@@ -530,19 +647,45 @@ void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBu
     k_cl_positions<<<div_up(T.n, 256), 256, 0, s>>>(T.n, T.perm.as<int>(), T.level.as<int>(), T.lptr_d.as<int>(),
                                                    eo.as<int>(), C, owner.as<unsigned char>(), ord.as<int>());
     SSG_LAUNCHED();
-    T.cl_tab.ensure(sizeof(int4) * tab.size());
-    SSG_CUDA(cudaMemcpyAsync(T.cl_tab.p, tab.data(), sizeof(int4) * tab.size(), cudaMemcpyHostToDevice, s));
     T.cl_code.ensure(sizeof(int) * (size_t)(T.nnz + T.nnz_pad));
     SSG_CUDA(cudaMemsetAsync(T.cl_code.p, 0, sizeof(int) * (size_t)(T.nnz + T.nnz_pad), s));
-    k_cl_codes<<<div_up(T.n, 256), 256, 0, s>>>(T.n, T.perm.as<int>(), T.level.as<int>(), T.prp.as<int>(),
-                                                T.pci.as<int>(), T.ipos.as<int>(), owner.as<unsigned char>(),
-                                                ord.as<int>(), eo.as<int>(), C, S, CL_STORE_K, T.cl_code.as<int>(),
-                                                inf.as<int>());
-    SSG_LAUNCHED();
+    if (p2p) {
+        DBuf nm, nr;
+        nm.alloc(sizeof(int) * tab.size());
+        nr.alloc(sizeof(int) * tab.size());
+        SSG_CUDA(cudaMemsetAsync(nm.p, 0, sizeof(int) * tab.size(), s));
+        SSG_CUDA(cudaMemsetAsync(nr.p, 0, sizeof(int) * tab.size(), s));
+        k_cl_codes_p2p<<<div_up(T.n, 256), 256, 0, s>>>(
+            T.n, T.perm.as<int>(), T.level.as<int>(), T.prp.as<int>(), T.pci.as<int>(), T.ipos.as<int>(),
+            owner.as<unsigned char>(), ord.as<int>(), eo.as<int>(), C, S, nlev, T.cl_code.as<int>(), nm.as<int>(),
+            nr.as<int>(), inf.as<int>());
+        SSG_LAUNCHED();
+        std::vector<int> hm(tab.size()), hr(tab.size());
+        SSG_CUDA(cudaMemcpyAsync(hm.data(), nm.p, sizeof(int) * tab.size(), cudaMemcpyDeviceToHost, s));
+        SSG_CUDA(cudaMemcpyAsync(hr.data(), nr.p, sizeof(int) * tab.size(), cudaMemcpyDeviceToHost, s));
+        SSG_CUDA(cudaStreamSynchronize(s));
+        for (int l = 0; l < nlev; ++l)
+            for (int c = 0; c < C; ++c) {
+                const size_t q = (size_t)l * C + c;
+                if (!hm[q]) continue;
+                const int delta = std::min(l - hr[q], 0x7FFF);  // >= 0: a dependency is an earlier level
+                tab[q].y |= hm[q] << 16;
+                tab[q].w |= delta << 16;
+            }
+    } else {
+        k_cl_codes<<<div_up(T.n, 256), 256, 0, s>>>(T.n, T.perm.as<int>(), T.level.as<int>(), T.prp.as<int>(),
+                                                    T.pci.as<int>(), T.ipos.as<int>(), owner.as<unsigned char>(),
+                                                    ord.as<int>(), eo.as<int>(), C, S, CL_STORE_K,
+                                                    T.cl_code.as<int>(), inf.as<int>());
+        SSG_LAUNCHED();
+    }
+    T.cl_tab.ensure(sizeof(int4) * tab.size());
+    SSG_CUDA(cudaMemcpyAsync(T.cl_tab.p, tab.data(), sizeof(int4) * tab.size(), cudaMemcpyHostToDevice, s));
     int infeasible = 0;
     SSG_CUDA(cudaMemcpyAsync(&infeasible, inf.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     SSG_CUDA(cudaStreamSynchronize(s));
     if (infeasible) return;
+    T.cl_p2p = p2p;
     T.cl_C = C;
     T.cl_S = S;
     T.cl_elem = elem;
@@ -552,9 +695,9 @@ void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBu
     T.cl_ready = true;
 }
 
-template <typename T, int G>
+template <typename T, int G, bool P2P>
 static void launch_cluster(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *lvec, T *out,
-                           T *out2, const KState *st, cudaStream_t s) {
+                           T *out2, const KState *st, int *err, cudaStream_t s) {
     const int elem = (int)sizeof(T);
     const ClLayout lay = cl_layout(tri.cl_S, tri.cl_cap_r, tri.cl_cap_e, elem, mode == SW_FWD_EIS ? 1 : 0,
                                    mode == SW_FWD_EIS ? 2 : 1, tri.nlev);
@@ -578,7 +721,7 @@ static void launch_cluster(const Tri &tri, const T *val, int mode, const T *rhs,
               *cd = tri.cl_code.as<int>();
 #define SSG_CL(M)                                                                                                \
     do {                                                                                                         \
-        auto kern = k_sweep_cluster<T, G, M>;                                                                    \
+        auto kern = k_sweep_cluster<T, G, M, P2P>;                                                               \
         static bool prepared = false;                                                                            \
         if (!prepared) {                                                                                         \
             if (tri.cl_C > 8)                                                                                    \
@@ -587,36 +730,53 @@ static void launch_cluster(const Tri &tri, const T *val, int mode, const T *rhs,
             prepared = true;                                                                                     \
         }                                                                                                        \
         SSG_CUDA(cudaLaunchKernelEx(&cfg, kern, tri.nlev, ncomp, lp, pm, pr, cd, val, lvec, rhs, aux, out, out2, \
-                                    st, tri.cl_tab.as<int4>(), lay));                                            \
+                                    st, tri.cl_tab.as<int4>(), err, lay));                                       \
     } while (0)
-    switch (mode) {
-        case SW_FWD_DIV: SSG_CL(SW_FWD_DIV); break;
-        case SW_BWD_IC: SSG_CL(SW_BWD_IC); break;
-        case SW_BWD_DIV: SSG_CL(SW_BWD_DIV); break;
-        default: SSG_CL(SW_FWD_EIS); break;
+    if (P2P) {
+        // the neighbour-synchronised plan serves the IC sweeps
+        switch (mode) {
+            case SW_FWD_DIV: SSG_CL(SW_FWD_DIV); break;
+            case SW_BWD_IC: SSG_CL(SW_BWD_IC); break;
+            default: throw Error{SSG_ERR_STATE, "neighbour-synchronised plan used for a non-IC sweep"};
+        }
+    } else {
+        switch (mode) {
+            case SW_FWD_DIV: SSG_CL(SW_FWD_DIV); break;
+            case SW_BWD_IC: SSG_CL(SW_BWD_IC); break;
+            case SW_BWD_DIV: SSG_CL(SW_BWD_DIV); break;
+            default: SSG_CL(SW_FWD_EIS); break;
+        }
     }
 #undef SSG_CL
 }
 
 template <typename T>
 void sweep_cluster(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *lvec, T *out, T *out2,
-                   const KState *st, int group, cudaStream_t s) {
+                   const KState *st, int group, int *err, cudaStream_t s) {
     if (tri.n == 0) return;
     const int G = group ? group : sweep_group(tri);
-    if (G == 8)
-        launch_cluster<T, 8>(tri, val, mode, rhs, aux, lvec, out, out2, st, s);
+    if (tri.cl_p2p) {
+        // neighbour-synchronised kernels exist for 4 and 8 lanes a row
+        if (G == 8)
+            launch_cluster<T, 8, true>(tri, val, mode, rhs, aux, lvec, out, out2, st, err, s);
+        else if (G == 4)
+            launch_cluster<T, 4, true>(tri, val, mode, rhs, aux, lvec, out, out2, st, err, s);
+        else
+            throw Error{SSG_ERR_ARG, "the neighbour-synchronised sweep runs with 4 or 8 lanes a row"};
+    } else if (G == 8)
+        launch_cluster<T, 8, false>(tri, val, mode, rhs, aux, lvec, out, out2, st, err, s);
     else if (G == 16)
-        launch_cluster<T, 16>(tri, val, mode, rhs, aux, lvec, out, out2, st, s);
+        launch_cluster<T, 16, false>(tri, val, mode, rhs, aux, lvec, out, out2, st, err, s);
     else if (G == 32)
-        launch_cluster<T, 32>(tri, val, mode, rhs, aux, lvec, out, out2, st, s);
+        launch_cluster<T, 32, false>(tri, val, mode, rhs, aux, lvec, out, out2, st, err, s);
     else
-        launch_cluster<T, 4>(tri, val, mode, rhs, aux, lvec, out, out2, st, s);
+        launch_cluster<T, 4, false>(tri, val, mode, rhs, aux, lvec, out, out2, st, err, s);
     SSG_LAUNCHED();
 }
 
 #define SSG_INST(T)                                                                                        \
     template void sweep_cluster<T>(const Tri &, const T *, int, const T *, const T *, const T *, T *, T *, \
-                                   const KState *, int, cudaStream_t);
+                                   const KState *, int, int *, cudaStream_t);
 SSG_INST(double)
 SSG_INST(cplx)
 SSG_INST(float)

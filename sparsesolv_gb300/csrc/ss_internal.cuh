@@ -23,17 +23,31 @@ void note_launch();
 #define SSG_LAUNCHED() ::ssg::note_launch()
 
 // ---------------------------------------------------------------- device memory
-// Owning device buffer (cudaMallocAsync on the handle's stream is avoided:
-// buffers live as long as the handle, allocated once per matrix pattern).
+// Stream that device buffers are allocated and freed on (thread-local; set by
+// the C ABI entry points to the handle's stream). A plain cudaFree waits for
+// the whole device, so every handle or batch that frees a temporary would stall
+// the work of all others; stream-ordered allocation (cudaMallocAsync /
+// cudaFreeAsync on the owning stream) frees in order with that stream only.
+// Null: synchronous cudaMalloc / cudaFree.
+cudaStream_t &alloc_stream();
+struct AllocStream {
+    cudaStream_t prev;
+    explicit AllocStream(cudaStream_t s) : prev(alloc_stream()) { alloc_stream() = s; }
+    ~AllocStream() { alloc_stream() = prev; }
+};
+
+// Owning device buffer; freed on the stream it was allocated on, which
+// therefore must outlive it (Handle keeps its stream in its first member).
 struct DBuf {
     void *p = nullptr;
     size_t bytes = 0;
+    cudaStream_t s = nullptr;  // allocation stream (null: synchronous)
     DBuf() = default;
     DBuf(const DBuf &) = delete;
     DBuf &operator=(const DBuf &) = delete;
-    DBuf(DBuf &&o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+    DBuf(DBuf &&o) noexcept : p(o.p), bytes(o.bytes), s(o.s) { o.p = nullptr; o.bytes = 0; o.s = nullptr; }
     DBuf &operator=(DBuf &&o) noexcept {
-        if (this != &o) { release(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+        if (this != &o) { release(); p = o.p; bytes = o.bytes; s = o.s; o.p = nullptr; o.bytes = 0; o.s = nullptr; }
         return *this;
     }
     ~DBuf() { release(); }
@@ -58,6 +72,8 @@ struct Tri {
     DBuf lptr_d;
     // cluster sweep plan (ss_cluster.cu)
     bool cl_ready = false;
+    bool cl_p2p = false;         // neighbour-synchronised plan (IC sweeps only)
+    int cl_fail = 0;             // plans found infeasible for this pattern: bit 0 lockstep, bit 1 neighbour-synchronised
     int cl_C = 0, cl_S = 0, cl_elem = 0, cl_ring_bytes = 0, cl_cap_r = 0, cl_cap_e = 0;
     DBuf cl_code;                // per level-ordered entry: row id, or -1 - (owner << 20 | ring slot)
     DBuf cl_tab;                 // per (level, CTA): rows [rs, re) and entries [e0, e1) of the chunk
@@ -118,12 +134,14 @@ int sweep_group(const Tri &tri);  // lanes per row from the mean row length
 
 // ss_cluster.cu: one-cluster level-synchronous sweeps
 int cluster_size_available();  // 16, 8 or 0
-void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBuf &tmp);
+// p2p: neighbour-synchronised plan (no cluster barrier per level; IC sweeps only)
+void cluster_plan(Tri &T, size_t elem_bytes, int ring_bytes, cudaStream_t s, DBuf &tmp, bool p2p);
 struct KState;
-// lvec: per-row vector in this triangle's level order (1/diagonal, or D for SW_BWD_IC)
+// lvec: per-row vector in this triangle's level order (1/diagonal, or D for SW_BWD_IC);
+// err: the handle's error word (bounded waits of the neighbour-synchronised sweep)
 template <typename T>
 void sweep_cluster(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *lvec, T *out, T *out2,
-                   const KState *st, int group, cudaStream_t s);
+                   const KState *st, int group, int *err, cudaStream_t s);
 
 // ss_spmv_vec.cu -- see the Krylov state there
 struct KState;

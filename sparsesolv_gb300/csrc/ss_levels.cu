@@ -25,15 +25,27 @@ void note_launch() {
 }
 long long launch_count() { return g_launches.load(); }
 
+cudaStream_t &alloc_stream() {
+    static thread_local cudaStream_t s = nullptr;
+    return s;
+}
+
 void DBuf::release() {
-    if (p) cudaFree(p);
+    if (p) {
+        if (s)
+            cudaFreeAsync(p, s);
+        else
+            cudaFree(p);
+    }
     p = nullptr;
     bytes = 0;
+    s = nullptr;
 }
 void DBuf::alloc(size_t b) {
     release();
     if (b == 0) b = 16;
-    cudaError_t e = cudaMalloc(&p, b);
+    s = alloc_stream();
+    cudaError_t e = s ? cudaMallocAsync(&p, b, s) : cudaMalloc(&p, b);
     if (e != cudaSuccess) {
         p = nullptr;
         (void)cudaGetLastError();
@@ -366,6 +378,7 @@ void build_tri(Tri &T, int n, int nnz, const int *rp, const int *ci, const int *
     T.nnz = nnz;
     T.lower = lower;
     T.cl_ready = false;
+    T.cl_fail = 0;
     T.cl_elem = 0;
     T.level.ensure(sizeof(int) * (size_t)n);
     T.perm.ensure(sizeof(int) * (size_t)n);

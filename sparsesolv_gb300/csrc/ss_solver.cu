@@ -22,7 +22,19 @@ namespace ssg {
 
 Handle::Handle(int dev) : device(dev) {
     SSG_CUDA(cudaSetDevice(dev));
-    SSG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    SSG_CUDA(cudaStreamCreateWithFlags(&sg.s, cudaStreamNonBlocking));
+    stream = sg.s;
+    // stream-ordered allocations come from the device's default pool; keep what it
+    // holds instead of returning it at every synchronisation (a per-process setting)
+    static bool pool_set[64] = {};
+    if (dev >= 0 && dev < 64 && !pool_set[dev]) {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        pool_set[dev] = true;
+    }
     ssg_default_options(&opt);
     part.alloc(part_bytes());
     SSG_CUDA(cudaMemset(part.p, 0, part.bytes));
@@ -81,7 +93,7 @@ Handle::~Handle() {
         if (e) cudaEventDestroy(e);
     if (h_state) cudaFreeHost(h_state);
     if (h_scal) cudaFreeHost(h_scal);
-    if (stream) cudaStreamDestroy(stream);
+    // the stream itself goes with sg, after the buffers have been freed on it
 }
 
 void Handle::check_err(const char *where) {
@@ -288,16 +300,28 @@ static double tri_bytes(const Tri &T, size_t v, int vecs) {
 // mean rows per level above which the automatic mode keeps the sync-free sweep
 static constexpr double kAutoClusterRowsPerLevel = 4096.0;
 
-bool Handle::cluster_ok(Tri &t, size_t elem) {
+bool Handle::cluster_ok(Tri &t, size_t elem, bool ic) {
     if (sweep_mode == 1 || t.n == 0) return false;
     // automatic: one cluster wins while the levels are narrow enough that the
     // per-level latency, not the row count, sets the pace
     if (sweep_mode == 0 && (double)t.n > kAutoClusterRowsPerLevel * (double)t.nlev) return false;
-    if (!t.cl_ready || t.cl_elem != (int)elem || t.cl_ring_bytes != cl_ring_bytes) {
+    // the neighbour-synchronised plan (mode 3) serves IC sweeps; a triangle whose plan
+    // is infeasible under it falls back to the lockstep plan
+    const bool p2p = ic && sweep_mode == 3 && !(t.cl_fail & 2);
+    const int ring = p2p ? cl_ring_bytes_p2p : cl_ring_bytes;
+    const bool planned = t.cl_ready && t.cl_elem == (int)elem && t.cl_ring_bytes == ring && t.cl_p2p == p2p;
+    if (!planned) {
         DBuf tmp;
-        cluster_plan(t, elem, cl_ring_bytes, stream, tmp);
+        if (p2p) {
+            cluster_plan(t, elem, ring, stream, tmp, true);
+            if (!t.cl_ready) t.cl_fail |= 2;
+        }
+        if (!t.cl_ready && !(t.cl_fail & 1)) {
+            cluster_plan(t, elem, cl_ring_bytes, stream, tmp, false);
+            if (!t.cl_ready) t.cl_fail |= 1;
+        }
     }
-    return t.cl_ready;
+    return t.cl_ready && (ic || !t.cl_p2p);
 }
 
 // z = (L D L^T)^{-1} r using vec[10] as the forward result
@@ -305,14 +329,14 @@ template <typename T>
 void Handle::apply_precond(const T *d_r, T *d_z, const KState *stp) {
     T *y = vec[10].as<T>();
     const size_t v = sizeof(T);
-    if (cluster_ok(Lf, v) && cluster_ok(Ltb, v)) {
+    if (cluster_ok(Lf, v, true) && cluster_ok(Ltb, v, true)) {
         timed(PC_FWD, tri_bytes(Lf, v, 2), [&] {
             sweep_cluster<T>(Lf, Lval.as<T>(), SW_FWD_DIV, d_r, nullptr, use_inv_diag ? invL_lev.as<T>() : nullptr, y,
-                             nullptr, stp, cl_group, stream);
+                             nullptr, stp, cl_group, err(), stream);
         });
         timed(PC_BWD, tri_bytes(Ltb, v, 3), [&] {
             sweep_cluster<T>(Ltb, Ltval.as<T>(), SW_BWD_IC, nullptr, y, D_lev.as<T>(), d_z, nullptr, stp, cl_group,
-                             stream);
+                             err(), stream);
         });
         return;
     }
@@ -399,9 +423,9 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
     }
     if (sgs && n) {
         // rd = C^{-1} r (src/MatSolverMRTR_SGSver.cpp:118-132)
-        if (cluster_ok(Lf, sizeof(T))) {
+        if (cluster_ok(Lf, sizeof(T), true)) {
             sweep_cluster<T>(Lf, Cval.as<T>(), SW_FWD_DIV, r, nullptr, use_inv_diag ? invC_lev.as<T>() : nullptr, t1,
-                             nullptr, nullptr, cl_group, s);
+                             nullptr, nullptr, cl_group, err(), s);
         } else {
             fill_sentinel_st<T>(t1, n, nullptr, s);
             sweep_st<T>(Lf, Cval.as<T>(), SW_FWD_DIV, r, nullptr, nullptr, t1, nullptr, ticket(), err(), nullptr, s,
@@ -486,7 +510,7 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
     const double nv = (double)vb * n;
     const double spmv_bytes = (4.0 + vb) * nnz + 4.0 * (n + 1) + 2.0 * nv;
     int iter_no = 0;
-    const bool sgs_cluster = sgs && cluster_ok(Ub, sizeof(T)) && cluster_ok(Lf, sizeof(T));
+    const bool sgs_cluster = sgs && cluster_ok(Ub, sizeof(T), false) && cluster_ok(Lf, sizeof(T), false);
     auto one_iteration = [&]() {
         prof.iter = ++iter_no;
         prof.pre = true;
@@ -512,11 +536,11 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
             if (sgs_cluster) {
                 timed(PC_BWD, tri_bytes(Ub, vb, 2), [&] {
                     sweep_cluster<T>(Ub, Uval.as<T>(), SW_BWD_DIV, r, nullptr,
-                                     use_inv_diag ? invU_lev.as<T>() : nullptr, u, nullptr, st, cl_group, s);
+                                     use_inv_diag ? invU_lev.as<T>() : nullptr, u, nullptr, st, cl_group, err(), s);
                 });
                 timed(PC_FWD, tri_bytes(Lf, vb, 4), [&] {
                     sweep_cluster<T>(Lf, Cval.as<T>(), SW_FWD_EIS, r, u, use_inv_diag ? invC_lev.as<T>() : nullptr,
-                                     t1, w, st, cl_group, s);
+                                     t1, w, st, cl_group, err(), s);
                 });
             } else {
                 timed(PC_VEC, nv, [&] { fill_sentinel_st<T>(u, n, st, s); });

@@ -31,7 +31,20 @@ struct Prof {
     bool pre = true;
 };
 
+// Owns the handle's stream. First member of Handle, so it is destroyed last:
+// the other members' device buffers are freed in order on this stream.
+struct StreamGuard {
+    cudaStream_t s = nullptr;
+    ~StreamGuard() {
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    }
+};
+
 struct Handle {
+    StreamGuard sg;
     int device = 0;
     cudaStream_t stream = nullptr;
     ssg_options opt{};
@@ -89,10 +102,12 @@ struct Handle {
     SweepCfg swcfg;
     int fac_backoff_ns = 0;
     bool use_inv_diag = true;
-    int sweep_mode = 0;            // 0 auto (default), 1 sync-free, 2 cluster
+    int sweep_mode = 0;            // 0 auto (default), 1 sync-free, 2 cluster, 3 neighbour-synchronised cluster
     int cl_ring_bytes = 16 * 1024; // distributed shared-memory ring per CTA
+    int cl_ring_bytes_p2p = 24 * 1024;  // its ring in mode 3 (producers may run ahead)
     int cl_group = 4;              // lanes per row in the cluster sweep
-    bool cluster_ok(Tri &t, size_t elem);
+    // ic: an IC sweep (the only kind the neighbour-synchronised plan serves)
+    bool cluster_ok(Tri &t, size_t elem, bool ic);
 
     Prof prof;
     int prof_begin(int cls);

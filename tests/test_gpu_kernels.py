@@ -138,9 +138,9 @@ def test_ic_factor_real_bit_identical(handle, oracle, name, alpha):
 
 @pytest.mark.parametrize("name", ["cc8", "cfg1", "rand", "ec6"])
 def test_cluster_and_syncfree_sweeps_agree(handle, name):
-    """The one-cluster level-synchronous sweep and the sync-free sweep do the
-    same per-row arithmetic (same lanes, same order), so the preconditioner
-    results are identical."""
+    """The one-cluster sweeps (level-synchronous and neighbour-synchronised) and
+    the sync-free sweep do the same per-row arithmetic (same lanes, same order),
+    so the preconditioner results are identical."""
     rp, ci, val = CASES[name]
     handle.set_matrix(rp, ci, val)
     handle.factor(1.1)
@@ -152,10 +152,11 @@ def test_cluster_and_syncfree_sweeps_agree(handle, name):
     for g in (4, 8):
         handle.set_tuning(_capi.TUNE_SWEEP_GROUP, g)
         handle.set_tuning(_capi.TUNE_CLUSTER_GROUP, g)
-        for mode in (1, 2):
+        for mode in (1, 2, 3):
             handle.set_tuning(_capi.TUNE_SWEEP_MODE, mode)
             out[mode, g] = handle.apply_precond(r)
         assert np.array_equal(out[1, g], out[2, g])
+        assert np.array_equal(out[1, g], out[3, g])
     handle.set_tuning(_capi.TUNE_SWEEP_MODE, 0)
     handle.set_tuning(_capi.TUNE_SWEEP_GROUP, 0)
     handle.set_tuning(_capi.TUNE_CLUSTER_GROUP, 4)

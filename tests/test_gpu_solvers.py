@@ -158,7 +158,7 @@ def test_zero_rhs_and_early_exit(handle, golden_cases):
     assert ok2 and iters2 == 0 and len(log2) == 0
 
 
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [1, 2, 3])
 @pytest.mark.parametrize("key", ["cfg1/iccg", "cfg1/mrtr_ic", "cfg1/mrtr_sgs", "ec8/iccg"])
 def test_sweep_modes_solve_alike(handle, golden, golden_cases, key, mode):
     """Both sweep schedules (sync-free and one-cluster) reach the reference's
