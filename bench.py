@@ -66,7 +66,9 @@ def parse():
                     help="mixed: FP32 inner solves inside FP64 refinement on the true residual "
                          "(default: mixed for the serving stream, fp64 otherwise)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sweep-mode", type=int, default=0, choices=[0, 1, 2],
+    ap.add_argument("--autotune", action="store_true",
+                    help="time the sweep schedules on the workload first (ssg_autotune) and keep the fastest")
+    ap.add_argument("--sweep-mode", type=int, default=0, choices=[0, 1, 2, 3],
                     help="triangular sweeps: 0 automatic, 1 sync-free, 2 one-cluster level-synchronous")
     return ap.parse_args()
 
@@ -259,6 +261,7 @@ def run_ours(args):
     h.set_options(o)
     h.set_tuning(_capi.TUNE_SWEEP_MODE, args.sweep_mode)
     h.set_matrix(rp, ci, val)
+    tuned = h.autotune() if args.autotune else None
     stream = torch.cuda.ExternalStream(h.stream(), device=dev)
 
     def step_device():
@@ -340,7 +343,8 @@ def run_ours(args):
                    "precision": args.precision,
                    "iterations": iters, "parallelism": "replicas only" if ws > 1 else "single GPU",
                    "factor": "recomputed every step",
-                   "sweep_mode": ["automatic", "sync-free", "one-cluster"][args.sweep_mode], "level_schedule": "computed once per sparsity pattern",
+                   "sweep_mode": ["automatic", "sync-free", "one-cluster", "one-cluster neighbour-synchronised"][
+                       args.sweep_mode] if tuned is None else "autotuned: %s" % json.dumps(tuned), "level_schedule": "computed once per sparsity pattern",
                    "l2": "inputs larger than L2 (matrix %.0f MB)" % ((12.0 * nnz) / 1e6),
                    "true_relative_residual": true_res},
         "time_to_tolerance_s": ms_max / args.steps / 1e3,
@@ -353,7 +357,8 @@ def run_ours(args):
                      "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_kind == "measured" else "fallback 6.8 TB/s",
                      "traffic": NCU_TRAFFIC.get((args.workload, args.precision,
-                                                 "sync-free" if args.sweep_mode == 1 else "cluster", dom)),
+                                                 {1: "sync-free", 3: "neighbour"}.get(
+                                                     tuned["mode"] if tuned else args.sweep_mode, "cluster"), dom)),
                      "traffic_source": "ncu capture in profiles/ (per launch)", "algorithmic_bytes": dbytes / max(dlaunch, 1),
                      "launch_ms": dms / max(dlaunch, 1), "launches": dlaunch},
         "kernel_ms_per_step": {k: v[0] / args.steps for k, v in stats.items()},

@@ -177,6 +177,14 @@ long long ssg_launch_count(void);
 #define SSG_TUNE_CLUSTER_RING_KB 6   /* distributed shared-memory ring per CTA of the cluster sweep (KB) */
 #define SSG_TUNE_CLUSTER_GROUP 7     /* lanes per row in the cluster sweep: 4 (default), 8, 16, 32 */
 int ssg_set_tuning(ssg_handle h, int key, int value);
+/* Autotuner (build addition): times the IC preconditioner of the current matrix
+ * and factor for each candidate sweep schedule (sync-free with 4/8/16 lanes a row
+ * and 2/4/8/16/automatic CTAs per SM; one-cluster level-synchronous and
+ * neighbour-synchronised with 4/8 lanes), keeps the fastest in the handle's
+ * tuning and reports it. keep_group = 1 keeps the current lanes per row, so
+ * results stay bit-identical to an untuned run; otherwise they may change at
+ * rounding level (a row's entries are summed in another order). */
+int ssg_autotune(ssg_handle h, int keep_group, int *mode, int *group, int *cta_per_sm, double *ms);
 
 /* ---- hot-path pieces on their own (host buffers) ---- */
 /* IC(0) factor of the current matrix with shift alpha: L in the lower(A) pattern

@@ -26,7 +26,7 @@ EXPORTED = [
     "ssg_set_matrix_device", "ssg_solve", "ssg_solve_device", "ssg_get_residual_log", "ssg_get_iters",
     "ssg_get_accel_used", "ssg_get_timings", "ssg_factor", "ssg_apply_precond", "ssg_spmv", "ssg_level_schedule",
     "ssg_update_values", "ssg_update_values_device", "ssg_get_stream", "ssg_set_profiling", "ssg_get_kernel_stats",
-    "ssg_launch_count", "ssg_set_tuning", "ssg_ic_factor_noalloc", "ssg_batch_create", "ssg_batch_destroy",
+    "ssg_launch_count", "ssg_set_tuning", "ssg_autotune", "ssg_ic_factor_noalloc", "ssg_batch_create", "ssg_batch_destroy",
     "ssg_batch_last_error", "ssg_batch_add", "ssg_batch_set_rhs", "ssg_batch_clear", "ssg_batch_start", "ssg_batch_poll", "ssg_batch_wait", "ssg_batch_step", "ssg_batch_finished",
     "ssg_batch_result", "ssg_batch_residual_log", "ssg_batch_timings", "ssg_batch_stream",
     "ssg_batch_set_profiling", "ssg_batch_kernel_stats", "ssg_batch_set_precision",
@@ -83,6 +83,7 @@ def declare(lib):
         "ssg_get_kernel_stats": ([H, P, P, P, I], I),
         "ssg_launch_count": ([], ctypes.c_longlong),
         "ssg_set_tuning": ([H, I, I], I),
+        "ssg_autotune": ([H, I, pI, pI, pI, ctypes.POINTER(ctypes.c_double)], I),
         "ssg_ic_factor_noalloc": ([I, I, P, P, P, P, P, D, I, P], I),
         "ssg_batch_create": ([ctypes.POINTER(ctypes.c_void_p), I], I),
         "ssg_batch_destroy": ([H], I),
@@ -273,6 +274,15 @@ class Handle:
 
     def set_tuning(self, key, value):
         self._check(self.lib.ssg_set_tuning(self.h, int(key), int(value)), "ssg_set_tuning")
+
+    def autotune(self, keep_group=False):
+        """Time the candidate sweep schedules on the current matrix, keep the fastest;
+        returns {"mode", "group", "cta_per_sm", "ms"} (ms: one preconditioner application)."""
+        m, g, c = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        ms = ctypes.c_double(0.0)
+        self._check(self.lib.ssg_autotune(self.h, 1 if keep_group else 0, ctypes.byref(m), ctypes.byref(g),
+                                          ctypes.byref(c), ctypes.byref(ms)), "ssg_autotune")
+        return {"mode": m.value, "group": g.value, "cta_per_sm": c.value, "ms": ms.value}
 
     def launch_count(self):
         return int(self.lib.ssg_launch_count())

@@ -253,6 +253,18 @@ int ssg_get_kernel_stats(ssg_handle hd, double *ms, long long *launches, double 
 
 long long ssg_launch_count(void) { return ssg::launch_count(); }
 
+int ssg_autotune(ssg_handle hd, int keep_group, int *mode, int *group, int *cta_per_sm, double *ms) {
+    return guarded(hd, [&](Handle &h) {
+        const Handle::TuneChoice c =
+            h.vtype == SSG_COMPLEX ? h.autotune<cplx>(keep_group != 0) : h.autotune<double>(keep_group != 0);
+        if (mode) *mode = c.mode;
+        if (group) *group = c.group;
+        if (cta_per_sm) *cta_per_sm = c.cta_per_sm;
+        if (ms) *ms = c.ms;
+        return SSG_OK;
+    });
+}
+
 int ssg_set_tuning(ssg_handle hd, int key, int value) {
     return guarded(hd, [&](Handle &h) {
         switch (key) {

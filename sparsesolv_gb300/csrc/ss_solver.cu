@@ -593,6 +593,78 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
     return converged ? SSG_OK : SSG_NOT_CONVERGED;
 }
 
+// Candidates differ only in schedule (which threads do which rows, and how they
+// wait): the sweep mode, the CTAs per SM of the sync-free sweep and, unless
+// keep_group, the lanes per row (a different lane count sums a row's entries in
+// a different order, so results change at rounding level). Each candidate is
+// run once to build its plans, then timed over three applications (median).
+template <typename T>
+Handle::TuneChoice Handle::autotune(bool keep_group) {
+    if (vtype < 0) throw Error{SSG_ERR_STATE, "no matrix set"};
+    if (n == 0) return TuneChoice{sweep_mode, swcfg.group, swcfg.cta_per_sm, 0.0};
+    ensure_factor<T>(opt.accel_factor, opt.is_diag_scale != 0);
+    ensure_work(sizeof(T));
+    T *r = vec[1].as<T>(), *z = vec[3].as<T>();
+    {
+        std::vector<T> ones((size_t)n, Sc<T>::one());
+        SSG_CUDA(cudaMemcpyAsync(r, ones.data(), sizeof(T) * (size_t)n, cudaMemcpyHostToDevice, stream));
+        SSG_CUDA(cudaStreamSynchronize(stream));
+    }
+    const int g0 = cl_group;
+    std::vector<TuneChoice> cand;
+    const std::vector<int> groups = keep_group ? std::vector<int>{g0} : std::vector<int>{4, 8, 16};
+    for (int g : groups)
+        for (int cps : {0, 2, 4, 8, 16}) cand.push_back({1, g, cps, 0.0});
+    for (int g : groups)
+        if (g == 4 || g == 8) {
+            cand.push_back({2, g, 0, 0.0});
+            cand.push_back({3, g, 0, 0.0});
+        }
+    const TuneChoice before{sweep_mode, swcfg.group, swcfg.cta_per_sm, 0.0};
+    const int cl_before = cl_group;
+    const bool prof_on = prof.on;
+    prof.on = false;
+    TuneChoice best{-1, 0, 0, 1e300};
+    for (TuneChoice &c : cand) {
+        sweep_mode = c.mode;
+        swcfg.group = c.group;
+        cl_group = c.group;
+        swcfg.cta_per_sm = c.cta_per_sm;
+        // a cluster candidate whose plan does not fit would time the sync-free sweep again
+        if (c.mode >= 2 && !(cluster_ok(Lf, sizeof(T), true) && cluster_ok(Ltb, sizeof(T), true))) continue;
+        if (c.mode == 3 && !(Lf.cl_p2p && Ltb.cl_p2p)) continue;
+        apply_precond<T>(r, z, nullptr);
+        check_err("autotune");
+        float t[3];
+        for (float &ti : t) {
+            SSG_CUDA(cudaEventRecord(ev[0], stream));
+            apply_precond<T>(r, z, nullptr);
+            SSG_CUDA(cudaEventRecord(ev[1], stream));
+            SSG_CUDA(cudaEventSynchronize(ev[1]));
+            SSG_CUDA(cudaEventElapsedTime(&ti, ev[0], ev[1]));
+        }
+        check_err("autotune");
+        std::sort(t, t + 3);
+        c.ms = t[1];
+        if (c.ms < best.ms) best = c;
+    }
+    prof.on = prof_on;
+    if (best.mode < 0) {
+        sweep_mode = before.mode;
+        swcfg.group = before.group;
+        swcfg.cta_per_sm = before.cta_per_sm;
+        cl_group = cl_before;
+        throw Error{SSG_ERR_STATE, "autotune: no candidate ran"};
+    }
+    sweep_mode = best.mode;
+    swcfg.group = best.group;
+    cl_group = best.group;
+    swcfg.cta_per_sm = best.cta_per_sm;
+    return best;
+}
+
+template Handle::TuneChoice Handle::autotune<double>(bool);
+template Handle::TuneChoice Handle::autotune<cplx>(bool);
 template int Handle::solve<double>(int, double, int, double, const double *, double *);
 template int Handle::solve<cplx>(int, double, int, double, const cplx *, cplx *);
 template void Handle::ensure_factor<double>(double, bool);

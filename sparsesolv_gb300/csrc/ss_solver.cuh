@@ -144,6 +144,14 @@ struct Handle {
     template <typename T>
     void apply_precond(const T *d_r, T *d_z, const KState *st);
     void ensure_work(size_t elem_bytes);
+    // schedule autotuner (ssg_autotune): times the preconditioner for each
+    // candidate sweep schedule on the current matrix and keeps the fastest
+    struct TuneChoice {
+        int mode, group, cta_per_sm;
+        double ms;
+    };
+    template <typename T>
+    TuneChoice autotune(bool keep_group);
 };
 
 }  // namespace ssg
