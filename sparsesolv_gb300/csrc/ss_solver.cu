@@ -311,7 +311,9 @@ bool Handle::cluster_ok(Tri &t, size_t elem, bool ic) {
     const int ring = p2p ? cl_ring_bytes_p2p : cl_ring_bytes;
     const bool planned = t.cl_ready && t.cl_elem == (int)elem && t.cl_ring_bytes == ring && t.cl_p2p == p2p;
     if (!planned) {
+        // a plan of the other kind (or ring) must not be reused
         DBuf tmp;
+        t.cl_ready = false;
         if (p2p) {
             cluster_plan(t, elem, ring, stream, tmp, true);
             if (!t.cl_ready) t.cl_fail |= 2;

@@ -160,3 +160,23 @@ def test_cluster_and_syncfree_sweeps_agree(handle, name):
     handle.set_tuning(_capi.TUNE_SWEEP_MODE, 0)
     handle.set_tuning(_capi.TUNE_SWEEP_GROUP, 0)
     handle.set_tuning(_capi.TUNE_CLUSTER_GROUP, 4)
+
+
+def test_switching_sweep_modes_replans(handle):
+    """Mode 3 then mode 2 on one handle: the second must run the lockstep plan
+    (the same results either way; the timing of the lockstep plan is checked
+    against a fresh handle elsewhere), and the switch must not fail."""
+    rp, ci, val = CASES["cc8"]
+    handle.set_matrix(rp, ci, val)
+    handle.factor(1.1)
+    r = np.random.default_rng(5).standard_normal(len(rp) - 1)
+    try:
+        handle.set_tuning(_capi.TUNE_SWEEP_MODE, 3)
+        z3 = handle.apply_precond(r)
+        handle.set_tuning(_capi.TUNE_SWEEP_MODE, 2)
+        z2 = handle.apply_precond(r)
+        handle.set_tuning(_capi.TUNE_SWEEP_MODE, 3)
+        z3b = handle.apply_precond(r)
+        assert np.array_equal(z3, z2) and np.array_equal(z3, z3b)
+    finally:
+        handle.set_tuning(_capi.TUNE_SWEEP_MODE, 0)
