@@ -130,6 +130,17 @@ int ssg_set_matrix(ssg_handle h, int n, int nnz, const int32_t *row_ptr, const i
 /* CSR already in device memory (copied device to device) */
 int ssg_set_matrix_device(ssg_handle h, int n, int nnz, const int32_t *d_row_ptr, const int32_t *d_col,
                           const double *d_val, int value_type);
+/* The matrix from COO triplets (row, col, value), built on the device: the
+ * counterpart of SparseBuilder::build + SparseMat(builder, to_square = true)
+ * (src/SparseBuilder.cpp:107-141, src/SparseMat.cpp:114-122) and of the COO
+ * constructor (src/SparseMat.cpp:80-104). n x n, columns ascending within a
+ * row, a (row, col) given several times summed in input order, as
+ * Eigen::setFromTriplets does; an entry outside [0, n) returns SSG_ERR_ARG.
+ * rows/cols/vals in host memory, or device memory with on_device = 1. */
+int ssg_set_matrix_coo(ssg_handle h, int n, int nnz, const int32_t *rows, const int32_t *cols, const double *vals,
+                       int value_type, int on_device);
+/* copy of the current matrix as CSR (host buffers; null pointers skip; n and nnz report the sizes) */
+int ssg_get_matrix(ssg_handle h, int32_t *row_ptr, int32_t *col, double *val, int *n, int *nnz);
 
 /*
  * One solve() call. b and x are host arrays of n values (x is in/out: the

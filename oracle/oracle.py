@@ -237,3 +237,49 @@ class Reference(_Base):
            _p(np.ascontiguousarray(val, dt)), ctypes.c_double(alpha), _p(lrp), _p(lci), _p(lval), _p(D))
         nl = lrp[n]
         return lrp, lci[:nl].copy(), lval[:nl].copy(), D
+
+    def coo_to_csr(self, rows, cols, vals):
+        """The reference's SparseMatTMPL COO constructor: (nrows, ncols, rp, ci, val)."""
+        rows = np.ascontiguousarray(rows, np.int32)
+        cols = np.ascontiguousarray(cols, np.int32)
+        cplx = np.iscomplexobj(vals)
+        dt = np.complex128 if cplx else np.float64
+        v = np.ascontiguousarray(vals, dt)
+        nnz = len(rows)
+        nr, nc = ctypes.c_int(0), ctypes.c_int(0)
+        rp = np.zeros(int(rows.max()) + 2 if nnz else 1, np.int32)
+        ci = np.zeros(max(nnz, 1), np.int32)
+        va = np.zeros(max(nnz, 1), dt)
+        fn = self.lib.ref_coo_to_csr_z if cplx else self.lib.ref_coo_to_csr_d
+        got = fn(ctypes.c_int(nnz), _p(rows), _p(cols), _p(v), ctypes.byref(nr), ctypes.byref(nc), _p(rp), _p(ci),
+                 _p(va), ctypes.c_int(len(ci)))
+        assert got >= 0
+        return nr.value, nc.value, rp[:nr.value + 1].copy(), ci[:got].copy(), va[:got].copy()
+
+
+def csr_from_coo(rows, cols, vals):
+    """Restatement of SparseMatTMPL's COO constructor (src/SparseMat.cpp:80-104,
+    which hands the triplets to Eigen's setFromTriplets): a matrix of
+    (max row + 1) x (max col + 1), columns ascending within a row, duplicate
+    (row, col) entries summed one after another in input order.
+    Returns (nrows, ncols, row_ptr, col, val)."""
+    rows = np.asarray(rows, np.int64)
+    cols = np.asarray(cols, np.int64)
+    vals = np.asarray(vals)
+    if len(rows) == 0:
+        return 0, 0, np.zeros(1, np.int32), np.zeros(0, np.int32), vals[:0].copy()
+    nrows, ncols = int(rows.max()) + 1, int(cols.max()) + 1
+    order = np.lexsort((cols, rows))  # stable: equal keys keep input order
+    key = rows[order] * ncols + cols[order]
+    head = np.ones(len(key), bool)
+    head[1:] = key[1:] != key[:-1]
+    start = np.flatnonzero(head)
+    length = np.diff(np.append(start, len(key)))
+    out = vals[order[start]].copy()
+    for k in range(1, int(length.max())):  # sequential sums, entry k of every run at once
+        m = length > k
+        out[m] = out[m] + vals[order[start[m] + k]]
+    r = rows[order[start]]
+    rp = np.zeros(nrows + 1, np.int32)
+    np.cumsum(np.bincount(r, minlength=nrows), out=rp[1:])
+    return nrows, ncols, rp, cols[order[start]].astype(np.int32), out

@@ -95,7 +95,37 @@ int factor_any(int n, const int *rp, const int *ci, const T *va, double accela, 
 }
 }  // namespace
 
+// SparseMatTMPL's COO constructor (src/SparseMat.cpp:80-104): CSR out; returns
+// the stored entry count, or its negative when cap is too small
+template <typename T>
+int coo_any(int nnz, const int *rows, const int *cols, const T *vals, int *nrows, int *ncols, int *rp, int *ci,
+            T *va, int cap) {
+    std::vector<slv_int> r(rows, rows + nnz), c(cols, cols + nnz);
+    std::vector<T> v(vals, vals + nnz);
+    SparseMatTMPL<T> M(nnz, r, c, v);
+    auto &E = M.mat();
+    E.makeCompressed();
+    *nrows = (int)E.rows();
+    *ncols = (int)E.cols();
+    const int nz = (int)E.nonZeros();
+    if (nz > cap) return -nz;
+    for (int i = 0; i <= *nrows; ++i) rp[i] = E.outerIndexPtr()[i];
+    for (int k = 0; k < nz; ++k) {
+        ci[k] = E.innerIndexPtr()[k];
+        va[k] = E.valuePtr()[k];
+    }
+    return nz;
+}
+
 extern "C" {
+int ref_coo_to_csr_d(int nnz, const int *rows, const int *cols, const double *vals, int *nrows, int *ncols, int *rp,
+                     int *ci, double *va, int cap) {
+    return coo_any<double>(nnz, rows, cols, vals, nrows, ncols, rp, ci, va, cap);
+}
+int ref_coo_to_csr_z(int nnz, const int *rows, const int *cols, const dcomplex *vals, int *nrows, int *ncols, int *rp,
+                     int *ci, dcomplex *va, int cap) {
+    return coo_any<dcomplex>(nnz, rows, cols, vals, nrows, ncols, rp, ci, va, cap);
+}
 int ref_solve_d(const Settings *o, int method, int n, const int *rp, const int *ci, const double *va,
                 const double *b, double normB, double conv, int maxit, double *x, double *log, int log_cap,
                 int *log_len) {

@@ -23,7 +23,7 @@ PREC_MIXED = 1
 
 EXPORTED = [
     "ssg_default_options", "ssg_create", "ssg_destroy", "ssg_last_error", "ssg_set_options", "ssg_set_matrix",
-    "ssg_set_matrix_device", "ssg_solve", "ssg_solve_device", "ssg_get_residual_log", "ssg_get_iters",
+    "ssg_set_matrix_device", "ssg_set_matrix_coo", "ssg_get_matrix", "ssg_solve", "ssg_solve_device", "ssg_get_residual_log", "ssg_get_iters",
     "ssg_get_accel_used", "ssg_get_timings", "ssg_factor", "ssg_apply_precond", "ssg_spmv", "ssg_level_schedule",
     "ssg_update_values", "ssg_update_values_device", "ssg_get_stream", "ssg_set_profiling", "ssg_get_kernel_stats",
     "ssg_launch_count", "ssg_set_tuning", "ssg_autotune", "ssg_ic_factor_noalloc", "ssg_batch_create", "ssg_batch_destroy",
@@ -66,6 +66,8 @@ def declare(lib):
         "ssg_set_options": ([H, ctypes.POINTER(Options)], I),
         "ssg_set_matrix": ([H, I, I, P, P, P, I], I),
         "ssg_set_matrix_device": ([H, I, I, P, P, P, I], I),
+        "ssg_set_matrix_coo": ([H, I, I, P, P, P, I, I], I),
+        "ssg_get_matrix": ([H, P, P, P, pI, pI], I),
         "ssg_solve": ([H, I, D, I, D, P, P], I),
         "ssg_solve_device": ([H, I, D, I, D, P, P], I),
         "ssg_get_residual_log": ([H, P, I, pI], I),
@@ -184,6 +186,32 @@ class Handle:
         self.n = n
         self.complex = cplx
         self._mat_key = None
+
+    def set_matrix_coo(self, n, rows, cols, vals):
+        """n x n matrix from COO triplets (host numpy), built on the device; a
+        repeated (row, col) is summed in input order."""
+        r = np.ascontiguousarray(rows, np.int32)
+        c = np.ascontiguousarray(cols, np.int32)
+        cplx = np.iscomplexobj(vals)
+        v = np.ascontiguousarray(vals, np.complex128 if cplx else np.float64)
+        assert len(r) == len(c) == len(v)
+        self._check(self.lib.ssg_set_matrix_coo(self.h, int(n), len(r), _p(r), _p(c), _p(v),
+                                                COMPLEX if cplx else REAL, 0), "ssg_set_matrix_coo")
+        self.n = int(n)
+        self.complex = cplx
+        self._mat_key = None
+
+    def get_matrix(self):
+        """(row_ptr, col, val) of the current matrix."""
+        n, nnz = ctypes.c_int(0), ctypes.c_int(0)
+        self._check(self.lib.ssg_get_matrix(self.h, None, None, None, ctypes.byref(n), ctypes.byref(nnz)),
+                    "ssg_get_matrix")
+        rp = np.zeros(n.value + 1, np.int32)
+        ci = np.zeros(max(nnz.value, 1), np.int32)
+        va = np.zeros(max(nnz.value, 1), np.complex128 if self.complex else np.float64)
+        self._check(self.lib.ssg_get_matrix(self.h, _p(rp), _p(ci), _p(va), ctypes.byref(n), ctypes.byref(nnz)),
+                    "ssg_get_matrix")
+        return rp, ci[:nnz.value], va[:nnz.value]
 
     def solve(self, method, b, x, conv=1e-8, max_ite=10000, normB=-1.0):
         """Host arrays; x is updated in place. Returns True when converged."""

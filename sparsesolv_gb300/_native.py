@@ -39,6 +39,7 @@ CUDA_SOURCES = [
     "ss_spmv_vec.cu",
     "ss_solver.cu",
     "ss_batch.cu",
+    "ss_build.cu",
     "ss_capi.cu",
 ]
 

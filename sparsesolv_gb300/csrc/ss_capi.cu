@@ -195,6 +195,33 @@ int ssg_solve(ssg_handle hd, int method, double conv_cri, int max_ite, double no
     });
 }
 
+int ssg_set_matrix_coo(ssg_handle hd, int n, int nnz, const int32_t *rows, const int32_t *cols, const double *vals,
+                       int value_type, int on_device) {
+    if (nnz > 0 && (!rows || !cols || !vals)) return SSG_ERR_ARG;
+    return guarded(hd, [&](Handle &h) {
+        h.set_matrix_coo(n, nnz, rows, cols, vals, value_type,
+                         on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
+        return SSG_OK;
+    });
+}
+
+int ssg_get_matrix(ssg_handle hd, int32_t *row_ptr, int32_t *col, double *val, int *n, int *nnz) {
+    return guarded(hd, [&](Handle &h) {
+        if (h.vtype < 0) return SSG_ERR_STATE;
+        if (n) *n = h.n;
+        if (nnz) *nnz = h.nnz;
+        if (row_ptr)
+            SSG_CUDA(cudaMemcpyAsync(row_ptr, h.A_rp.p, sizeof(int) * ((size_t)h.n + 1), cudaMemcpyDeviceToHost,
+                                     h.stream));
+        if (col && h.nnz)
+            SSG_CUDA(cudaMemcpyAsync(col, h.A_ci.p, sizeof(int) * (size_t)h.nnz, cudaMemcpyDeviceToHost, h.stream));
+        if (val && h.nnz)
+            SSG_CUDA(cudaMemcpyAsync(val, h.A_val.p, vbytes(h) * (size_t)h.nnz, cudaMemcpyDeviceToHost, h.stream));
+        SSG_CUDA(cudaStreamSynchronize(h.stream));
+        return SSG_OK;
+    });
+}
+
 int ssg_update_values(ssg_handle hd, const double *val) {
     return guarded(hd, [&](Handle &h) {
         if (h.nnz > 0 && !val) return SSG_ERR_ARG;

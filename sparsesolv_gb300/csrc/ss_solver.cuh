@@ -130,6 +130,9 @@ struct Handle {
     void set_matrix(int n_, int nnz_, const int32_t *rp, const int32_t *ci, const double *val, int vt,
                     cudaMemcpyKind kind);
     void update_values(const double *val, cudaMemcpyKind kind);
+    // the matrix from COO triplets, built on the device (ss_build.cu)
+    void set_matrix_coo(int n_, int m, const int *rows, const int *cols, const double *vals, int vt,
+                        cudaMemcpyKind kind);
     void values_changed();  // A_val was rewritten in place: keep the pattern, drop the factors
     void ensure_patterns(bool need_ltb, bool need_ub);
     void check_err(const char *where);

@@ -183,3 +183,30 @@ def test_oracle_vs_reference_warm_start(oracle, golden_cases):
         r2 = ref.solve(method, rp, ci, va, b, s, x0=x_part)
         assert r1.iters == len(r2.log) - 1
         assert np.allclose(r1.log, r2.log, rtol=REAL_LOG_RTOL, atol=1e-14 * r2.log[0])
+
+
+def _coo_case(seed, cplx):
+    rng = np.random.default_rng(seed)
+    n, m = 400, 9000
+    r = rng.integers(0, n, m)
+    c = rng.integers(0, n, m)
+    r[0], c[0] = n - 1, n - 1  # square: the largest row and column are n - 1
+    v = rng.standard_normal(m) * 10.0 ** rng.uniform(-8, 8, m)
+    if cplx:
+        v = v + 1j * rng.standard_normal(m)
+    return n, r, c, v
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_coo_restatement_matches_reference_constructor(cplx):
+    """The oracle's COO -> CSR (stable sort, duplicates summed in input order)
+    against SparseMatTMPL's COO constructor compiled from the reference."""
+    from oracle.oracle import Reference, csr_from_coo
+    if not Reference.available():
+        pytest.skip("reference build not present")
+    n, r, c, v = _coo_case(3, cplx)
+    a = Reference().coo_to_csr(r, c, v)
+    b = csr_from_coo(r, c, v)
+    assert a[0] == b[0] == n and a[1] == b[1] == n
+    for x, y in zip(a[2:], b[2:]):
+        assert np.array_equal(x, y)
