@@ -141,6 +141,16 @@ int ssg_set_matrix_coo(ssg_handle h, int n, int nnz, const int32_t *rows, const 
                        int value_type, int on_device);
 /* copy of the current matrix as CSR (host buffers; null pointers skip; n and nnz report the sizes) */
 int ssg_get_matrix(ssg_handle h, int32_t *row_ptr, int32_t *col, double *val, int *n, int *nnz);
+/* Post-processing: flux density B = curl A at the centre of every voxel of an
+ * nx x ny x nz grid of hx x hy x hz elements, from the edge unknowns A[nunk]
+ * of a solution (real, or complex for eddy-current systems); the counterpart of
+ * Element::calcB of the reference's VoxelFEM example (examples/VoxelFEM/
+ * Element.cpp:116-168). ex/ey/ez[(nx+1)(ny+1)(nz+1)]: unknown of the x/y/z edge
+ * starting at node x + (nx+1)(y + (ny+1) z), -1 where there is none (Dirichlet);
+ * B[3 * (x + nx (y + ny z)) + c]. Host buffers, or device with on_device = 1. */
+int ssg_flux_density(ssg_handle h, int nx, int ny, int nz, double hx, double hy, double hz, const int32_t *ex,
+                     const int32_t *ey, const int32_t *ez, int nunk, const void *A, int value_type, void *B,
+                     int on_device);
 
 /*
  * One solve() call. b and x are host arrays of n values (x is in/out: the

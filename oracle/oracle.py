@@ -283,3 +283,48 @@ def csr_from_coo(rows, cols, vals):
     rp = np.zeros(nrows + 1, np.int32)
     np.cumsum(np.bincount(r, minlength=nrows), out=rp[1:])
     return nrows, ncols, rp, cols[order[start]].astype(np.int32), out
+
+
+# the local edge tables of Element::calcB (examples/VoxelFEM/Element.cpp:141-143)
+_RK = (0, 0, 0, 0, 1, 1, -1, -1, 1, -1, -1, 1)
+_SK = (1, -1, -1, 1, 0, 0, 0, 0, 1, 1, -1, -1)
+_TK = (1, 1, -1, -1, 1, -1, -1, 1, 0, 0, 0, 0)
+
+
+def flux_density(nx, ny, nz, h, ex, ey, ez, A):
+    """Restatement of Element::calcB / calcRot (examples/VoxelFEM/Element.cpp:116-168)
+    at every element centre (pos_rst = 0) of a uniform voxel grid: for the 12
+    edges in the example's order, rot = sign * 1.0 / 8.0 / L_a / L_b (L = h / 2),
+    B += A_edge * rot edge by edge, edges without an unknown skipped.
+    Returns B[ne, 3], element index x + nx (y + ny z)."""
+    A = np.asarray(A)
+    L = h / 2.0
+    zz, yy, xx = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    x, y, z = xx.ravel(), yy.ravel(), zz.ravel()
+    parts = [A.real, A.imag] if np.iscomplexobj(A) else [A]
+    out = [np.zeros((x.size, 3)) for _ in parts]
+    for i in range(12):
+        r, s, t = float(_RK[i]), float(_SK[i]), float(_TK[i])
+        cx, cy, cz = x.copy(), y.copy(), z.copy()
+        if i < 4:
+            cy += s > 0
+            cz += t > 0
+            m = ex
+            rot = (0.0, t * 1.0 / 8.0 / L / L, -s * 1.0 / 8.0 / L / L)
+        elif i < 8:
+            cx += r > 0
+            cz += t > 0
+            m = ey
+            rot = (-t * 1.0 / 8.0 / L / L, 0.0, r * 1.0 / 8.0 / L / L)
+        else:
+            cx += r > 0
+            cy += s > 0
+            m = ez
+            rot = (s * 1.0 / 8.0 / L / L, -r * 1.0 / 8.0 / L / L, 0.0)
+        ids = m[cx + (nx + 1) * (cy + (ny + 1) * cz)]
+        ok = ids >= 0
+        for p, o in zip(parts, out):
+            a = p[ids[ok]]
+            for c in range(3):
+                o[ok, c] = o[ok, c] + a * rot[c]
+    return out[0] + 1j * out[1] if len(out) == 2 else out[0]

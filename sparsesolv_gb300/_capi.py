@@ -23,7 +23,7 @@ PREC_MIXED = 1
 
 EXPORTED = [
     "ssg_default_options", "ssg_create", "ssg_destroy", "ssg_last_error", "ssg_set_options", "ssg_set_matrix",
-    "ssg_set_matrix_device", "ssg_set_matrix_coo", "ssg_get_matrix", "ssg_solve", "ssg_solve_device", "ssg_get_residual_log", "ssg_get_iters",
+    "ssg_set_matrix_device", "ssg_set_matrix_coo", "ssg_get_matrix", "ssg_flux_density", "ssg_solve", "ssg_solve_device", "ssg_get_residual_log", "ssg_get_iters",
     "ssg_get_accel_used", "ssg_get_timings", "ssg_factor", "ssg_apply_precond", "ssg_spmv", "ssg_level_schedule",
     "ssg_update_values", "ssg_update_values_device", "ssg_get_stream", "ssg_set_profiling", "ssg_get_kernel_stats",
     "ssg_launch_count", "ssg_set_tuning", "ssg_autotune", "ssg_ic_factor_noalloc", "ssg_batch_create", "ssg_batch_destroy",
@@ -68,6 +68,7 @@ def declare(lib):
         "ssg_set_matrix_device": ([H, I, I, P, P, P, I], I),
         "ssg_set_matrix_coo": ([H, I, I, P, P, P, I, I], I),
         "ssg_get_matrix": ([H, P, P, P, pI, pI], I),
+        "ssg_flux_density": ([H, I, I, I, D, D, D, P, P, P, I, P, I, P, I], I),
         "ssg_solve": ([H, I, D, I, D, P, P], I),
         "ssg_solve_device": ([H, I, D, I, D, P, P], I),
         "ssg_get_residual_log": ([H, P, I, pI], I),
@@ -200,6 +201,19 @@ class Handle:
         self.n = int(n)
         self.complex = cplx
         self._mat_key = None
+
+    def flux_density(self, case, A):
+        """B = curl A at every voxel centre of a voxel case (sparsesolv_gb300.voxel),
+        shape (nz, ny, nx, 3), from the solution A of its system."""
+        ex, ey, ez = case.edge_maps()
+        cplx = np.iscomplexobj(A)
+        a = np.ascontiguousarray(A, np.complex128 if cplx else np.float64)
+        B = np.zeros(case.nx * case.ny * case.nz * 3, a.dtype)
+        h = case.h
+        self._check(self.lib.ssg_flux_density(self.h, case.nx, case.ny, case.nz, float(h), float(h), float(h),
+                                              _p(ex), _p(ey), _p(ez), len(a), _p(a), COMPLEX if cplx else REAL,
+                                              _p(B), 0), "ssg_flux_density")
+        return B.reshape(case.nz, case.ny, case.nx, 3)
 
     def get_matrix(self):
         """(row_ptr, col, val) of the current matrix."""

@@ -40,6 +40,7 @@ CUDA_SOURCES = [
     "ss_solver.cu",
     "ss_batch.cu",
     "ss_build.cu",
+    "ss_post.cu",
     "ss_capi.cu",
 ]
 
@@ -95,7 +96,8 @@ def build_solver(force=False, verbose=False):
     if verbose:
         for _, out in results:
             sys.stdout.write(out)
-    _run([NVCC, *ARCH_FLAGS, "-shared", "-o", SOLVER_LIB, *objs, "-lcudart"])
+    # every symbol resolved at link time: a missing definition fails the build, not the first load
+    _run([NVCC, *ARCH_FLAGS, "-shared", "-Xlinker", "--no-undefined", "-o", SOLVER_LIB, *objs, "-lcudart"])
     return SOLVER_LIB
 
 

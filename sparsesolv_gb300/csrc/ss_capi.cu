@@ -205,6 +205,16 @@ int ssg_set_matrix_coo(ssg_handle hd, int n, int nnz, const int32_t *rows, const
     });
 }
 
+int ssg_flux_density(ssg_handle hd, int nx, int ny, int nz, double hx, double hy, double hz, const int32_t *ex,
+                     const int32_t *ey, const int32_t *ez, int nunk, const void *A, int value_type, void *B,
+                     int on_device) {
+    if (!ex || !ey || !ez || !B || (nunk > 0 && !A)) return SSG_ERR_ARG;
+    return guarded(hd, [&](Handle &h) {
+        ssg::flux_density_any(h, nx, ny, nz, hx, hy, hz, ex, ey, ez, nunk, A, value_type, B, on_device != 0);
+        return SSG_OK;
+    });
+}
+
 int ssg_get_matrix(ssg_handle hd, int32_t *row_ptr, int32_t *col, double *val, int *n, int *nnz) {
     return guarded(hd, [&](Handle &h) {
         if (h.vtype < 0) return SSG_ERR_STATE;

@@ -157,4 +157,8 @@ struct Handle {
     TuneChoice autotune(bool keep_group);
 };
 
+// flux density B = curl A per voxel element (ss_post.cu)
+void flux_density_any(Handle &h, int nx, int ny, int nz, double hx, double hy, double hz, const int *ex,
+                      const int *ey, const int *ez, int nunk, const void *A, int vt, void *B, bool on_device);
+
 }  // namespace ssg

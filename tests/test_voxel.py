@@ -118,3 +118,43 @@ def test_batched_cases_sizes():
         n, _ = case.size()
         B = np.stack([case.rhs(cl) for cl in coils])
         assert B.shape == (4, n) and np.all(np.linalg.norm(B, axis=1) > 0)
+
+
+def _interior_fields(N, seed):
+    """A gradient field and the field of a uniform B0 on the edges of an N^3 case."""
+    case = voxel.curl_curl_case(N, seed=seed, iron_size=2)
+    ex, ey, ez = case.edge_maps()
+    n = int(max(ex.max(), ey.max(), ez.max())) + 1
+    h = case.h
+    P = np.arange(N + 1) * h
+    Z, Y, X = np.meshgrid(P, P, P, indexing="ij")
+    X, Y, Z = X.ravel(), Y.ravel(), Z.ravel()
+    rng = np.random.default_rng(seed)
+    # zero on the boundary, whose edges carry no unknown (n x A = 0 there)
+    on_bnd = (X == 0) | (Y == 0) | (Z == 0) | (X == P[-1]) | (Y == P[-1]) | (Z == P[-1])
+    phi = np.where(on_bnd, 0.0, rng.standard_normal(X.size))
+    B0 = np.array([0.3, -0.7, 1.1])
+    grad = np.zeros(n)
+    unif = np.zeros(n)
+    stride = {0: 1, 1: N + 1, 2: (N + 1) ** 2}
+    for d, m in enumerate((ex, ey, ez)):
+        nodes = np.flatnonzero(m >= 0)
+        grad[m[nodes]] = phi[nodes + stride[d]] - phi[nodes]
+        # A = B0 x r / 2 is linear, so its edge integral is A(midpoint) . e_d h
+        mid = np.stack([X[nodes], Y[nodes], Z[nodes]], 1)
+        mid[:, d] += h / 2
+        unif[m[nodes]] = 0.5 * np.cross(B0, mid)[:, d] * h
+    return case, ex, ey, ez, grad, unif, B0
+
+
+def test_flux_density_restatement_on_exact_fields():
+    """curl of a gradient is zero; a uniform field is reproduced in every element
+    whose 12 edges all carry unknowns (the boundary edges are Dirichlet)."""
+    from oracle.oracle import flux_density
+    N = 6
+    case, ex, ey, ez, grad, unif, B0 = _interior_fields(N, 3)
+    Bg = flux_density(N, N, N, case.h, ex, ey, ez, grad)
+    assert np.abs(Bg).max() <= 1e-9 * np.abs(grad).max() / case.h
+    Bu = flux_density(N, N, N, case.h, ex, ey, ez, unif).reshape(N, N, N, 3)
+    inner = Bu[1:-1, 1:-1, 1:-1].reshape(-1, 3)
+    assert np.allclose(inner, B0[None, :], rtol=1e-12, atol=1e-12)
