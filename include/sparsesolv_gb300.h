@@ -266,6 +266,9 @@ int ssg_batch_set_precision(ssg_batch b, int precision, double inner_tol);
 int ssg_batch_stream(ssg_batch b, void **stream);
 /* per-kernel-class event timing of the batch's solves, as ssg_set_profiling / ssg_get_kernel_stats */
 int ssg_batch_set_profiling(ssg_batch b, int enable);
+/* 1 (default): each start captures 8 iterations in a CUDA graph once and replays it
+ * for the later chunks (direct launches while profiling); 0: direct launches only */
+int ssg_batch_set_graphs(ssg_batch b, int enable);
 int ssg_batch_kernel_stats(ssg_batch b, double *ms, long long *launches, double *bytes, int capacity);
 
 /* ---- IC(0) factor that allocates nothing (no counterpart in the reference) ----

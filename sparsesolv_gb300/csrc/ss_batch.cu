@@ -514,8 +514,14 @@ Batch::Batch(int dev) : h(dev) {
     SSG_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
 }
 
+void Batch::drop_graph() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    graph_exec = nullptr;
+}
+
 Batch::~Batch() {
     cudaSetDevice(h.device);
+    drop_graph();
     if (h_st) cudaFreeHost(h_st);
     if (h_ctl) cudaFreeHost(h_ctl);
     if (h_octl) cudaFreeHost(h_octl);
@@ -702,6 +708,7 @@ void Batch::start(int method_, double alpha, double conv, int max_ite_) {
     method = method_;
     max_ite = max_ite_;
     cudaStream_t s = h.stream;
+    drop_graph();  // buffers and plans may have changed since the last start
     SSG_CUDA(cudaEventRecord(ev[0], s));
     const int n = h.n;
     // the factor is recomputed on every start, as the reference's solve() does
@@ -811,7 +818,7 @@ void Batch::queue_chunk() {
     const int todo = std::min(chunk, max_ite - queued);
     const double nv = (double)sizeof(T) * n;
     const double spmv_bytes = (4.0 + sizeof(T)) * h.nnz + 4.0 * (n + 1) + 2.0 * nv;
-    for (int c = 0; c < todo; ++c) {
+    run_iterations(todo, [&] {
         h.prof.iter = ++iter_no;
         h.prof.pre = true;
         if (method == SSG_METHOD_ICCG) {
@@ -853,7 +860,7 @@ void Batch::queue_chunk() {
                 SSG_LAUNCHED();
             });
         }
-    }
+    });
     queued += todo;
     chunk = std::min(chunk * 2, 32);
     SSG_CUDA(cudaMemcpyAsync(h_ctl, ctl(), sizeof(KState), cudaMemcpyDeviceToHost, s));
@@ -1102,7 +1109,7 @@ void Batch::queue_inner(int todo) {
     todo = std::min(todo, max_ite - queued);
     const double nv = (double)sizeof(Ti) * n;
     const double spmv_bytes = (4.0 + sizeof(Ti)) * h.nnz + 4.0 * (n + 1) + 2.0 * nv;
-    for (int c = 0; c < todo; ++c) {
+    run_iterations(todo, [&] {
         h.prof.iter = ++iter_no;
         h.prof.pre = true;
         if (method == SSG_METHOD_ICCG) {
@@ -1142,7 +1149,7 @@ void Batch::queue_inner(int todo) {
                 SSG_LAUNCHED();
             });
         }
-    }
+    });
     queued += todo;
     chunk = std::min(chunk * 2, 32);
     SSG_CUDA(cudaMemcpyAsync(h_ctl, ctl(), sizeof(KState), cudaMemcpyDeviceToHost, s));

@@ -115,6 +115,15 @@ struct Batch {
     bool poll();  // true when finished
     void wait();
     bool step();  // waits for the iterations in flight, queues more; true when finished
+    // CUDA graph of GRAPH_ITERS iterations, captured once per start and replayed for
+    // every whole group of that many iterations (not while profiling)
+    static constexpr int GRAPH_ITERS = 8;
+    bool use_graphs = true;
+    cudaGraphExec_t graph_exec = nullptr;
+    long long graph_kernels = 0;
+    void drop_graph();
+    template <typename F>
+    void run_iterations(int todo, F &&issue_one);
     bool finished(int index) const;  // every instance of system `index` ended (as of the last completed chunk)
     // instance states as of the last completed chunk (the pinned copies are refilled by the next one)
     std::vector<KState> seen_st;
@@ -129,5 +138,42 @@ struct Batch {
 // built from the handle's matrix (kept while the matrix version is unchanged)
 int solve_mixed(Handle &h, Batch *&mb, uint64_t &mver, uint64_t &mpat, int method, double conv, int max_ite,
                 const void *d_b, void *d_x);
+
+template <typename F>
+void Batch::run_iterations(int todo, F &&issue_one) {
+    cudaStream_t s = h.stream;
+    if (!use_graphs || h.prof.on || todo < GRAPH_ITERS || todo % GRAPH_ITERS != 0) {
+        for (int c = 0; c < todo; ++c) issue_one();
+        return;
+    }
+    if (!graph_exec) {
+        cudaGraph_t g = nullptr;
+        const long long l0 = launch_count();
+        SSG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        try {
+            for (int c = 0; c < GRAPH_ITERS; ++c) issue_one();
+        } catch (...) {
+            cudaStreamEndCapture(s, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        SSG_CUDA(cudaStreamEndCapture(s, &g));
+        const cudaError_t e = cudaGraphInstantiate(&graph_exec, g, 0);
+        cudaGraphDestroy(g);
+        graph_kernels = launch_count() - l0;
+        add_launches(-graph_kernels);  // captured, not run
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            graph_exec = nullptr;
+            use_graphs = false;
+            for (int c = 0; c < todo; ++c) issue_one();
+            return;
+        }
+    }
+    for (int k = 0; k < todo / GRAPH_ITERS; ++k) {
+        SSG_CUDA(cudaGraphLaunch(graph_exec, s));
+        add_launches(graph_kernels);
+    }
+}
 
 }  // namespace ssg

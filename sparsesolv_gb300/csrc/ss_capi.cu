@@ -9,9 +9,6 @@ using ssg::cplx;
 using ssg::Error;
 using ssg::Handle;
 
-namespace ssg {
-long long launch_count();
-}
 
 struct ssg_handle_s {
     Handle *h;
@@ -577,6 +574,15 @@ int ssg_batch_set_precision(ssg_batch bd, int precision, double inner_tol) {
         if (inner_tol >= 1.0) return SSG_ERR_ARG;
         b.precision = precision;
         b.inner_tol = inner_tol > 0.0 ? inner_tol : 0.0;
+        return SSG_OK;
+    });
+}
+
+int ssg_batch_set_graphs(ssg_batch bd, int enable) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        if (b.running) return SSG_ERR_STATE;
+        b.use_graphs = enable != 0;
+        b.drop_graph();
         return SSG_OK;
     });
 }

@@ -20,6 +20,8 @@ void cuda_check(cudaError_t e, const char *what);
 #define SSG_CUDA(call) ::ssg::cuda_check((call), #call)
 // after every kernel launch: count it and surface launch errors
 void note_launch();
+long long launch_count();
+void add_launches(long long k);  // kernels run from a replayed graph (negative: captured, not run)
 #define SSG_LAUNCHED() ::ssg::note_launch()
 
 // ---------------------------------------------------------------- device memory

@@ -24,6 +24,7 @@ void note_launch() {
     cuda_check(cudaGetLastError(), "kernel launch");
 }
 long long launch_count() { return g_launches.load(); }
+void add_launches(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
 cudaStream_t &alloc_stream() {
     static thread_local cudaStream_t s = nullptr;

@@ -204,3 +204,26 @@ def test_finished_system_result_while_batch_runs(gpu):
                 bt.wait()
     finally:
         bt.close()
+
+
+@pytest.mark.parametrize("precision", [_capi.PREC_FP64, _capi.PREC_MIXED])
+def test_graph_replay_equals_direct_launches(gpu, systems, precision):
+    """Chunks replayed from a captured CUDA graph give the same bits as direct launches."""
+    out = {}
+    for graphs in (True, False):
+        bt = _capi.Batch(0)
+        try:
+            bt.set_graphs(graphs)
+            bt.set_precision(precision)
+            for rp, ci, va, b in systems:
+                bt.add(rp, ci, va, b)
+            l0 = bt.lib.ssg_launch_count()
+            bt.start(_capi.METHOD_ICCG, ALPHA, conv=1e-8, max_ite=5000)
+            bt.wait()
+            out[graphs] = [bt.result(k) for k in range(len(systems))], bt.lib.ssg_launch_count() - l0
+        finally:
+            bt.close()
+    for a, b in zip(out[True][0], out[False][0]):
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    # replayed kernels are counted too: the same iterations, a similar count (no-op tail launches differ)
+    assert out[True][1] > 0.5 * out[False][1]
