@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--method", default="iccg", choices=["iccg", "sgs", "mrtr_ic"])
     ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5"])
     ap.add_argument("--requests", type=int, default=32, help="cfg5: requests per stream")
+    ap.add_argument("--slots", default="4,4", help="cfg5: slots for real ICCG, complex IC-MRTR")
+    ap.add_argument("--share", action=argparse.BooleanOptionalAction, default=True,
+                    help="cfg5: spread a burst's rows over the slots of a kind")
     ap.add_argument("--precision", default=None, choices=["fp64", "mixed"],
                     help="mixed: FP32 inner solves inside FP64 refinement on the true residual "
                          "(default: mixed for the serving stream, fp64 otherwise)")
@@ -546,7 +549,9 @@ def run_serving(args):
             worst = max(worst, float(np.linalg.norm(r.b - A @ r.x) / np.linalg.norm(r.b)))
         return worst
 
-    srv = serving.Server(be)
+    ns = [int(v) for v in args.slots.split(",")]
+    srv = serving.Server(be, serving.ServerConfig(slots={serving.KIND_REAL_ICCG: ns[0],
+                                                        serving.KIND_COMPLEX_MRTR: ns[1]}, share=args.share))
     for _ in range(max(1, args.warmup - 2)):  # warm the slots (buffers, modules)
         srv.run(fresh(0.0, 0))
     sat = srv.run(fresh(0.0, 0))
@@ -591,7 +596,7 @@ def run_serving(args):
                    "real": kinds.count(serving.KIND_REAL_ICCG), "complex": kinds.count(serving.KIND_COMPLEX_MRTR),
                    "rows": int(sum(r.n for r in base)), "tolerance": TOL, "alpha": 1.1,
                    "precision": ("real ICCG mixed, complex IC-MRTR fp64" if args.precision != "fp64" else "fp64"),
-                   "slots": {k: v for k, v in srv.cfg.slots.items()},
+                   "slots": {k: v for k, v in srv.cfg.slots.items()}, "share": args.share,
                    "worst_true_relative_residual": worst},
         "latency_ms": {"p50": st_sat["p50_ms"], "p99": st_sat["p99_ms"]},
         "rate_sweep": sweep,

@@ -118,6 +118,8 @@ class ServerConfig:
     slots: dict = field(default_factory=lambda: {KIND_REAL_ICCG: 3, KIND_COMPLEX_MRTR: 2})
     max_rows_per_batch: int = 3_000_000
     size_ratio: float = 0.0            # > 1: a batch only groups requests within this factor of its oldest one
+    share: bool = False                # a batch takes at most the waiting rows / the kind's slots (spreads the
+                                       # work of a burst over the slots, which then run side by side)
     bytes_per_nnz: float = 96.0        # device bytes a request needs per matrix entry (estimate)
     memory_reserve: int = 2 << 30      # left free for everything else
 
@@ -154,13 +156,16 @@ class Server:
         if self._need(head) > free and self.reserved > 0:
             return []  # wait for memory held by running batches
         out, rows, need = [head], head.n, self._need(head)
+        budget = self.cfg.max_rows_per_batch
+        if self.cfg.share:
+            budget = min(budget, max(head.n, sum(r.n for r in q) // max(1, self.cfg.slots[kind])))
         ratio = self.cfg.size_ratio if self.cfg.size_ratio > 1.0 else float("inf")
         lo, hi = head.n / ratio, head.n * ratio
         for r in list(q)[1:]:
             if not lo <= r.n <= hi:
                 continue
             nr = self._need(r)
-            if rows + r.n > self.cfg.max_rows_per_batch or need + nr > free:
+            if rows + r.n > budget or need + nr > free:
                 break
             out.append(r)
             rows += r.n

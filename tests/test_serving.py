@@ -119,3 +119,15 @@ def test_latency_stats_and_stream_shape():
     assert len(s) == 6 and all(s[i].arrival <= s[i + 1].arrival for i in range(5))
     assert all(1_000 // 2 <= r.n <= 3 * 3_000 for r in s)
     assert {r.kind for r in s} <= {KIND_REAL_ICCG, KIND_COMPLEX_MRTR}
+
+
+def test_share_spreads_a_burst_over_the_slots():
+    be = FakeBackend(sec_per_row=1e-6)
+    cfg = ServerConfig(slots={KIND_REAL_ICCG: 4}, max_rows_per_batch=10**9, memory_reserve=0, share=True)
+    reqs = [req(i, 0.0, 5_000) for i in range(16)]
+    out = Server(be, cfg).run(reqs)
+    assert all(r.converged for r in out)
+    # the first batch takes a quarter of the burst, not all of it
+    assert len(be.batches[0][1]) == 4
+    assert be.max_active >= 2
+    assert sorted(i for _, ids in be.batches for i in ids) == list(range(16))
