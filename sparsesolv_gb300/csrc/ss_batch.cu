@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(BT) k_bspmv(BDev B, const int *__restrict__ rp
             T acc = Sc<T>::zero();
             if (row < tr.y) {
                 const int a = rp[row], e = rp[row + 1];
-                for (int k = a + gl; k < e; k += G) acc = acc + val[k] * x[ci[k]];
+                for (int k = a + gl; k < e; k += G) acc = madd(acc, val[k], x[ci[k]]);
             }
 #pragma unroll
             for (int m = G / 2; m >= 1; m >>= 1) acc = acc + Sc<T>::shfl_xor(acc, m);

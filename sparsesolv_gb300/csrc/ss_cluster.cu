@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
                         if (k0 + u * G < oe) xx[u] = ld_rc<T>(ad[u]);
 #pragma unroll
                     for (int u = 0; u < 4; ++u)
-                        if (k0 + u * G < oe) acc = acc + vv[u] * xx[u];
+                        if (k0 + u * G < oe) acc = madd(acc, vv[u], xx[u]);
                 }
 #pragma unroll
                 for (int m = G / 2; m >= 1; m >>= 1) acc = acc + gshfl_xor(acc, m, gm);

@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep(int n, const int *__restri
                 const int c = pci[k];
                 const T v = val[k];
                 const T x = wait_value(poll + c, err, backoff_ns);
-                acc = acc + v * x;
+                acc = madd(acc, v, x);
             }
             const unsigned gm = group_mask(G);
 #pragma unroll
