@@ -17,7 +17,7 @@
 
 namespace ssg {
 
-constexpr int FAC_MAX_PER_LANE = 8;  // rows of the lower triangle up to 256 entries
+constexpr int FAC_MAX_PER_LANE = 8;  // rows of the lower triangle up to 256 entries in registers; longer ones in memory
 
 template <typename T>
 __device__ __forceinline__ T ldcg(const T *p) {
@@ -27,6 +27,79 @@ template <>
 __device__ __forceinline__ cplx ldcg<cplx>(const cplx *p) {
     const double2 v = __ldcg((const double2 *)p);
     return {v.x, v.y};
+}
+__device__ __forceinline__ void stcg(double *p, double v) { __stcg(p, v); }
+__device__ __forceinline__ void stcg(cplx *p, cplx v) { __stcg((double2 *)p, make_double2(v.x, v.y)); }
+
+// bounded wait until row c of the factor has published its done flag
+__device__ __forceinline__ void wait_row_done(const int *done, int c, int *err) {
+    const volatile int *f = done + c;
+    if (*f != 0) return;
+    const unsigned long long start = gtimer();
+    int polls = 0;
+    while (*f == 0) {
+        if ((++polls & 63) == 0) {
+            if (*(volatile int *)err) return;
+            if (gtimer() - start > SPIN_LIMIT_NS) {
+                atomicExch(err, ERR_TIMEOUT);
+                return;
+            }
+        }
+    }
+}
+
+// A row longer than the registers of a warp hold (a dense coupling row): the
+// same recurrence on the row in place in memory. Entry jj takes the updated
+// entries left of it from memory (finished before it: written by lane 0, ordered
+// by __syncwarp), and finds the columns shared with row j by binary search in
+// the row's sorted columns. The sums over k are warp reductions, as for short rows.
+template <typename T>
+__device__ void factor_long_row(int i, int a, int m, const int *ipos, const int *prp, const int *pci, T *lval, T *D,
+                                const int *done, double alpha, int *err, int lane) {
+    for (int k = lane; k < m; k += 32) {
+        const int c = pci[a + k];
+        if (c < i) wait_row_done(done, c, err);
+    }
+    __syncwarp();
+    __threadfence();
+    if (pci[a + m - 1] != i) {  // the last entry must be the diagonal (src/SprsPreconditioner.cpp:88-94)
+        if (lane == 0) {
+            atomicExch(err, ERR_NO_DIAG);
+            D[i] = Sc<T>::one();
+        }
+        return;
+    }
+    for (int jj = 0; jj < m - 1; ++jj) {
+        const int cj = pci[a + jj];
+        const int pj = ipos[cj];
+        const int aj = prp[pj], mj = prp[pj + 1] - aj;
+        T part = Sc<T>::zero();
+        for (int l = lane; l < mj; l += 32) {
+            const int cc = ldcg(pci + aj + l);
+            if (cc >= cj) continue;  // only entries left of the diagonal of row j
+            int lo = 0, hi = jj;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (pci[a + mid] < cc) lo = mid + 1;
+                else hi = mid;
+            }
+            if (lo < jj && pci[a + lo] == cc) part = part + ldcg(lval + a + lo) * ldcg(lval + aj + l) * ldcg(D + cc);
+        }
+        part = warp_sum(part);
+        if (lane == 0) stcg(lval + a + jj, ldcg(lval + a + jj) - part);
+        __syncwarp();
+    }
+    T sq = Sc<T>::zero();
+    for (int q = lane; q < m - 1; q += 32) {
+        const T v = ldcg(lval + a + q);
+        sq = sq + v * v * ldcg(D + pci[a + q]);
+    }
+    sq = warp_sum(sq);
+    if (lane == 0) {
+        const T s = ldcg(lval + a + m - 1) * Sc<T>::from(alpha) - sq;
+        lval[a + m - 1] = s;
+        D[i] = (Sc<T>::absv(s) < 1.0e-12) ? Sc<T>::from(1.0 / DBL_EPSILON) : Sc<T>::one() / s;
+    }
 }
 
 template <typename T>
@@ -41,8 +114,15 @@ __global__ void __launch_bounds__(256) k_ic_factor(int n, const int *perm, const
         if (t >= n) return;
         const int i = perm[t];
         const int a = prp[t], m = prp[t + 1] - a;
+        if (m > 32 * FAC_MAX_PER_LANE) {
+            factor_long_row<T>(i, a, m, ipos, prp, pci, lval, D, done, alpha, err, lane);
+            __syncwarp();
+            __threadfence();
+            if (lane == 0) *(volatile int *)(done + i) = 1;
+            continue;
+        }
         int bad = 0;
-        if (m > 32 * FAC_MAX_PER_LANE || m < 1) bad = 1;
+        if (m < 1) bad = 1;
         int c[FAC_MAX_PER_LANE];
         T v[FAC_MAX_PER_LANE], dk[FAC_MAX_PER_LANE];
         // load the row and wait for every row it depends on (all j < i)

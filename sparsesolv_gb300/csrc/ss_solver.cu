@@ -106,7 +106,7 @@ void Handle::check_err(const char *where) {
     if (herr == ERR_TIMEOUT) throw Error{SSG_ERR_TIMEOUT, std::string(where) + ": a bounded device wait timed out"};
     if (herr == ERR_NO_DIAG) throw Error{SSG_ERR_NO_DIAGONAL, "there is not diagonal element!"};
     if (herr == ERR_ROW_TOO_LONG)
-        throw Error{SSG_ERR_ARG, std::string(where) + ": a row of the lower triangle has more than 256 entries"};
+        throw Error{SSG_ERR_ARG, std::string(where) + ": a row of the lower triangle is longer than the kernel takes"};
     throw Error{SSG_ERR_STATE, std::string(where) + ": device error " + std::to_string(herr)};
 }
 
