@@ -61,6 +61,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--method", default="iccg", choices=["iccg", "sgs", "mrtr_ic"])
     ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5"])
+    ap.add_argument("--rhs", type=int, default=1,
+                    help="cfg2/cfg3: right-hand sides per step, solved in one ssg_solve_multi call "
+                         "(the first is the workload's b, the others consistent ones of the same norm)")
     ap.add_argument("--requests", type=int, default=32, help="cfg5: requests per stream")
     ap.add_argument("--slots", default="4,4", help="cfg5: slots for real ICCG, complex IC-MRTR")
     ap.add_argument("--share", action=argparse.BooleanOptionalAction, default=True,
@@ -247,14 +250,25 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     cplx = np.iscomplexobj(val)
     tdt = torch.complex128 if cplx else torch.float64
+    K = max(1, args.rhs)
+    b1 = b  # the workload's own right-hand side (the CPU baseline solves it)
+    if K > 1:
+        # further right-hand sides in the range of A (the curl-curl systems are singular), |b| each
+        rng = np.random.default_rng(2024)
+        extra = []
+        for _ in range(K - 1):
+            v = rng.standard_normal(n) + (1j * rng.standard_normal(n) if cplx else 0.0)
+            e = _spmv_host(rp, ci, val, v)
+            extra.append(e * (np.linalg.norm(b) / np.linalg.norm(e)))
+        b = np.ascontiguousarray(np.concatenate([b] + extra))
     # device-resident inputs
     val_d = torch.from_numpy(val).to(dev)
     b_d = torch.from_numpy(b).to(dev)
-    x_d = torch.zeros(n, dtype=tdt, device=dev)
+    x_d = torch.zeros(n * K, dtype=tdt, device=dev)
     # pinned host buffers for the end-to-end path
     val_h = torch.from_numpy(val).pin_memory()
     b_h = torch.from_numpy(b).pin_memory()
-    x_h = torch.zeros(n, dtype=tdt).pin_memory()
+    x_h = torch.zeros(n * K, dtype=tdt).pin_memory()
     h = _capi.Handle(local)
     o = h.default_options()
     o.accel_factor = ALPHA
@@ -267,20 +281,28 @@ def run_ours(args):
     tuned = h.autotune() if args.autotune else None
     stream = torch.cuda.ExternalStream(h.stream(), device=dev)
 
+    multi_iters = []
+
     def step_device():
         h.update_values_device(val_d.data_ptr())
-        return h.solve_device(meth, b_d.data_ptr(), x_d.data_ptr(), conv=TOL, max_ite=20000)
+        if K == 1:
+            return h.solve_device(meth, b_d.data_ptr(), x_d.data_ptr(), conv=TOL, max_ite=20000)
+        ok_m, it_m, _ = h.solve_multi_device(meth, K, b_d.data_ptr(), x_d.data_ptr(), conv=TOL, max_ite=20000)
+        multi_iters[:] = it_m.tolist()
+        return ok_m
 
     def step_host():
         h.update_values(val_h.numpy())
         xh = x_h.numpy()
         xh[:] = 0.0
-        return h.solve(meth, b_h.numpy(), xh, conv=TOL, max_ite=20000)
+        if K == 1:
+            return h.solve(meth, b_h.numpy(), xh, conv=TOL, max_ite=20000)
+        return h.solve_multi(meth, b_h.numpy().reshape(K, n), xh.reshape(K, n), conv=TOL, max_ite=20000)[0]
 
     for _ in range(args.warmup):
         ok = step_device()
     assert ok, "warm-up solve did not converge"
-    iters = h.iters()
+    iters = multi_iters[:] if K > 1 else h.iters()
 
     def barrier():
         torch.cuda.synchronize(dev)
@@ -321,12 +343,15 @@ def run_ours(args):
     f1.record(stream)
     barrier()
     ms_e2e = f0.elapsed_time(f1)
-    true_res = float(np.linalg.norm(b - _spmv_host(rp, ci, val, x_h.numpy())) / np.linalg.norm(b))
+    xs = x_h.numpy().reshape(K, n)
+    bs = b.reshape(K, n)
+    true_res = max(float(np.linalg.norm(bs[j] - _spmv_host(rp, ci, val, xs[j])) / np.linalg.norm(bs[j]))
+                   for j in range(K))
 
     from sparsesolv_gb300 import replicas
     ms_max, ms_e2e_max = replicas.max_over_ranks([ms, ms_e2e])
-    value = replicas.whole_job_rate(args.steps, ws, ms_max)
-    e2e = replicas.whole_job_rate(args.steps, ws, ms_e2e_max)
+    value = replicas.whole_job_rate(args.steps * K, ws, ms_max)
+    e2e = replicas.whole_job_rate(args.steps * K, ws, ms_e2e_max)
 
     # roofline of the dominant kernel class
     dom = max(("forward sweep", "backward sweep", "spmv"), key=lambda k: stats[k][0])
@@ -343,7 +368,7 @@ def run_ours(args):
         "dtype": ("c128" if cplx else "f64") + ("+fp32-inner" if args.precision == "mixed" else ""),
         "data": "synthetic (seeded voxel generator)",
         "config": {"workload": label, "n": n, "nnz": nnz, "method": mname, "alpha": ALPHA, "tolerance": TOL,
-                   "precision": args.precision,
+                   "precision": args.precision, "right_hand_sides": K,
                    "iterations": iters, "parallelism": "replicas only" if ws > 1 else "single GPU",
                    "factor": "recomputed every step",
                    "sweep_mode": ["automatic", "sync-free", "one-cluster", "one-cluster neighbour-synchronised"][
@@ -353,13 +378,13 @@ def run_ours(args):
         "time_to_tolerance_s": ms_max / args.steps / 1e3,
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
                        "steps": len(step_ms)},
-        "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": val.itemsize * nnz + 2 * b.itemsize * n,
-                "d2h_bytes_per_step": b.itemsize * n},
+        "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": val.itemsize * nnz + 2 * b.itemsize * n * K,
+                "d2h_bytes_per_step": b.itemsize * n * K},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_kind == "measured" else "fallback 6.8 TB/s",
-                     "traffic": NCU_TRAFFIC.get((args.workload, args.precision,
+                     "traffic": None if K > 1 else NCU_TRAFFIC.get((args.workload, args.precision,
                                                  {1: "sync-free", 3: "neighbour"}.get(
                                                      tuned["mode"] if tuned else args.sweep_mode, "cluster"), dom)),
                      "traffic_source": "ncu capture in profiles/ (per launch)", "algorithmic_bytes": dbytes / max(dlaunch, 1),
@@ -371,12 +396,13 @@ def run_ours(args):
         from oracle.oracle import Reference, build
         build()
         use_ref = Reference.available()
-        sec, ts, ti, cores = cpu_time_sample(rp, ci, val, b, args.method, pt, CPU_SAMPLE_ITERS, iters, use_ref)
+        it1 = iters if K == 1 else iters[0]
+        sec, ts, ti, cores = cpu_time_sample(rp, ci, val, b1, args.method, pt, CPU_SAMPLE_ITERS, it1, use_ref)
         line["cpu_baseline"] = {
             "value": 1.0 / sec, "unit": "solves/s", "cores": cores,
             "kind": "reference" if use_ref else "port",
             "sample": "IC(0) factorisation (%.2f s) + %d iterations (%.3f s each), scaled to %d iterations"
-                      % (ts, CPU_SAMPLE_ITERS, ti, iters)}
+                      % (ts, CPU_SAMPLE_ITERS, ti, it1)}
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()

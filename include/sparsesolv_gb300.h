@@ -27,6 +27,9 @@
  *                                src/MatSolverICCG.cpp:44-124, :348-424,
  *                                src/MatSolverMRTR_ICver.cpp:44-128, :393-476)
  *   ssg_solve_device             the same solve on device-resident b and x
+ *   ssg_solve_multi[_device]     (new) n_rhs right-hand sides in one call, the
+ *                                solve(b, x, n_rhs) of the C ABI: solve() once
+ *                                per b, sharing the factor and the launches
  *   ssg_get_residual_log         MatSolverBase::getResidualLog
  *                                (src/MatSolverBase.cpp:55-64)
  *   ssg_get_iters                (new) iteration count of the last solve
@@ -161,6 +164,25 @@ int ssg_flux_density(ssg_handle h, int nx, int ny, int nz, double hx, double hy,
 int ssg_solve(ssg_handle h, int method, double conv_cri, int max_ite, double normB, const double *b, double *x);
 int ssg_solve_device(ssg_handle h, int method, double conv_cri, int max_ite, double normB, const double *d_b,
                      double *d_x);
+/*
+ * Several right-hand sides of the handle's matrix in one call (the C ABI's
+ * solve(b, x, n_rhs); the reference solves one b per solve() call,
+ * src/MatSolverICCG.cpp:44-124, src/MatSolverMRTR_ICver.cpp:44-128). B and X hold
+ * n_rhs vectors of n values one after another (X in/out as in ssg_solve); iters and
+ * status (may be NULL) receive per right-hand side the iteration count and SSG_OK /
+ * SSG_NOT_CONVERGED. Returns SSG_OK when every right-hand side converged.
+ * With the settings of a batch (ICCG or IC-MRTR, fixed accel_factor > 0, is_init = 1,
+ * conv_normalize_type 0, no diagonal scaling, no save-best, no divergence judge) and
+ * n_rhs > 1, the right-hand sides share one factor and run in the same launches: each
+ * is solved as its own batch instance (the same method and stopping rule; numbers
+ * agree with ssg_solve to rounding). Otherwise they are solved one after another
+ * exactly as ssg_solve solves them.
+ * The residual log afterwards is that of the last right-hand side.
+ */
+int ssg_solve_multi(ssg_handle h, int method, double conv_cri, int max_ite, int n_rhs, const double *B, double *X,
+                    int *iters, int *status);
+int ssg_solve_multi_device(ssg_handle h, int method, double conv_cri, int max_ite, int n_rhs, const double *d_B,
+                           double *d_X, int *iters, int *status);
 
 /* new values for the current pattern (same n, nnz, row_ptr, col); invalidates the factor */
 int ssg_update_values(ssg_handle h, const double *val);

@@ -23,7 +23,7 @@ PREC_MIXED = 1
 
 EXPORTED = [
     "ssg_default_options", "ssg_create", "ssg_destroy", "ssg_last_error", "ssg_set_options", "ssg_set_matrix",
-    "ssg_set_matrix_device", "ssg_set_matrix_coo", "ssg_get_matrix", "ssg_flux_density", "ssg_solve", "ssg_solve_device", "ssg_get_residual_log", "ssg_get_iters",
+    "ssg_set_matrix_device", "ssg_set_matrix_coo", "ssg_get_matrix", "ssg_flux_density", "ssg_solve", "ssg_solve_device", "ssg_solve_multi", "ssg_solve_multi_device", "ssg_get_residual_log", "ssg_get_iters",
     "ssg_get_accel_used", "ssg_get_timings", "ssg_factor", "ssg_apply_precond", "ssg_spmv", "ssg_level_schedule",
     "ssg_update_values", "ssg_update_values_device", "ssg_get_stream", "ssg_set_profiling", "ssg_get_kernel_stats",
     "ssg_launch_count", "ssg_set_tuning", "ssg_autotune", "ssg_ic_factor_noalloc", "ssg_batch_create", "ssg_batch_destroy",
@@ -71,6 +71,8 @@ def declare(lib):
         "ssg_flux_density": ([H, I, I, I, D, D, D, P, P, P, I, P, I, P, I], I),
         "ssg_solve": ([H, I, D, I, D, P, P], I),
         "ssg_solve_device": ([H, I, D, I, D, P, P], I),
+        "ssg_solve_multi": ([H, I, D, I, I, P, P, P, P], I),
+        "ssg_solve_multi_device": ([H, I, D, I, I, P, P, P, P], I),
         "ssg_get_residual_log": ([H, P, I, pI], I),
         "ssg_get_iters": ([H, pI], I),
         "ssg_get_accel_used": ([H, ctypes.POINTER(ctypes.c_double)], I),
@@ -235,6 +237,29 @@ class Handle:
         rc = self._check(self.lib.ssg_solve(self.h, method, float(conv), int(max_ite), float(normB), _p(b), _p(x)),
                          "ssg_solve")
         return rc == SSG_OK
+
+    def solve_multi(self, method, B, X, conv=1e-8, max_ite=10000):
+        """B, X: host arrays (n_rhs, n); X is updated in place. Returns
+        (all converged, iterations per right-hand side, status per right-hand side)."""
+        dt = np.complex128 if self.complex else np.float64
+        assert B.dtype == dt and X.dtype == dt and B.flags.c_contiguous and X.flags.c_contiguous
+        assert B.ndim == 2 and B.shape == X.shape
+        k = B.shape[0]
+        it = np.zeros(k, np.int32)
+        st = np.zeros(k, np.int32)
+        rc = self._check(self.lib.ssg_solve_multi(self.h, method, float(conv), int(max_ite), k, _p(B), _p(X), _p(it),
+                                                  _p(st)), "ssg_solve_multi")
+        return rc == SSG_OK, it, st
+
+    def solve_multi_device(self, method, nrhs, B_ptr, X_ptr, conv=1e-8, max_ite=10000):
+        """Device pointers to nrhs vectors of n values each; returns
+        (all converged, iterations per right-hand side, status per right-hand side)."""
+        it = np.zeros(nrhs, np.int32)
+        st = np.zeros(nrhs, np.int32)
+        rc = self._check(self.lib.ssg_solve_multi_device(self.h, method, float(conv), int(max_ite), int(nrhs),
+                                                         ctypes.c_void_p(B_ptr), ctypes.c_void_p(X_ptr), _p(it),
+                                                         _p(st)), "ssg_solve_multi_device")
+        return rc == SSG_OK, it, st
 
     def solve_device(self, method, b_ptr, x_ptr, conv=1e-8, max_ite=10000, normB=-1.0):
         rc = self._check(self.lib.ssg_solve_device(self.h, method, float(conv), int(max_ite), float(normB),

@@ -1184,16 +1184,20 @@ void Batch::queue_outer_step() {
     inner_setup<Ti>();
 }
 
-int solve_mixed(Handle &h, Batch *&mb, uint64_t &mver, uint64_t &mpat, int method, double conv, int max_ite,
-                const void *d_b, void *d_x) {
+bool batch_takes(const ssg_options &o, int method) {
+    return !o.is_diag_scale && !(method == SSG_METHOD_MRTR && o.precondition_type != 0) && o.accel_factor > 0.0 &&
+           o.is_init && o.conv_normalize_type == 0;
+}
+
+int solve_batched(Handle &h, Batch *&mb, uint64_t &mver, uint64_t &mpat, int precision, int method, double conv,
+                  int max_ite, int nrhs, const void *d_B, void *d_X, int *iters, int *status) {
     const ssg_options &o = h.opt;
-    if (o.is_diag_scale || (method == SSG_METHOD_MRTR && o.precondition_type != 0) || !(o.accel_factor > 0.0) ||
-        !o.is_init || o.conv_normalize_type != 0)
-        throw Error{SSG_ERR_ARG,
-                    "mixed precision solves ICCG or IC-MRTR with a fixed accel_factor > 0, x0 = 0, the |b| "
-                    "normaliser and no diagonal scaling"};
     if (h.vtype < 0) throw Error{SSG_ERR_STATE, "no matrix set"};
-    if (h.n == 0) {
+    if (h.n == 0 || nrhs == 0) {
+        for (int j = 0; j < nrhs; ++j) {
+            if (iters) iters[j] = 0;
+            if (status) status[j] = SSG_OK;
+        }
         h.iters = 0;
         h.residual_log.clear();
         return SSG_OK;
@@ -1202,48 +1206,62 @@ int solve_mixed(Handle &h, Batch *&mb, uint64_t &mver, uint64_t &mpat, int metho
     mb->h.prof.on = h.prof.on;  // profiling follows the owning handle
     AllocStream as(mb->h.stream);  // the batch's buffers are ordered on its own stream
     const int w = h.vtype == SSG_COMPLEX ? 2 : 1;
-    if (mver != h.version && mpat == h.pattern_id && mb->assembled && !mb->sys.empty() && mb->vtype == h.vtype) {
+    const bool same_rhs = !mb->sys.empty() && mb->sys[0].nrhs == nrhs;
+    if (mver != h.version && mpat == h.pattern_id && mb->assembled && same_rhs && mb->vtype == h.vtype) {
         // values-only update: the batch keeps its pattern analysis
         SSG_CUDA(cudaStreamSynchronize(h.stream));
         mb->update_values_device(0, h.A_val.p);
         mver = h.version;
     }
-    if (mver != h.version || mb->sys.empty()) {
+    if (mver != h.version || !same_rhs) {
         // the handle's matrix, through the host once per matrix version
         std::vector<int> rp((size_t)h.n + 1), ci((size_t)h.nnz);
-        std::vector<double> val((size_t)w * h.nnz), B((size_t)w * h.n, 0.0);
+        std::vector<double> val((size_t)w * h.nnz), B((size_t)w * h.n * nrhs, 0.0);
         SSG_CUDA(cudaMemcpyAsync(rp.data(), h.A_rp.p, sizeof(int) * rp.size(), cudaMemcpyDeviceToHost, h.stream));
         SSG_CUDA(cudaMemcpyAsync(ci.data(), h.A_ci.p, sizeof(int) * ci.size(), cudaMemcpyDeviceToHost, h.stream));
         SSG_CUDA(cudaMemcpyAsync(val.data(), h.A_val.p, sizeof(double) * val.size(), cudaMemcpyDeviceToHost, h.stream));
         SSG_CUDA(cudaStreamSynchronize(h.stream));
         mb->clear();
-        mb->add(h.n, h.nnz, rp.data(), ci.data(), val.data(), h.vtype, 1, B.data());
+        mb->add(h.n, h.nnz, rp.data(), ci.data(), val.data(), h.vtype, nrhs, B.data());
         mver = h.version;
         mpat = h.pattern_id;
     }
-    SSG_CUDA(cudaStreamSynchronize(h.stream));  // d_b may come from work queued on the handle's stream
-    mb->precision = SSG_PREC_MIXED;
-    mb->set_rhs_device(0, d_b);
+    SSG_CUDA(cudaStreamSynchronize(h.stream));  // d_B may come from work queued on the handle's stream
+    mb->precision = precision;
+    mb->set_rhs_device(0, d_B);
     if (h.vtype == SSG_COMPLEX)
         mb->start<cplx>(method, o.accel_factor, conv, max_ite);
     else
         mb->start<double>(method, o.accel_factor, conv, max_ite);
     mb->wait();
-    mb->result_device(0, d_x);
-    int it = 0, stt = 0;
-    const int rc = mb->result(0, nullptr, &it, &stt);
-    h.iters = it;
+    mb->result_device(0, d_X);
+    std::vector<int> it((size_t)nrhs, 0), stt((size_t)nrhs, 0);
+    const int rc = mb->result(0, nullptr, it.data(), stt.data());
+    for (int j = 0; j < nrhs; ++j) {
+        if (iters) iters[j] = it[j];
+        if (status) status[j] = stt[j] == ST_CONVERGED ? SSG_OK : SSG_NOT_CONVERGED;
+    }
+    h.iters = it[nrhs - 1];
     h.alpha_used = o.accel_factor;
     h.residual_log.clear();
     if (o.is_save_residual_log) {
         int len = 0;
-        mb->residual_log(0, 0, nullptr, 0, &len);
+        mb->residual_log(0, nrhs - 1, nullptr, 0, &len);
         h.residual_log.resize((size_t)len);
-        if (len) mb->residual_log(0, 0, h.residual_log.data(), len, &len);
+        if (len) mb->residual_log(0, nrhs - 1, h.residual_log.data(), len, &len);
     }
     h.t_setup_ms = mb->t_ms.size() > 0 ? mb->t_ms[0] : 0.0;
     h.t_iter_ms = mb->t_ms.size() > 1 ? mb->t_ms[1] : 0.0;
     return rc;
+}
+
+int solve_mixed(Handle &h, Batch *&mb, uint64_t &mver, uint64_t &mpat, int method, double conv, int max_ite,
+                const void *d_b, void *d_x) {
+    if (!batch_takes(h.opt, method))
+        throw Error{SSG_ERR_ARG,
+                    "mixed precision solves ICCG or IC-MRTR with a fixed accel_factor > 0, x0 = 0, the |b| "
+                    "normaliser and no diagonal scaling"};
+    return solve_batched(h, mb, mver, mpat, SSG_PREC_MIXED, method, conv, max_ite, 1, d_b, d_x, nullptr, nullptr);
 }
 
 template void Batch::start<double>(int, double, double, int);

@@ -134,8 +134,15 @@ struct Batch {
     int instance(int index, int rhs) const;
 };
 
-// ssg_solve / ssg_solve_device with precision SSG_PREC_MIXED: a one-system batch
-// built from the handle's matrix (kept while the matrix version is unchanged)
+// settings a batch solves as the single-system path would: ICCG or IC-MRTR, a fixed
+// accel_factor > 0, x0 = 0, the |b| normaliser, no diagonal scaling
+bool batch_takes(const ssg_options &o, int method);
+// nrhs right-hand sides of the handle's matrix (d_B, d_X: nrhs vectors of n values) in a
+// one-system batch built from that matrix, kept while its version and nrhs are unchanged;
+// iters / status (nullable) per right-hand side, status SSG_OK or SSG_NOT_CONVERGED
+int solve_batched(Handle &h, Batch *&mb, uint64_t &mver, uint64_t &mpat, int precision, int method, double conv,
+                  int max_ite, int nrhs, const void *d_B, void *d_X, int *iters, int *status);
+// ssg_solve / ssg_solve_device with precision SSG_PREC_MIXED: the batch above, one right-hand side
 int solve_mixed(Handle &h, Batch *&mb, uint64_t &mver, uint64_t &mpat, int method, double conv, int max_ite,
                 const void *d_b, void *d_x);
 

@@ -13,8 +13,10 @@ using ssg::Handle;
 struct ssg_handle_s {
     Handle *h;
     ssg::DBuf io_b, io_x;
-    ssg::Batch *mixed = nullptr;  // precision SSG_PREC_MIXED: one-system batch over this handle's matrix
-    uint64_t mixed_version = ~0ull, mixed_pattern = ~0ull;
+    // one-system batch over this handle's matrix: mixed-precision solves and
+    // several right-hand sides at once (ssg_solve_multi)
+    ssg::Batch *ibatch = nullptr;
+    uint64_t ib_version = ~0ull, ib_pattern = ~0ull;
 };
 
 namespace {
@@ -109,7 +111,7 @@ int ssg_destroy(ssg_handle hd) {
     if (hd->h) cudaSetDevice(hd->h->device);
     hd->io_b.release();  // freed on the handle's stream, which lives until delete hd->h
     hd->io_x.release();
-    delete hd->mixed;
+    delete hd->ibatch;
     delete hd->h;
     delete hd;
     return SSG_OK;
@@ -161,7 +163,7 @@ int ssg_solve_device(ssg_handle hd, int method, double conv_cri, int max_ite, do
         if (rc) return rc;
         if (h.n > 0 && (!d_b || !d_x)) return SSG_ERR_ARG;
         if (h.opt.precision == SSG_PREC_MIXED)
-            return ssg::solve_mixed(h, hd->mixed, hd->mixed_version, hd->mixed_pattern, method, conv_cri, max_ite, d_b, d_x);
+            return ssg::solve_mixed(h, hd->ibatch, hd->ib_version, hd->ib_pattern, method, conv_cri, max_ite, d_b, d_x);
         if (h.vtype == SSG_COMPLEX) return h.solve<cplx>(method, conv_cri, max_ite, normB, (const cplx *)d_b, (cplx *)d_x);
         return h.solve<double>(method, conv_cri, max_ite, normB, d_b, d_x);
     });
@@ -181,12 +183,69 @@ int ssg_solve(ssg_handle hd, int method, double conv_cri, int max_ite, double no
         }
         int res;
         if (h.opt.precision == SSG_PREC_MIXED)
-            res = ssg::solve_mixed(h, hd->mixed, hd->mixed_version, hd->mixed_pattern, method, conv_cri, max_ite, hd->io_b.p, hd->io_x.p);
+            res = ssg::solve_mixed(h, hd->ibatch, hd->ib_version, hd->ib_pattern, method, conv_cri, max_ite, hd->io_b.p, hd->io_x.p);
         else if (h.vtype == SSG_COMPLEX)
             res = h.solve<cplx>(method, conv_cri, max_ite, normB, hd->io_b.as<cplx>(), hd->io_x.as<cplx>());
         else
             res = h.solve<double>(method, conv_cri, max_ite, normB, hd->io_b.as<double>(), hd->io_x.as<double>());
         if (bytes) SSG_CUDA(cudaMemcpyAsync(x, hd->io_x.p, bytes, cudaMemcpyDeviceToHost, h.stream));
+        SSG_CUDA(cudaStreamSynchronize(h.stream));
+        return res;
+    });
+}
+
+// n_rhs right-hand sides: in the internal batch when its settings allow (one factor,
+// shared launches), else one after another exactly as ssg_solve_device
+static int solve_multi(ssg_handle hd, Handle &h, int method, double conv, int max_ite, int nrhs, const void *d_B,
+                       void *d_X, int *iters, int *status) {
+    const bool batched = ssg::batch_takes(h.opt, method) && !h.opt.is_save_best && h.opt.diverge_judge_type == 0;
+    if (nrhs > 1 && h.n > 0 && batched)
+        return ssg::solve_batched(h, hd->ibatch, hd->ib_version, hd->ib_pattern, h.opt.precision, method, conv,
+                                  max_ite, nrhs, d_B, d_X, iters, status);
+    const size_t vb = vbytes(h) * (size_t)h.n;
+    int all = SSG_OK;
+    for (int k = 0; k < nrhs; ++k) {
+        const char *b = (const char *)d_B + vb * k;
+        char *x = (char *)d_X + vb * k;
+        int r;
+        if (h.opt.precision == SSG_PREC_MIXED)
+            r = ssg::solve_mixed(h, hd->ibatch, hd->ib_version, hd->ib_pattern, method, conv, max_ite, b, x);
+        else if (h.vtype == SSG_COMPLEX)
+            r = h.solve<cplx>(method, conv, max_ite, -1.0, (const cplx *)b, (cplx *)x);
+        else
+            r = h.solve<double>(method, conv, max_ite, -1.0, (const double *)b, (double *)x);
+        if (iters) iters[k] = h.iters;
+        if (status) status[k] = r;
+        if (r != SSG_OK) all = SSG_NOT_CONVERGED;
+    }
+    return all;
+}
+
+int ssg_solve_multi_device(ssg_handle hd, int method, double conv_cri, int max_ite, int n_rhs, const double *d_B,
+                           double *d_X, int *iters, int *status) {
+    return guarded(hd, [&](Handle &h) {
+        const int rc = check_solve_args(h, method, max_ite);
+        if (rc) return rc;
+        if (n_rhs < 0 || (h.n > 0 && n_rhs > 0 && (!d_B || !d_X))) return SSG_ERR_ARG;
+        return solve_multi(hd, h, method, conv_cri, max_ite, n_rhs, d_B, d_X, iters, status);
+    });
+}
+
+int ssg_solve_multi(ssg_handle hd, int method, double conv_cri, int max_ite, int n_rhs, const double *B, double *X,
+                    int *iters, int *status) {
+    return guarded(hd, [&](Handle &h) {
+        const int rc = check_solve_args(h, method, max_ite);
+        if (rc) return rc;
+        if (n_rhs < 0 || (h.n > 0 && n_rhs > 0 && (!B || !X))) return SSG_ERR_ARG;
+        const size_t bytes = vbytes(h) * (size_t)h.n * (size_t)n_rhs;
+        hd->io_b.ensure(bytes + 16);
+        hd->io_x.ensure(bytes + 16);
+        if (bytes) {
+            SSG_CUDA(cudaMemcpyAsync(hd->io_b.p, B, bytes, cudaMemcpyHostToDevice, h.stream));
+            SSG_CUDA(cudaMemcpyAsync(hd->io_x.p, X, bytes, cudaMemcpyHostToDevice, h.stream));
+        }
+        const int res = solve_multi(hd, h, method, conv_cri, max_ite, n_rhs, hd->io_b.p, hd->io_x.p, iters, status);
+        if (bytes) SSG_CUDA(cudaMemcpyAsync(X, hd->io_x.p, bytes, cudaMemcpyDeviceToHost, h.stream));
         SSG_CUDA(cudaStreamSynchronize(h.stream));
         return res;
     });
@@ -267,15 +326,16 @@ static void prof_reset(Handle &h, bool on) {
 int ssg_set_profiling(ssg_handle hd, int enable) {
     return guarded(hd, [&](Handle &h) {
         prof_reset(h, enable != 0);
-        if (hd->mixed) prof_reset(hd->mixed->h, enable != 0);
+        if (hd->ibatch) prof_reset(hd->ibatch->h, enable != 0);
         return SSG_OK;
     });
 }
 
 int ssg_get_kernel_stats(ssg_handle hd, double *ms, long long *launches, double *bytes, int cap) {
     return guarded(hd, [&](Handle &h) {
-        // a mixed-precision solve runs in the handle's internal batch: its launches count too
-        const Handle *mh = hd->mixed ? &hd->mixed->h : nullptr;
+        // mixed-precision and multi-right-hand-side solves run in the handle's internal batch:
+        // its launches count too
+        const Handle *mh = hd->ibatch ? &hd->ibatch->h : nullptr;
         for (int c = 0; c < ssg::PC_N && c < cap; ++c) {
             if (ms) ms[c] = h.prof.ms[c] + (mh ? mh->prof.ms[c] : 0.0);
             if (launches) launches[c] = h.prof.launches[c] + (mh ? mh->prof.launches[c] : 0);
