@@ -645,6 +645,16 @@ void Batch::assemble() {
     rp[(size_t)N] = (int)e;
     NT = (int)tiles.size();
     h.set_matrix((int)N, (int)NNZ, rp.data(), ci.data(), val.data(), vtype, cudaMemcpyHostToDevice);
+    // a system's instances for its second and later right-hand sides have the same matrix
+    // as its first: their factor rows are copies of the first instance's
+    std::vector<int> rep;
+    for (int s = 0; s < S; ++s) {
+        if (inst_rhs[s] == 0) continue;
+        if (rep.empty()) rep.assign((size_t)N, -1);
+        const int src0 = inst_row[s - inst_rhs[s]];
+        for (int i = 0; i < sys[inst_sys[s]].n; ++i) rep[(size_t)inst_row[s] + i] = src0 + i;
+    }
+    h.set_replicas(rep);
     d_tile.ensure(sizeof(int2) * (size_t)NT);
     d_tile_sys.ensure(sizeof(int) * (size_t)NT);
     d_sys_tile.ensure(sizeof(int) * (size_t)(S + 1));
@@ -1203,7 +1213,14 @@ int solve_batched(Handle &h, Batch *&mb, uint64_t &mver, uint64_t &mpat, int pre
         return SSG_OK;
     }
     if (!mb) mb = new Batch(h.device);
-    mb->h.prof.on = h.prof.on;  // profiling follows the owning handle
+    mb->h.prof.on = h.prof.on;  // profiling and the sweep schedule follow the owning handle
+    // lanes a row: several right-hand sides make the levels wide, and rows of more than 6
+    // off-diagonal entries then run faster on 16 lanes; one right-hand side keeps 8
+    int g = h.batch_group;
+    if (!g) g = (nrhs > 1 && (h.nnz - h.n) > 12ll * h.n) ? 16 : 8;
+    mb->h.swcfg.group = mb->h.cl_group = g;
+    mb->h.swcfg.cta_per_sm = h.swcfg.cta_per_sm;
+    mb->h.sweep_mode = h.sweep_mode;
     AllocStream as(mb->h.stream);  // the batch's buffers are ordered on its own stream
     const int w = h.vtype == SSG_COMPLEX ? 2 : 1;
     const bool same_rhs = !mb->sys.empty() && mb->sys[0].nrhs == nrhs;

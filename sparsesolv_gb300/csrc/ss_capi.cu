@@ -393,6 +393,10 @@ int ssg_set_tuning(ssg_handle hd, int key, int value) {
                 if (value != 4 && value != 8 && value != 16 && value != 32) return SSG_ERR_ARG;
                 h.cl_group = value;
                 break;
+            case SSG_TUNE_BATCH_GROUP:
+                if (value != 0 && value != 4 && value != 8 && value != 16) return SSG_ERR_ARG;
+                h.batch_group = value;
+                break;
             default:
                 return SSG_ERR_ARG;
         }

@@ -105,13 +105,14 @@ __device__ void factor_long_row(int i, int a, int m, const int *ipos, const int 
 template <typename T>
 __global__ void __launch_bounds__(256) k_ic_factor(int n, const int *perm, const int *ipos, const int *prp,
                                                    const int *pci, T *lval, T *D, int *done, double alpha,
-                                                   int *ticket, int *err) {
+                                                   int *ticket, int *err, const int *sub) {
     const int lane = threadIdx.x & 31;
     for (;;) {
         int t = 0;
         if (lane == 0) t = atomicAdd(ticket, 1);
         t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= n) return;
+        if (sub) t = sub[t];
         const int i = perm[t];
         const int a = prp[t], m = prp[t + 1] - a;
         if (m > 32 * FAC_MAX_PER_LANE) {
@@ -250,7 +251,7 @@ template <typename T, bool NAT = false>
 __global__ void __launch_bounds__(ff_warps<T>() * 32) k_ic_factor_fast(int n, const int *perm, const int *prp,
                                                                        const int *pci, const int2 *dep, T *lval,
                                                                        T *D, int *done, double alpha, int *ticket,
-                                                                       int *err, int backoff_ns) {
+                                                                       int *err, int backoff_ns, const int *sub) {
     constexpr int FF_WARPS = ff_warps<T>();
     __shared__ int s_c[FF_WARPS][FF_MAXROW][FF_MAXROW - 1];
     __shared__ T s_v[FF_WARPS][FF_MAXROW][FF_MAXROW - 1];
@@ -260,6 +261,7 @@ __global__ void __launch_bounds__(ff_warps<T>() * 32) k_ic_factor_fast(int n, co
         if (lane == 0) t = atomicAdd(ticket, 1);
         t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= n) return;
+        if (!NAT && sub) t = sub[t];
         const int i = NAT ? t : perm[t];
         const int a = prp[t], m = prp[t + 1] - a;
         const bool have = lane < m;
@@ -365,8 +367,10 @@ void factor_plan(const Tri &L, DBuf &dep, int &max_row, cudaStream_t s) {
 
 template <typename T>
 void ic_factor(const Tri &L, T *lval, T *D, double alpha, int *d_err, int *d_ticket, cudaStream_t s,
-               const int2 *dep, int max_row, int *done, int backoff_ns) {
+               const int2 *dep, int max_row, int *done, int backoff_ns, const int *sub, int nsub) {
     if (L.n == 0) return;
+    const int cnt = sub ? nsub : L.n;  // rows to factor (sub: their level-ordered positions, ascending)
+    if (cnt == 0) return;
     SSG_CUDA(cudaMemsetAsync(done, 0, sizeof(int) * (size_t)L.n, s));
     SSG_CUDA(cudaMemsetAsync(d_ticket, 0, sizeof(int), s));
     int dev = 0, sms = 0;
@@ -375,18 +379,67 @@ void ic_factor(const Tri &L, T *lval, T *D, double alpha, int *d_err, int *d_tic
     if (dep && max_row <= FF_MAXROW) {
         constexpr int W = ff_warps<T>();
         // wide levels (batches of many systems) keep more rows in flight
-        const double width = L.nlev > 0 ? (double)L.n / L.nlev : (double)L.n;
+        const double width = L.nlev > 0 ? (double)cnt / L.nlev : (double)cnt;
         const int per_sm = width >= 8192.0 ? 6 : factor_blocks_per_sm;
-        const int blocks = min(div_up(L.n, W), sms * per_sm);
-        k_ic_factor_fast<T><<<blocks, W * 32, 0, s>>>(L.n, L.perm.as<int>(), L.prp.as<int>(), L.pci.as<int>(), dep,
-                                                      lval, D, done, alpha, d_ticket, d_err, backoff_ns);
+        const int blocks = min(div_up(cnt, W), sms * per_sm);
+        k_ic_factor_fast<T><<<blocks, W * 32, 0, s>>>(cnt, L.perm.as<int>(), L.prp.as<int>(), L.pci.as<int>(), dep,
+                                                      lval, D, done, alpha, d_ticket, d_err, backoff_ns, sub);
     } else {
-        const int warps = min(L.n, sms * 32);
-        k_ic_factor<T><<<div_up(warps * 32, 256), 256, 0, s>>>(L.n, L.perm.as<int>(), L.ipos.as<int>(),
+        const int warps = min(cnt, sms * 32);
+        k_ic_factor<T><<<div_up(warps * 32, 256), 256, 0, s>>>(cnt, L.perm.as<int>(), L.ipos.as<int>(),
                                                                L.prp.as<int>(), L.pci.as<int>(), lval, D, done,
-                                                               alpha, d_ticket, d_err);
+                                                               alpha, d_ticket, d_err, sub);
     }
     SSG_LAUNCHED();
+}
+
+// Rows whose factor equals another row's (a system repeated in a batch, once per
+// right-hand side): copy that row's entries and pivot instead of factoring it.
+// rep_src[i] = the source row of row i, or -1; both rows have the same pattern.
+template <typename T>
+__global__ void k_copy_replica_rows(int n, const int *rep_src, const int *ipos, const int *prp, T *lval, T *D) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int src = rep_src[i];
+    if (src < 0) return;
+    const int pd = prp[ipos[i]], ps = prp[ipos[src]], m = prp[ipos[i] + 1] - pd;
+    for (int k = 0; k < m; ++k) lval[pd + k] = lval[ps + k];
+    D[i] = D[src];
+}
+
+template <typename T>
+void copy_replica_rows(const Tri &L, const int *rep_src, T *lval, T *D, cudaStream_t s) {
+    if (L.n == 0) return;
+    k_copy_replica_rows<T><<<div_up(L.n, 256), 256, 0, s>>>(L.n, rep_src, L.ipos.as<int>(), L.prp.as<int>(), lval, D);
+    SSG_LAUNCHED();
+}
+
+// level-ordered positions t of the rows without a source (rep_src[perm[t]] < 0), ascending
+__global__ void k_own_flags(int n, const int *perm, const int *rep_src, int *flag) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) flag[t] = rep_src[perm[t]] < 0 ? 1 : 0;
+}
+__global__ void k_own_scatter(int n, const int *perm, const int *rep_src, const int *pos, int *sub) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n && rep_src[perm[t]] < 0) sub[pos[t]] = t;
+}
+
+int own_rows(const Tri &L, const int *rep_src, DBuf &sub, cudaStream_t s) {
+    if (L.n == 0) return 0;
+    DBuf pos, tot, tmp;
+    pos.alloc(sizeof(int) * ((size_t)L.n + 1));
+    tot.alloc(sizeof(int));
+    k_own_flags<<<div_up(L.n, 256), 256, 0, s>>>(L.n, L.perm.as<int>(), rep_src, pos.as<int>());
+    SSG_LAUNCHED();
+    scan_exclusive(pos.as<int>(), L.n, tot.as<int>(), s, tmp);
+    int cnt = 0;
+    SSG_CUDA(cudaMemcpyAsync(&cnt, tot.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SSG_CUDA(cudaStreamSynchronize(s));
+    sub.ensure(sizeof(int) * ((size_t)cnt + 1));
+    k_own_scatter<<<div_up(L.n, 256), 256, 0, s>>>(L.n, L.perm.as<int>(), rep_src, pos.as<int>(), sub.as<int>());
+    SSG_LAUNCHED();
+    SSG_CUDA(cudaStreamSynchronize(s));
+    return cnt;
 }
 
 // ---------------------------------------------------------------- diagonal scaling
@@ -451,7 +504,8 @@ void all_pivots_positive(int n, const T *D, int *d_flag, cudaStream_t s) {
 
 #define SSG_INST(T)                                                                                      \
     template void ic_factor<T>(const Tri &, T *, T *, double, int *, int *, cudaStream_t, const int2 *, int,  \
-                               int *, int);                                                                  \
+                               int *, int, const int *, int);                                                \
+    template void copy_replica_rows<T>(const Tri &, const int *, T *, T *, cudaStream_t);                     \
     template void diag_scaling<T>(int, const int *, const int *, const T *, const T *, T *, T *,        \
                                   cudaStream_t);                                                         \
     template void dad_values<T>(int, const int *, const int *, const T *, const T *, T *, cudaStream_t); \
@@ -492,7 +546,7 @@ static cudaError_t noalloc_launch(int n, const int *lrp, const int *lci, void *l
     constexpr int W = ff_warps<T>();
     const int blocks = min(div_up(n, W), sms * factor_blocks_per_sm);
     k_ic_factor_fast<T, true><<<blocks, W * 32, 0, s>>>(n, nullptr, lrp, lci, nullptr, (T *)lval, (T *)D,
-                                                        scr + NA_HEAD, alpha, scr, scr + 1, 0);
+                                                        scr + NA_HEAD, alpha, scr, scr + 1, 0, nullptr);
     return cudaGetLastError();
 }
 

@@ -103,7 +103,12 @@ void factor_plan(const Tri &L, DBuf &dep, int &max_row, cudaStream_t s);
 // asynchronous; done[n] is scratch the caller owns
 template <typename T>
 void ic_factor(const Tri &L, T *lval, T *D, double alpha, int *d_err, int *d_ticket, cudaStream_t s,
-               const int2 *dep, int max_row, int *done, int backoff_ns);
+               const int2 *dep, int max_row, int *done, int backoff_ns, const int *sub = nullptr, int nsub = 0);
+// copy the factor rows of rows with a source row (rep_src[i] >= 0) from that row
+template <typename T>
+void copy_replica_rows(const Tri &L, const int *rep_src, T *lval, T *D, cudaStream_t s);
+// level-ordered positions of the rows without a source row, ascending, into sub; returns their count
+int own_rows(const Tri &L, const int *rep_src, DBuf &sub, cudaStream_t s);
 // natural-order factor with library-owned scratch; returns an SSG_* code
 int ic_factor_noalloc(int n, int nnz, const int *lrp, const int *lci, const void *val, void *lval, void *D,
                       double alpha, int vtype, cudaStream_t s);

@@ -163,9 +163,27 @@ void Handle::values_changed() {
     fac_valid = sgs_valid = dad_valid = false;
 }
 
+void Handle::set_replicas(const std::vector<int> &src) {
+    rep_on = false;
+    for (int v : src)
+        if (v >= 0) {
+            rep_on = true;
+            break;
+        }
+    if (rep_on) {
+        if ((int)src.size() != n) throw Error{SSG_ERR_ARG, "replica map size"};
+        rep_src.ensure(sizeof(int) * (size_t)(n + 1));
+        SSG_CUDA(cudaMemcpyAsync(rep_src.p, src.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, stream));
+        SSG_CUDA(cudaStreamSynchronize(stream));
+    }
+    fac_sub_valid = false;
+    fac_valid = false;
+}
+
 void Handle::ensure_patterns(bool need_ltb, bool need_ub) {
     DBuf tmp;
     if (pat_version != version) {
+        fac_sub_valid = false;
         triangle_pattern(n, A_rp.as<int>(), A_ci.as<int>(), true, Lnat_rp, Lnat_ci, Lnat_src, nnzL, stream, tmp);
         timed(PC_LEVELS, 0.0, [&] {
             build_tri(Lf, n, nnzL, Lnat_rp.as<int>(), Lnat_ci.as<int>(), Lnat_src.as<int>(), true, err(), stream, tmp);
@@ -224,11 +242,16 @@ void Handle::ensure_factor(double alpha, bool scaled) {
     Dvec.ensure(sizeof(T) * (size_t)(n + 1));
     invL.ensure(sizeof(T) * (size_t)(n + 1));
     done_buf.ensure(sizeof(int) * (size_t)(n + 1));
+    if (rep_on && !fac_sub_valid) {
+        fac_sub_n = own_rows(Lf, rep_src.as<int>(), fac_sub, stream);
+        fac_sub_valid = true;
+    }
     auto factor_once = [&](double a) {
         gather_values<T>(Lf.psrc.as<int>(), aval, Lval.as<T>(), nnzL, stream);
         timed(PC_FACTOR, 2.0 * (4.0 + sizeof(T)) * nnzL + (double)sizeof(T) * n, [&] {
             ic_factor<T>(Lf, Lval.as<T>(), Dvec.as<T>(), a, err(), ticket() + 2, stream, dep.as<int2>(), max_row,
-                         done_buf.as<int>(), fac_backoff_ns);
+                         done_buf.as<int>(), fac_backoff_ns, rep_on ? fac_sub.as<int>() : nullptr, fac_sub_n);
+            if (rep_on) copy_replica_rows<T>(Lf, rep_src.as<int>(), Lval.as<T>(), Dvec.as<T>(), stream);
         });
         check_err("IC factorisation");
     };

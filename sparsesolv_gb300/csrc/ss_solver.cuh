@@ -103,6 +103,15 @@ struct Handle {
     int fac_backoff_ns = 0;
     bool use_inv_diag = true;
     int sweep_mode = 0;            // 0 auto (default), 1 sync-free, 2 cluster, 3 neighbour-synchronised cluster
+    int batch_group = 0;           // lanes a row in the sweeps of the owning C handle's internal batch (0: auto)
+    // rows whose factor is a copy of another row's (a batch holds a system once per
+    // right-hand side): only the rows without a source are factored
+    DBuf rep_src;                  // [n] source row or -1
+    bool rep_on = false;
+    DBuf fac_sub;                  // level-ordered positions of the rows factored
+    int fac_sub_n = 0;
+    bool fac_sub_valid = false;
+    void set_replicas(const std::vector<int> &src);  // empty: every row is factored
     int cl_ring_bytes = 16 * 1024; // distributed shared-memory ring per CTA
     int cl_ring_bytes_p2p = 24 * 1024;  // its ring in mode 3 (producers may run ahead)
     int cl_group = 4;              // lanes per row in the cluster sweep

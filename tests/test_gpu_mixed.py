@@ -98,6 +98,7 @@ def test_single_system_solve_with_mixed_precision(gpu):
         o.is_save_residual_log = 1
         o.precision = _capi.PREC_MIXED
         h.set_options(o)
+        h.set_tuning(_capi.TUNE_BATCH_GROUP, 8)  # the lanes a row of a user batch, for the bitwise comparison
         for _ in range(2):  # the second call reuses the prepared batch
             x = np.zeros_like(b)
             assert h.solve(_capi.METHOD_ICCG, b, x, conv=TOL, max_ite=5000)

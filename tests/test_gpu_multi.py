@@ -5,7 +5,8 @@ one-system batch (one factor, shared launches). Each must then meet the solver
 parity bar against a separate ssg_solve of the same right-hand side: iteration
 count within 3% (real) / 10% (complex), x within 1e-6 relative (real), true
 residual below 1e-7 (real) / A x within 5e-8 |b| (complex). In mixed precision a
-single solve is itself a one-system batch, so the results must be the same bits.
+single solve is itself a one-system batch, so with the lanes a row pinned the
+results must be the same bits.
 With other settings the right-hand sides are solved one after another by the
 single-system path: the same bits as separate ssg_solve calls."""
 import numpy as np
@@ -84,6 +85,7 @@ def test_multi_rhs_mixed_precision_same_bits_as_single(handle, golden_cases):
     rp, ci, va, b = golden_cases["cfg1"]
     handle.set_matrix(rp, ci, va)
     set_opts(handle, precision=_capi.PREC_MIXED)
+    handle.set_tuning(_capi.TUNE_BATCH_GROUP, 8)  # one lane count for one and several right-hand sides
     try:
         B = rhs_set(rp, ci, va, b, 3)
         X = np.zeros_like(B)
@@ -93,6 +95,7 @@ def test_multi_rhs_mixed_precision_same_bits_as_single(handle, golden_cases):
             ok1, xs, its = single(handle, "iccg", B[j])
             assert ok1 and its == it[j] and np.array_equal(xs, X[j])
     finally:
+        handle.set_tuning(_capi.TUNE_BATCH_GROUP, 0)
         set_opts(handle)
 
 
