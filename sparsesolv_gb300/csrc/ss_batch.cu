@@ -668,6 +668,17 @@ void Batch::assemble() {
     SSG_CUDA(cudaMemcpyAsync(d_sys_tile.p, sys_tile.data(), sizeof(int) * (size_t)(S + 1), cudaMemcpyHostToDevice, st));
     SSG_CUDA(cudaMemcpyAsync(d_sys_row.p, inst_row.data(), sizeof(int) * (size_t)(S + 1), cudaMemcpyHostToDevice, st));
     SSG_CUDA(cudaMemsetAsync(d_ctl_counter.p, 0, sizeof(KState) + 64, st));
+    {
+        std::vector<int> row_inst((size_t)N);
+        for (int q = 0; q < S; ++q)
+            std::fill(row_inst.begin() + inst_row[q], row_inst.begin() + inst_row[q + 1], q);
+        d_row_inst.ensure(sizeof(int) * ((size_t)N + 1));
+        SSG_CUDA(cudaMemcpyAsync(d_row_inst.p, row_inst.data(), sizeof(int) * (size_t)N, cudaMemcpyHostToDevice, st));
+        SSG_CUDA(cudaStreamSynchronize(st));  // row_inst is freed at the end of this scope
+        h.swcfg.row_inst = d_row_inst.as<int>();
+        h.swcfg.act = &d_st.as<KState>()->active;
+        h.swcfg.act_stride = (int)(sizeof(KState) / sizeof(int));
+    }
     // pinned copies grow only: freeing pinned memory waits for the whole device
     if (S > h_cap) {
         if (h_st) cudaFreeHost(h_st);

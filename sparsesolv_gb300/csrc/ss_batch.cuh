@@ -65,6 +65,7 @@ struct Batch {
     bool assembled = false;
     bool rhs_dirty = true;  // right-hand sides changed since the last upload
     DBuf d_tile, d_tile_sys, d_sys_tile, d_sys_row, d_st, d_part, d_logs, d_ctl_counter;
+    DBuf d_row_inst;  // instance of every row (the sync-free sweeps skip ended instances)
     KState *h_st = nullptr;   // pinned copy of the instance states
     int h_cap = 0;            // instances the pinned copies hold
     KState *h_ctl = nullptr;  // pinned copy of the control state

@@ -134,6 +134,11 @@ struct SweepCfg {
     int cta_per_sm = 0;   // resident CTAs per SM claiming rows (0: from the mean level width)
     int group = 0;        // lanes per row: 4, 8, 16 or 32 (0: from the mean row length)
     int backoff_ns = 0;   // __nanosleep between polls of an unsolved entry
+    // batches: rows whose instance has ended are skipped (row -> instance, and the
+    // instances' active flags act[instance * act_stride]); null for one system
+    const int *row_inst = nullptr;
+    const int *act = nullptr;
+    int act_stride = 0;
 };
 template <typename T>
 void inv_diag(const Tri &tri, const T *val, T *inv, cudaStream_t s);

@@ -96,7 +96,8 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep(int n, const int *__restri
                                                       const int *__restrict__ pci, const T *__restrict__ val,
                                                       const T *rhs, const T *aux, const T *D, T *out, T *out2,
                                                       int *ticket, int *err, const KState *st, const T *dinv,
-                                                      int backoff_ns) {
+                                                      int backoff_ns, const int *row_inst, const int *act,
+                                                      int act_stride) {
     if (st && !st->active) return;
     constexpr int ROWS = SW_THREADS / G;
     __shared__ int s_base;
@@ -111,8 +112,9 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep(int n, const int *__restri
         __syncthreads();
         if (base >= n) return;
         const int t = base + g;
-        if (t < n) {
-            const int r = perm[t];
+        const int r = t < n ? perm[t] : 0;
+        // a batch skips the rows of instances that have ended (nothing of another instance reads them)
+        if (t < n && (!row_inst || act[(size_t)row_inst[r] * act_stride])) {
             const int a = prp[t], e = prp[t + 1];
             const bool fwd = (MODE == SW_FWD_DIV || MODE == SW_FWD_EIS);
             const int ob = fwd ? a : a + 1;       // off-diagonal range (empty when the row is)
@@ -154,12 +156,12 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep(int n, const int *__restri
 
 template <typename T, int G>
 static void launch_sweep(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *D, T *out,
-                         T *out2, int *ticket, int *err, const KState *st, int grid, const T *dinv, int backoff,
-                         cudaStream_t s) {
+                         T *out2, int *ticket, int *err, const KState *st, int grid, const T *dinv,
+                         const SweepCfg &cfg, cudaStream_t s) {
     const int *perm = tri.perm.as<int>(), *prp = tri.prp.as<int>(), *pci = tri.pci.as<int>();
 #define SSG_SW(M)                                                                                                 \
     k_sweep<T, G, M><<<grid, SW_THREADS, 0, s>>>(tri.n, perm, prp, pci, val, rhs, aux, D, out, out2, ticket, err, \
-                                                 st, dinv, backoff)
+                                                 st, dinv, cfg.backoff_ns, cfg.row_inst, cfg.act, cfg.act_stride)
     switch (mode) {
         case SW_FWD_DIV: SSG_SW(SW_FWD_DIV); break;
         case SW_BWD_IC: SSG_SW(SW_BWD_IC); break;
@@ -206,15 +208,13 @@ void sweep_st(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux
     }
     const int grid = sweep_grid(tri.n, SW_THREADS / G, cps);
     if (G == 8)
-        launch_sweep<T, 8>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, dinv, cfg.backoff_ns, s);
+        launch_sweep<T, 8>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, dinv, cfg, s);
     else if (G == 16)
-        launch_sweep<T, 16>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, dinv, cfg.backoff_ns,
-                            s);
+        launch_sweep<T, 16>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, dinv, cfg, s);
     else if (G == 4)
-        launch_sweep<T, 4>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, dinv, cfg.backoff_ns, s);
+        launch_sweep<T, 4>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, dinv, cfg, s);
     else
-        launch_sweep<T, 32>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, dinv, cfg.backoff_ns,
-                            s);
+        launch_sweep<T, 32>(tri, val, mode, rhs, aux, D, out, out2, d_ticket, d_err, st, grid, dinv, cfg, s);
     SSG_LAUNCHED();
 }
 
