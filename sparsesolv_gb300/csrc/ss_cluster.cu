@@ -347,7 +347,11 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
                 const int a = sprp[q] - base_e, e = sprp[q + 1] - base_e;
                 const int ob = fwd ? a : a + 1;
                 const int oe = fwd ? (e > a ? e - 1 : a) : e;
-                T acc = Sc<T>::zero();
+                // IC pair: the sum is taken negated, and the forward right-hand side starts
+                // lane 0's sum, so the row's result is one operation after the reduction
+                // (the same arithmetic as the sync-free sweep)
+                constexpr bool neg = (MODE == SW_FWD_DIV || MODE == SW_BWD_IC);
+                T acc = (MODE == SW_FWD_DIV && gl == 0 && q < cnt) ? sg[q] : Sc<T>::zero();
                 // four entries per step: all addresses first, then all loads, then the
                 // multiply-adds in entry order (the same order as the sync-free sweep)
                 for (int k0 = ob + gl; k0 < oe; k0 += 4 * G) {
@@ -370,14 +374,16 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
                         if (k0 + u * G < oe) xx[u] = ld_rc<T>(ad[u]);
 #pragma unroll
                     for (int u = 0; u < 4; ++u)
-                        if (k0 + u * G < oe) acc = madd(acc, vv[u], xx[u]);
+                        if (k0 + u * G < oe) acc = madd(acc, neg ? -vv[u] : vv[u], xx[u]);
                 }
 #pragma unroll
                 for (int m = G / 2; m >= 1; m >>= 1) acc = acc + gshfl_xor(acc, m, gm);
                 if (gl == 0) {
                     T res;
                     if (MODE == SW_BWD_IC) {
-                        res = slvec[q] * (Sc<T>::zero() - acc) + sg[q];
+                        res = madd(sg[q], slvec[q], acc);  // aux + D * (-sum)
+                    } else if (MODE == SW_FWD_DIV) {
+                        res = lvec ? acc * slvec[q] : acc / ((e > a) ? sval[e - 1] : Sc<T>::zero());
                     } else {
                         T num = sg[q] - acc;
                         T u = Sc<T>::zero();

@@ -57,6 +57,7 @@ __host__ __device__ __forceinline__ cplx operator/(cplx a, cplx b) {
 }
 __host__ __device__ __forceinline__ cplxf operator+(cplxf a, cplxf b) { return {a.x + b.x, a.y + b.y}; }
 __host__ __device__ __forceinline__ cplxf operator-(cplxf a, cplxf b) { return {a.x - b.x, a.y - b.y}; }
+__host__ __device__ __forceinline__ cplxf operator-(cplxf a) { return {-a.x, -a.y}; }
 __host__ __device__ __forceinline__ cplxf operator*(cplxf a, cplxf b) {
     return {mul_rn(a.x, b.x) - mul_rn(a.y, b.y), mul_rn(a.x, b.y) + mul_rn(a.y, b.x)};
 }

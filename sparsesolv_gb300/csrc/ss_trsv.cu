@@ -120,12 +120,15 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep(int n, const int *__restri
             const int ob = fwd ? a : a + 1;       // off-diagonal range (empty when the row is)
             const int oe = fwd ? (e > a ? e - 1 : a) : e;
             const int dpos = fwd ? e - 1 : a;     // diagonal position
-            T acc = Sc<T>::zero();
+            // IC pair: the sum is taken negated, and the forward right-hand side starts
+            // lane 0's sum, so the row's result is one operation after the reduction
+            constexpr bool neg = (MODE == SW_FWD_DIV || MODE == SW_BWD_IC);
+            T acc = (MODE == SW_FWD_DIV && gl == 0) ? rhs[r] : Sc<T>::zero();
             for (int k = ob + gl; k < oe; k += G) {
                 const int c = pci[k];
                 const T v = val[k];
                 const T x = wait_value(poll + c, err, backoff_ns);
-                acc = madd(acc, v, x);
+                acc = madd(acc, neg ? -v : v, x);
             }
             const unsigned gm = group_mask(G);
 #pragma unroll
@@ -136,7 +139,9 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep(int n, const int *__restri
                 // precomputed reciprocal (off the critical path; rounding within 1 ulp).
                 T res;
                 if (MODE == SW_BWD_IC) {
-                    res = D[r] * (Sc<T>::zero() - acc) + aux[r];
+                    res = madd(aux[r], D[r], acc);  // aux + D * (-sum)
+                } else if (MODE == SW_FWD_DIV) {
+                    res = dinv ? acc * dinv[r] : acc / ((e > a) ? val[dpos] : Sc<T>::zero());
                 } else {
                     T num = rhs[r] - acc;
                     T u = Sc<T>::zero();
