@@ -47,8 +47,8 @@ CPU_SAMPLE_ITERS = 10
 # capture of the same workload: profiles/k_sweep_cluster_80cube.md (cluster sweeps, the automatic mode's choice
 # here) and profiles/k_sweep_fwd_80cube.md (sync-free forward sweep)
 NCU_TRAFFIC = {
-    ("cfg2", "fp64", "cluster", "forward sweep"): 348.0e6,
-    ("cfg2", "fp64", "cluster", "backward sweep"): 348.7e6,
+    ("cfg2", "fp64", "cluster", "forward sweep"): 348.7e6,
+    ("cfg2", "fp64", "cluster", "backward sweep"): 347.6e6,
     ("cfg2", "fp64", "sync-free", "forward sweep"): 360.6e6,
 }
 
