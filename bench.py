@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--autotune", action="store_true",
                     help="time the sweep schedules on the workload first (ssg_autotune) and keep the fastest")
+    ap.add_argument("--batch-group", type=int, default=0, choices=[0, 4, 8, 16],
+                    help="lanes a row in the sweeps of the handle's internal batch (mixed precision, --rhs); 0 auto")
     ap.add_argument("--sweep-mode", type=int, default=0, choices=[0, 1, 2, 3],
                     help="triangular sweeps: 0 automatic, 1 sync-free, 2 one-cluster level-synchronous")
     return ap.parse_args()
@@ -277,6 +279,7 @@ def run_ours(args):
     o.precision = _capi.PREC_MIXED if args.precision == "mixed" else _capi.PREC_FP64
     h.set_options(o)
     h.set_tuning(_capi.TUNE_SWEEP_MODE, args.sweep_mode)
+    h.set_tuning(_capi.TUNE_BATCH_GROUP, args.batch_group)
     h.set_matrix(rp, ci, val)
     tuned = h.autotune() if args.autotune else None
     stream = torch.cuda.ExternalStream(h.stream(), device=dev)

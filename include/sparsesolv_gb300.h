@@ -220,10 +220,11 @@ long long ssg_launch_count(void);
 #define SSG_TUNE_CLUSTER_RING_KB 6   /* distributed shared-memory ring per CTA of the cluster sweep (KB) */
 #define SSG_TUNE_CLUSTER_GROUP 7     /* lanes per row in the cluster sweep: 4 (default), 8, 16, 32 */
 #define SSG_TUNE_BATCH_GROUP 8       /* lanes per row in both sweeps of the handle's internal batch (ssg_solve_multi,
-                                        mixed precision): 0 (default: 16 for several right-hand sides of rows
-                                        with more than 6 off-diagonal lower entries on average, else 8), 4, 8,
-                                        16; the internal batch also follows SSG_TUNE_SWEEP_MODE and
-                                        SSG_TUNE_SWEEP_CTA_PER_SM */
+                                        mixed precision): 0 (default: 4 for one real right-hand side, 8 for one
+                                        complex one; for several,
+                                        16 when the lower rows hold more than 6 off-diagonal entries on average,
+                                        else 8), 4, 8, 16; the internal batch also follows SSG_TUNE_SWEEP_MODE
+                                        and SSG_TUNE_SWEEP_CTA_PER_SM */
 int ssg_set_tuning(ssg_handle h, int key, int value);
 /* Autotuner (build addition): times the IC preconditioner of the current matrix
  * and factor for each candidate sweep schedule (sync-free with 4/8/16 lanes a row

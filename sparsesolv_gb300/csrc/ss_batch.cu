@@ -47,14 +47,27 @@ __device__ __forceinline__ bool last_block(unsigned *counter) {
     return s_last != 0;
 }
 
-// an instance's tile partials, added in tile order
+// an instance's tile partials, added in tile order; the loads of D tiles are issued
+// together before their additions (a large instance has hundreds of tiles, and one
+// L2 round trip per tile dominated the reduction)
 template <int K>
 __device__ __forceinline__ void inst_sum(const BDev &B, int s, double (&tot)[K]) {
+    constexpr int D = K <= 2 ? 16 : 4;
 #pragma unroll
     for (int k = 0; k < K; ++k) tot[k] = 0.0;
-    for (int t = B.sys_tile[s]; t < B.sys_tile[s + 1]; ++t)
+    const int t1 = B.sys_tile[s + 1];
+    for (int t = B.sys_tile[s]; t < t1; t += D) {
+        double v[D][K];
 #pragma unroll
-        for (int k = 0; k < K; ++k) tot[k] += __ldcg(B.part + (size_t)t * BATCH_PARTS + k);
+        for (int u = 0; u < D; ++u)
+#pragma unroll
+            for (int k = 0; k < K; ++k) v[u][k] = t + u < t1 ? __ldcg(B.part + (size_t)(t + u) * BATCH_PARTS + k) : 0.0;
+#pragma unroll
+        for (int u = 0; u < D; ++u)
+            if (t + u < t1)
+#pragma unroll
+                for (int k = 0; k < K; ++k) tot[k] += v[u][k];
+    }
 }
 
 // last block, after the per-instance updates: the batch stays active while any instance is
@@ -1225,10 +1238,12 @@ int solve_batched(Handle &h, Batch *&mb, uint64_t &mver, uint64_t &mpat, int pre
     }
     if (!mb) mb = new Batch(h.device);
     mb->h.prof.on = h.prof.on;  // profiling and the sweep schedule follow the owning handle
-    // lanes a row: several right-hand sides make the levels wide, and rows of more than 6
-    // off-diagonal entries then run faster on 16 lanes; one right-hand side keeps 8
+    // lanes a row: one right-hand side runs the one-system schedule (the cluster sweep is
+    // fastest with 4 lanes for real rows; complex rows carry four times the multiply-adds
+    // and keep 8); several make the levels wide, and rows of more than 6 off-diagonal
+    // entries then run faster on 16 lanes
     int g = h.batch_group;
-    if (!g) g = (nrhs > 1 && (h.nnz - h.n) > 12ll * h.n) ? 16 : 8;
+    if (!g) g = nrhs == 1 ? (h.vtype == SSG_COMPLEX ? 8 : 4) : ((h.nnz - h.n) > 12ll * h.n ? 16 : 8);
     mb->h.swcfg.group = mb->h.cl_group = g;
     mb->h.swcfg.cta_per_sm = h.swcfg.cta_per_sm;
     mb->h.sweep_mode = h.sweep_mode;
