@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--method", default="iccg", choices=["iccg", "sgs", "mrtr_ic"])
+    ap.add_argument("--alpha", type=float, default=1.1, help="acceleration factor (shift) of the IC(0) factor")
     ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5"])
     ap.add_argument("--rhs", type=int, default=1,
                     help="cfg2/cfg3: right-hand sides per step, solved in one ssg_solve_multi call "
@@ -643,7 +644,9 @@ def _spmv_host(rp, ci, val, x):
 
 
 def main():
+    global ALPHA
     args = parse()
+    ALPHA = args.alpha
     if args.precision is None:
         args.precision = "mixed" if args.workload == "cfg5" else "fp64"
     if args.impl == "reference":
