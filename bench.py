@@ -436,6 +436,7 @@ def run_batch(args):
     for rp, ci, va, B in systems:
         bt.add(rp, ci, va, B)
     inst = sum(len(B) for _, _, _, B in systems)
+    tuned = bt.autotune() if args.autotune else None
     t0 = time.perf_counter()
     bt.start(_capi.METHOD_ICCG, ALPHA, conv=TOL, max_ite=20000)
     bt.wait()
@@ -525,6 +526,7 @@ def run_batch(args):
         "config": {"workload": "256 curl-curl systems, N ~ U{8..32} voxels, 4 coil right-hand sides each",
                    "instances": total_inst, "rows": int(sum(len(B) * (len(rp) - 1) for rp, _, _, B in systems)),
                    "method": "shifted ICCG", "alpha": ALPHA, "tolerance": TOL, "converged": conv_all,
+                   "sweep_schedule": "autotuned: %s" % json.dumps(tuned) if tuned else "fixed (8 lanes a row)",
                    "precision": args.precision,
                    "iterations": {"min": min(iters), "median": float(np.median(iters)), "max": max(iters)},
                    "factor": "recomputed every step", "pattern_analysis_s": t_first,

@@ -297,6 +297,13 @@ int ssg_batch_set_profiling(ssg_batch b, int enable);
 /* 1 (default): each start captures 8 iterations in a CUDA graph once and replays it
  * for the later chunks (direct launches while profiling); 0: direct launches only */
 int ssg_batch_set_graphs(ssg_batch b, int enable);
+/* Times the sweep schedules on the batch's block-diagonal matrix (as ssg_autotune:
+ * sync-free with 4/8/16 lanes a row and 2..16 CTAs per SM, one-cluster lockstep and
+ * neighbour-synchronised with 4/8) and keeps the fastest for the following starts.
+ * Results stay deterministic; an instance's bits then follow the lanes a row chosen
+ * for this batch instead of the fixed 8 (the same instance in another batch may
+ * differ at rounding level). Assembles the batch if needed; not while it runs. */
+int ssg_batch_autotune(ssg_batch b, int *mode, int *group, int *cta_per_sm, double *ms);
 int ssg_batch_kernel_stats(ssg_batch b, double *ms, long long *launches, double *bytes, int capacity);
 
 /* ---- IC(0) factor that allocates nothing (no counterpart in the reference) ----

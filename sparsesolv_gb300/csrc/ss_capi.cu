@@ -651,6 +651,20 @@ int ssg_batch_set_graphs(ssg_batch bd, int enable) {
     });
 }
 
+int ssg_batch_autotune(ssg_batch bd, int *mode, int *group, int *cta_per_sm, double *ms) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        if (b.running) return SSG_ERR_STATE;
+        if (!b.assembled) b.assemble();
+        const Handle::TuneChoice c = b.vtype == SSG_COMPLEX ? b.h.autotune<cplx>(false) : b.h.autotune<double>(false);
+        b.drop_graph();  // the captured iterations used the previous schedule
+        if (mode) *mode = c.mode;
+        if (group) *group = c.group;
+        if (cta_per_sm) *cta_per_sm = c.cta_per_sm;
+        if (ms) *ms = c.ms;
+        return SSG_OK;
+    });
+}
+
 int ssg_batch_set_profiling(ssg_batch bd, int enable) {
     return bguarded(bd, [&](ssg::Batch &b) {
         Handle &h = b.h;

@@ -649,42 +649,51 @@ Handle::TuneChoice Handle::autotune(bool keep_group) {
     const int cl_before = cl_group;
     const bool prof_on = prof.on;
     prof.on = false;
+    // a batch's sweeps skip ended instances: time every row
+    const int *row_inst = swcfg.row_inst;
+    swcfg.row_inst = nullptr;
     TuneChoice best{-1, 0, 0, 1e300};
-    for (TuneChoice &c : cand) {
-        sweep_mode = c.mode;
-        swcfg.group = c.group;
-        cl_group = c.group;
-        swcfg.cta_per_sm = c.cta_per_sm;
-        // a cluster candidate whose plan does not fit would time the sync-free sweep again
-        if (c.mode >= 2 && !(cluster_ok(Lf, sizeof(T), true) && cluster_ok(Ltb, sizeof(T), true))) continue;
-        if (c.mode == 3 && !(Lf.cl_p2p && Ltb.cl_p2p)) continue;
-        apply_precond<T>(r, z, nullptr);
-        check_err("autotune");
-        float t[3];
-        for (float &ti : t) {
-            SSG_CUDA(cudaEventRecord(ev[0], stream));
+    auto restore = [&](const TuneChoice &k, int clg) {
+        prof.on = prof_on;
+        swcfg.row_inst = row_inst;
+        sweep_mode = k.mode;
+        swcfg.group = k.group;
+        swcfg.cta_per_sm = k.cta_per_sm;
+        cl_group = clg;
+    };
+    try {
+        for (TuneChoice &c : cand) {
+            sweep_mode = c.mode;
+            swcfg.group = c.group;
+            cl_group = c.group;
+            swcfg.cta_per_sm = c.cta_per_sm;
+            // a cluster candidate whose plan does not fit would time the sync-free sweep again
+            if (c.mode >= 2 && !(cluster_ok(Lf, sizeof(T), true) && cluster_ok(Ltb, sizeof(T), true))) continue;
+            if (c.mode == 3 && !(Lf.cl_p2p && Ltb.cl_p2p)) continue;
             apply_precond<T>(r, z, nullptr);
-            SSG_CUDA(cudaEventRecord(ev[1], stream));
-            SSG_CUDA(cudaEventSynchronize(ev[1]));
-            SSG_CUDA(cudaEventElapsedTime(&ti, ev[0], ev[1]));
+            check_err("autotune");
+            float t[3];
+            for (float &ti : t) {
+                SSG_CUDA(cudaEventRecord(ev[0], stream));
+                apply_precond<T>(r, z, nullptr);
+                SSG_CUDA(cudaEventRecord(ev[1], stream));
+                SSG_CUDA(cudaEventSynchronize(ev[1]));
+                SSG_CUDA(cudaEventElapsedTime(&ti, ev[0], ev[1]));
+            }
+            check_err("autotune");
+            std::sort(t, t + 3);
+            c.ms = t[1];
+            if (c.ms < best.ms) best = c;
         }
-        check_err("autotune");
-        std::sort(t, t + 3);
-        c.ms = t[1];
-        if (c.ms < best.ms) best = c;
+    } catch (...) {
+        restore(before, cl_before);
+        throw;
     }
-    prof.on = prof_on;
     if (best.mode < 0) {
-        sweep_mode = before.mode;
-        swcfg.group = before.group;
-        swcfg.cta_per_sm = before.cta_per_sm;
-        cl_group = cl_before;
+        restore(before, cl_before);
         throw Error{SSG_ERR_STATE, "autotune: no candidate ran"};
     }
-    sweep_mode = best.mode;
-    swcfg.group = best.group;
-    cl_group = best.group;
-    swcfg.cta_per_sm = best.cta_per_sm;
+    restore(best, best.group);
     return best;
 }
 

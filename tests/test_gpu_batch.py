@@ -227,3 +227,26 @@ def test_graph_replay_equals_direct_launches(gpu, systems, precision):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     # replayed kernels are counted too: the same iterations, a similar count (no-op tail launches differ)
     assert out[True][1] > 0.5 * out[False][1]
+
+
+def test_autotuned_batch_meets_the_bar_and_stays_deterministic(gpu, oracle, systems):
+    """ssg_batch_autotune picks a sweep schedule by timing; the batch then still
+    matches the oracle per system, and repeated starts give the same bits."""
+    bt = _capi.Batch(0)
+    try:
+        for k, (rp, ci, va, b) in enumerate(systems):
+            bt.add(rp, ci, va, coil_rhs(k, 2, seed=40 + k) if k == 1 else b)
+        c = bt.autotune()
+        assert c["mode"] in (1, 2, 3) and c["group"] in (4, 8, 16) and c["ms"] > 0
+        runs = []
+        for _ in range(2):
+            bt.start(_capi.METHOD_ICCG, ALPHA, conv=1e-8, max_ite=5000)
+            bt.wait()
+            runs.append([bt.result(k) for k in range(len(systems))])
+        for k, (rp, ci, va, b) in enumerate(systems):
+            X, it, stt, ok = runs[0][k]
+            assert ok and np.array_equal(X, runs[1][k][0]) and np.array_equal(it, runs[1][k][1])
+            if k != 1:
+                check_against_oracle(oracle, "iccg", rp, ci, va, b, X[0], bt.residual_log(k), int(it[0]), False)
+    finally:
+        bt.close()
