@@ -219,6 +219,8 @@ long long ssg_launch_count(void);
                                         3 one-cluster neighbour-synchronised (IC sweeps; others as 2) */
 #define SSG_TUNE_CLUSTER_RING_KB 6   /* distributed shared-memory ring per CTA of the cluster sweep (KB) */
 #define SSG_TUNE_CLUSTER_GROUP 7     /* lanes per row in the cluster sweep: 4 (default), 8, 16, 32 */
+#define SSG_TUNE_SPMV_GROUP 9        /* lanes per row in the SpMV: 0 (default: about 8 entries a lane for real
+                                        rows, 16 for complex: 4 and 2 lanes for the voxel systems), 2, 4, 8, 16, 32 */
 #define SSG_TUNE_BATCH_GROUP 8       /* lanes per row in both sweeps of the handle's internal batch (ssg_solve_multi,
                                         mixed precision): 0 (default: 4 for one real right-hand side, 8 for one
                                         complex one; for several,

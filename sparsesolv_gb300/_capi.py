@@ -41,6 +41,7 @@ TUNE_SWEEP_MODE = 5
 TUNE_CLUSTER_RING_KB = 6
 TUNE_CLUSTER_GROUP = 7
 TUNE_BATCH_GROUP = 8
+TUNE_SPMV_GROUP = 9
 KERNEL_CLASSES = ["forward sweep", "backward sweep", "spmv", "vector", "ic factor", "level schedule"]
 
 

@@ -153,13 +153,14 @@ __global__ void __launch_bounds__(BT) k_brur0(BDev B, const T *r, const T *z) {
 }
 
 // ---------------------------------------------------------------- SpMV per tile
-// y = A x on the rows of active instances (G = 8 lanes a row, the lanes' sums
+// y = A x on the rows of active instances (G lanes a row, 4 real / 2 complex: the
+// lane count the single-system SpMV takes for the voxel systems; the lanes' sums
 // combined by a fixed butterfly); with DOT also alpha = rur0 / (x . y).
 template <typename T, bool DOT>
 __global__ void __launch_bounds__(BT) k_bspmv(BDev B, const int *__restrict__ rp, const int *__restrict__ ci,
                                               const T *__restrict__ val, const T *__restrict__ x, T *__restrict__ y) {
     if (!B.ctl->active) return;
-    constexpr int G = 8, RPB = BT / G;
+    constexpr int G = Sc<T>::is_complex ? 2 : 4, RPB = BT / G;
     const int g = threadIdx.x / G, gl = threadIdx.x % G;
     for (int t = blockIdx.x; t < B.NT; t += gridDim.x) {
         if (!B.act[(size_t)B.tile_sys[t] * B.act_stride]) continue;

@@ -393,6 +393,10 @@ int ssg_set_tuning(ssg_handle hd, int key, int value) {
                 if (value != 4 && value != 8 && value != 16 && value != 32) return SSG_ERR_ARG;
                 h.cl_group = value;
                 break;
+            case SSG_TUNE_SPMV_GROUP:
+                if (value != 0 && value != 2 && value != 4 && value != 8 && value != 16 && value != 32) return SSG_ERR_ARG;
+                h.spmv_group_req = value;
+                break;
             case SSG_TUNE_BATCH_GROUP:
                 if (value != 0 && value != 4 && value != 8 && value != 16) return SSG_ERR_ARG;
                 h.batch_group = value;
@@ -492,10 +496,10 @@ int ssg_spmv(ssg_handle hd, const double *x, double *y) {
         hd->io_x.ensure(bytes + 16);
         SSG_CUDA(cudaMemcpyAsync(hd->io_b.p, x, bytes, cudaMemcpyHostToDevice, h.stream));
         if (h.vtype == SSG_COMPLEX)
-            ssg::spmv<cplx>(h.n, h.A_rp.as<int>(), h.A_ci.as<int>(), h.A_val.as<cplx>(), hd->io_b.as<cplx>(),
+            ssg::spmv<cplx>(h.n, h.spmv_lanes(), h.A_rp.as<int>(), h.A_ci.as<int>(), h.A_val.as<cplx>(), hd->io_b.as<cplx>(),
                             hd->io_x.as<cplx>(), h.stream);
         else
-            ssg::spmv<double>(h.n, h.A_rp.as<int>(), h.A_ci.as<int>(), h.A_val.as<double>(), hd->io_b.as<double>(),
+            ssg::spmv<double>(h.n, h.spmv_lanes(), h.A_rp.as<int>(), h.A_ci.as<int>(), h.A_val.as<double>(), hd->io_b.as<double>(),
                               hd->io_x.as<double>(), h.stream);
         SSG_CUDA(cudaMemcpyAsync(y, hd->io_x.p, bytes, cudaMemcpyDeviceToHost, h.stream));
         SSG_CUDA(cudaStreamSynchronize(h.stream));

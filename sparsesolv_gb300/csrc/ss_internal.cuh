@@ -158,7 +158,7 @@ void sweep_cluster(const Tri &tri, const T *val, int mode, const T *rhs, const T
 // ss_spmv_vec.cu -- see the Krylov state there
 struct KState;
 template <typename T>
-void spmv(int n, const int *rp, const int *ci, const T *val, const T *x, T *y, cudaStream_t s);
+void spmv(int n, int group, const int *rp, const int *ci, const T *val, const T *x, T *y, cudaStream_t s);
 size_t part_bytes();
 // nat2lev[e] = level-ordered position of entry e of the natural-order triangle (rp)
 void level_positions(const Tri &T, const int *rp, int *nat2lev, cudaStream_t s);

@@ -61,8 +61,9 @@ int red_grid(int n);
 // y = A x ; with st: skipped when the solve is inactive; with dot_alpha: also
 // alpha = rur0 / (x . y) into st (ICCG)
 template <typename T>
-void k_spmv_launch(int n, const int *rp, const int *ci, const T *val, const T *x, T *y, KState *st, bool dot_alpha,
-                   double *part, cudaStream_t s);
+void k_spmv_launch(int n, int group, const int *rp, const int *ci, const T *val, const T *x, T *y, KState *st,
+                   bool dot_alpha, double *part, cudaStream_t s);
+int spmv_group(int n, long long nnz, bool cplx);  // lanes a row from the mean row length
 // ICCG: x += alpha p, r -= alpha Ap, |r| -> convergence decision
 template <typename T>
 void iccg_update(int n, KState *st, T *x, T *r, const T *p, const T *ap, double *part, double *log, cudaStream_t s);

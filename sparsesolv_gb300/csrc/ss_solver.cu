@@ -441,7 +441,7 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
     bool subtract = !zero_start;
     if (method == SSG_METHOD_MRTR && quirks) subtract = false;
     if (subtract) {
-        spmv<T>(n, rp, ci, aval, x, v, s);
+        spmv<T>(n, spmv_lanes(), rp, ci, aval, x, v, s);
         vec_sub<T>(n, b, v, r, s);
     } else if (n) {
         SSG_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, s));
@@ -540,7 +540,7 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
         prof.iter = ++iter_no;
         prof.pre = true;
         if (method == SSG_METHOD_ICCG) {
-            timed(PC_SPMV, spmv_bytes, [&] { k_spmv_launch<T>(n, rp, ci, aval, p, v, st, true, part.as<double>(), s); });
+            timed(PC_SPMV, spmv_bytes, [&] { k_spmv_launch<T>(n, spmv_lanes(), rp, ci, aval, p, v, st, true, part.as<double>(), s); });
             timed(PC_VEC, 6 * nv, [&] { iccg_update<T>(n, st, x, r, p, v, part.as<double>(), log, s); });
             prof.pre = false;
             if (o.is_save_best) timed(PC_VEC, 2 * nv, [&] { copy_if_improved<T>(n, st, x, best, s); });
@@ -548,7 +548,7 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
             timed(PC_VEC, 2 * nv, [&] { iccg_beta<T>(n, st, r, z, part.as<double>(), s); });
             timed(PC_VEC, 3 * nv, [&] { iccg_p<T>(n, st, p, z, s); });
         } else if (!sgs) {
-            timed(PC_SPMV, spmv_bytes, [&] { k_spmv_launch<T>(n, rp, ci, aval, u, v, st, false, part.as<double>(), s); });
+            timed(PC_SPMV, spmv_bytes, [&] { k_spmv_launch<T>(n, spmv_lanes(), rp, ci, aval, u, v, st, false, part.as<double>(), s); });
             apply_precond<T>(v, w, st);
             timed(PC_VEC, 4 * nv, [&] { mrtr_dots<T>(n, st, w, r, v, y, part.as<double>(), s); });
             timed(PC_VEC, 10 * nv,

@@ -104,6 +104,8 @@ struct Handle {
     bool use_inv_diag = true;
     int sweep_mode = 0;            // 0 auto (default), 1 sync-free, 2 cluster, 3 neighbour-synchronised cluster
     int batch_group = 0;           // lanes a row in the sweeps of the owning C handle's internal batch (0: auto)
+    int spmv_group_req = 0;        // lanes a row in the SpMV (0: from the mean row length)
+    int spmv_lanes() const { return spmv_group_req ? spmv_group_req : spmv_group(n, nnz, vtype == SSG_COMPLEX); }
     // rows whose factor is a copy of another row's (a batch holds a system once per
     // right-hand side): only the rows without a source are factored
     DBuf rep_src;                  // [n] source row or -1

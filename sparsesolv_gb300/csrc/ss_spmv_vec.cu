@@ -123,13 +123,21 @@ __global__ void __launch_bounds__(RED_T) k_spmv(int n, const int *__restrict__ r
     }
 }
 
-static int spmv_group(int n, const int *rp_host_mean_hint) { return 8; }
+// lanes a row from the mean row length: GB300 issues few FP64 operations per
+// clock, and every lane pays the butterfly adds and the padding of the last step,
+// so a lane takes about 8 real (16 complex) entries; measured on the 33-entry
+// rows of the voxel systems: 4 lanes 174 us, 8 lanes 233 us, 16 lanes 411 us
+// (80^3, real); 2 lanes 173 us, 4 lanes 195 us, 8 lanes 240 us (60^3, complex)
+int spmv_group(int n, long long nnz, bool cplx) {
+    const double lanes = (n ? (double)nnz / n : 0.0) / (cplx ? 16.0 : 8.0);
+    int g = 2;
+    while (g < 32 && 1.5 * g < lanes) g *= 2;
+    return g;
+}
 
-template <typename T>
-void k_spmv_launch(int n, const int *rp, const int *ci, const T *val, const T *x, T *y, KState *st, bool dot_alpha,
-                   double *part, cudaStream_t s) {
-    if (n == 0) return;
-    constexpr int G = 8;
+template <typename T, int G>
+static void spmv_launch_g(int n, const int *rp, const int *ci, const T *val, const T *x, T *y, KState *st,
+                          bool dot_alpha, double *part, cudaStream_t s) {
     const int rows_per_block = RED_T / G;
     int grid = div_up(n, rows_per_block);
     if (dot_alpha) {
@@ -143,7 +151,19 @@ void k_spmv_launch(int n, const int *rp, const int *ci, const T *val, const T *x
         k_spmv<T, G, false><<<grid, RED_T, 0, s>>>(n, rp, ci, val, x, y, st, part);
     }
     SSG_LAUNCHED();
-    (void)spmv_group;
+}
+
+template <typename T>
+void k_spmv_launch(int n, int group, const int *rp, const int *ci, const T *val, const T *x, T *y, KState *st,
+                   bool dot_alpha, double *part, cudaStream_t s) {
+    if (n == 0) return;
+    switch (group) {
+        case 2: spmv_launch_g<T, 2>(n, rp, ci, val, x, y, st, dot_alpha, part, s); break;
+        case 4: spmv_launch_g<T, 4>(n, rp, ci, val, x, y, st, dot_alpha, part, s); break;
+        case 16: spmv_launch_g<T, 16>(n, rp, ci, val, x, y, st, dot_alpha, part, s); break;
+        case 32: spmv_launch_g<T, 32>(n, rp, ci, val, x, y, st, dot_alpha, part, s); break;
+        default: spmv_launch_g<T, 8>(n, rp, ci, val, x, y, st, dot_alpha, part, s); break;
+    }
 }
 
 // ---------------------------------------------------------------- ICCG steps
@@ -382,14 +402,14 @@ void fill_sentinel_st(T *p, int n, const KState *st, cudaStream_t s) {
     SSG_LAUNCHED();
 }
 template <typename T>
-void spmv(int n, const int *rp, const int *ci, const T *val, const T *x, T *y, cudaStream_t s) {
-    k_spmv_launch<T>(n, rp, ci, val, x, y, nullptr, false, nullptr, s);
+void spmv(int n, int group, const int *rp, const int *ci, const T *val, const T *x, T *y, cudaStream_t s) {
+    k_spmv_launch<T>(n, group, rp, ci, val, x, y, nullptr, false, nullptr, s);
 }
 
 #define SSG_INST(T)                                                                                              \
-    template void k_spmv_launch<T>(int, const int *, const int *, const T *, const T *, T *, KState *, bool,   \
-                                   double *, cudaStream_t);                                                      \
-    template void spmv<T>(int, const int *, const int *, const T *, const T *, T *, cudaStream_t);              \
+    template void k_spmv_launch<T>(int, int, const int *, const int *, const T *, const T *, T *, KState *,    \
+                                   bool, double *, cudaStream_t);                                                \
+    template void spmv<T>(int, int, const int *, const int *, const T *, const T *, T *, cudaStream_t);         \
     template void iccg_update<T>(int, KState *, T *, T *, const T *, const T *, double *, double *,             \
                                  cudaStream_t);                                                                  \
     template void iccg_beta<T>(int, KState *, const T *, const T *, double *, cudaStream_t);                    \
