@@ -30,6 +30,29 @@ def test_library_exports_every_declared_symbol(solver_lib):
     assert sorted(declared) == sorted(_capi.EXPORTED)
 
 
+def test_python_constants_match_the_header():
+    """Every #define of the C header that the ctypes layer mirrors has the same value there."""
+    with open(os.path.join(_native.INCLUDE, "sparsesolv_gb300.h")) as f:
+        defines = dict(re.findall(r"#define\s+(SSG_\w+)\s+\(?(-?[0-9]+)", f.read()))
+    pairs = {
+        "SSG_OK": "SSG_OK", "SSG_NOT_CONVERGED": "SSG_NOT_CONVERGED", "SSG_ERR_ARG": "SSG_ERR_ARG",
+        "SSG_ERR_CUDA": "SSG_ERR_CUDA", "SSG_ERR_NO_DIAGONAL": "SSG_ERR_NO_DIAGONAL",
+        "SSG_ERR_TIMEOUT": "SSG_ERR_TIMEOUT", "SSG_ERR_NOMEM": "SSG_ERR_NOMEM", "SSG_ERR_STATE": "SSG_ERR_STATE",
+        "SSG_METHOD_ICCG": "METHOD_ICCG", "SSG_METHOD_MRTR": "METHOD_MRTR", "SSG_REAL": "REAL",
+        "SSG_COMPLEX": "COMPLEX", "SSG_PREC_FP64": "PREC_FP64", "SSG_PREC_MIXED": "PREC_MIXED",
+    }
+    for name, value in defines.items():
+        if name.startswith("SSG_TUNE_"):
+            pairs[name] = name[len("SSG_"):]
+    tune = [n for n in defines if n.startswith("SSG_TUNE_")]
+    assert len(tune) >= 10
+    for c_name, py_name in pairs.items():
+        assert c_name in defines, c_name
+        assert getattr(_capi, py_name) == int(defines[c_name]), (c_name, py_name)
+    # (1 << 21) is written as a shift in the header
+    assert _capi.NOALLOC_MAX_ROWS == 1 << 21
+
+
 def test_library_is_built_for_sm_103a(solver_lib):
     # the fatbinary names the target architecture in its ELF notes; cuobjdump is
     # not needed, the gencode is recorded by the build recipe
