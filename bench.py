@@ -73,6 +73,8 @@ def parse():
                     help="mixed: FP32 inner solves inside FP64 refinement on the true residual "
                          "(default: mixed for the serving stream, fp64 otherwise)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-threads", type=int, default=0,
+                    help="OpenMP threads of the CPU path (reference arm and cpu_baseline); 0: all host cores")
     ap.add_argument("--autotune", action="store_true",
                     help="time the sweep schedules on the workload first (ssg_autotune) and keep the fastest")
     ap.add_argument("--batch-group", type=int, default=0, choices=[0, 4, 8, 16],
@@ -649,6 +651,9 @@ def main():
     global ALPHA
     args = parse()
     ALPHA = args.alpha
+    if args.cpu_threads > 0:
+        # read by the CPU path's OpenMP runtime when its library loads (after this point)
+        os.environ["OMP_NUM_THREADS"] = str(args.cpu_threads)
     if args.precision is None:
         args.precision = "mixed" if args.workload == "cfg5" else "fp64"
     if args.impl == "reference":
