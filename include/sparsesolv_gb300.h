@@ -227,6 +227,11 @@ long long ssg_launch_count(void);
                                         16 when the lower rows hold more than 6 off-diagonal entries on average,
                                         else 8), 4, 8, 16; the internal batch also follows SSG_TUNE_SWEEP_MODE
                                         and SSG_TUNE_SWEEP_CTA_PER_SM */
+#define SSG_TUNE_SPIN_LIMIT_US 10    /* how long a bounded device wait (factor row flags, sync-free sweep values,
+                                        level schedule, neighbour-synchronised progress) polls before it gives up
+                                        and the call returns SSG_ERR_TIMEOUT, in microseconds; 0 (default): 4 s.
+                                        A short limit makes waits that would have succeeded fail: for tests of the
+                                        timeout path; the handle stays usable after such a failure */
 int ssg_set_tuning(ssg_handle h, int key, int value);
 /* Autotuner (build addition): times the IC preconditioner of the current matrix
  * and factor for each candidate sweep schedule (sync-free with 4/8/16 lanes a row
@@ -319,24 +324,30 @@ int ssg_batch_kernel_stats(ssg_batch b, double *ms, long long *launches, double 
  *
  * All pointers are device memory on the calling thread's current device:
  *   lrp[n+1], lci[nnz]  lower triangle of A including the diagonal, CSR in
- *                       natural row order, columns ascending, diagonal last in
- *                       each row, at most 32 entries a row (the pattern
- *                       ssg_factor returns)
- *   lower_val[nnz]      A's values on that pattern (double, or interleaved
- *                       complex for value_type SSG_COMPLEX)
+ *                       natural row order, columns strictly ascending, diagonal
+ *                       last in each row, at most 32 entries a row (the pattern
+ *                       ssg_factor returns); 4-byte aligned
+ *   lower_val[nnz]      A's values on that pattern (double, 8-byte aligned, or
+ *                       interleaved complex, 16-byte aligned, for value_type
+ *                       SSG_COMPLEX; lval and D have the same alignment)
  *   lval[nnz], D[n]     outputs: L on the same pattern and D = 1/pivot, the
  *                       shifted IC(0) of src/SprsPreconditioner.cpp:43-111;
  *                       lval may be lower_val (factor in place)
  *   alpha > 0           the shift (acceleration factor); no automatic search
  * Work is queued on `stream` (NULL: the legacy default stream) and the call
  * waits for it, so the result is ready on return. Returns SSG_OK,
- * SSG_ERR_ARG (n > SSG_NOALLOC_MAX_ROWS, a bad argument, or a row longer than
- * 32 entries), SSG_ERR_NO_DIAGONAL, SSG_ERR_TIMEOUT or SSG_ERR_CUDA.
- * The first call on a device looks up the array's device address (once per
- * device, cudaGetSymbolAddress); make that first call before any stream
- * capture. All calls share the one array and it keeps the last call's
- * contents (each call clears what it uses), so calls whose work overlaps on
- * the GPU (other threads, other streams) race: serialise them. */
+ * SSG_ERR_ARG (n > SSG_NOALLOC_MAX_ROWS, a null or misaligned pointer, a row
+ * longer than 32 entries, a column out of range or columns not ascending),
+ * SSG_ERR_NO_DIAGONAL, SSG_ERR_TIMEOUT or SSG_ERR_CUDA; every argument check
+ * is made before any GPU work. A stream that is capturing work into a CUDA
+ * graph is refused with SSG_ERR_STATE before anything is queued: the call
+ * reads its status back to the host and waits. The first call on a device
+ * looks up the array's device address (once per device, cudaGetSymbolAddress).
+ * All calls share the one array and it keeps the last call's contents (each
+ * call clears what it uses), so calls whose work overlaps on the GPU (other
+ * threads, other streams) race: serialise them. A call that fails after its
+ * kernel was queued waits for that kernel before it returns, so the array is
+ * idle whenever a call has returned. */
 #define SSG_NOALLOC_MAX_ROWS (1 << 21)
 int ssg_ic_factor_noalloc(int n, int nnz, const int32_t *lrp, const int32_t *lci, const void *lower_val, void *lval,
                           void *D, double alpha, int value_type, void *stream);

@@ -18,17 +18,18 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libsparsesolv_ref.so")
-REF_SRC = os.environ.get("SPARSESOLV_REFERENCE", "/root/reference")
 
 
 def build(force=False):
-    """Build liboracle.so, and _ref/ when the reference checkout is present."""
+    """Build liboracle.so, and _ref/ when the reference checkout is present
+    (oracle/Makefile's ref-if-present: the SPARSESOLV_REFERENCE environment
+    variable names the checkout; without one the step prints a message)."""
     cmd = ["make", "-s", "-C", HERE, "all"]
     if force:
         cmd.insert(1, "-B")
     subprocess.run(cmd, check=True)
-    if os.path.isdir(os.path.join(REF_SRC, "src")):
-        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", "REF=" + REF_SRC], check=True)
+    subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref-if-present"], check=True,
+                   stdout=subprocess.DEVNULL if os.path.exists(REF_LIB) else None)
 
 
 class _Opts(ctypes.Structure):

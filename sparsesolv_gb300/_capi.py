@@ -42,6 +42,7 @@ TUNE_CLUSTER_RING_KB = 6
 TUNE_CLUSTER_GROUP = 7
 TUNE_BATCH_GROUP = 8
 TUNE_SPMV_GROUP = 9
+TUNE_SPIN_LIMIT_US = 10
 KERNEL_CLASSES = ["forward sweep", "backward sweep", "spmv", "vector", "ic factor", "level schedule"]
 
 

@@ -1248,6 +1248,7 @@ int solve_batched(Handle &h, Batch *&mb, uint64_t &mver, uint64_t &mpat, int pre
     mb->h.swcfg.group = mb->h.cl_group = g;
     mb->h.swcfg.cta_per_sm = h.swcfg.cta_per_sm;
     mb->h.sweep_mode = h.sweep_mode;
+    if (mb->h.spin_limit_us != h.spin_limit_us) mb->h.set_spin_limit(h.spin_limit_us);
     AllocStream as(mb->h.stream);  // the batch's buffers are ordered on its own stream
     const int w = h.vtype == SSG_COMPLEX ? 2 : 1;
     const bool same_rhs = !mb->sys.empty() && mb->sys[0].nrhs == nrhs;

@@ -401,6 +401,10 @@ int ssg_set_tuning(ssg_handle hd, int key, int value) {
                 if (value != 0 && value != 4 && value != 8 && value != 16) return SSG_ERR_ARG;
                 h.batch_group = value;
                 break;
+            case SSG_TUNE_SPIN_LIMIT_US:
+                if (value < 0) return SSG_ERR_ARG;
+                h.set_spin_limit(value);
+                break;
             default:
                 return SSG_ERR_ARG;
         }

@@ -448,7 +448,7 @@ __global__ void __launch_bounds__(544) k_sweep_cluster(int nlev, int ncomp, cons
                             while ((int)ld_acquire_progress(ra) < req) {
                                 if ((++polls & 63) == 0) {
                                     if (*(volatile int *)err) break;
-                                    if (gtimer() - t0 > SPIN_LIMIT_NS) {
+                                    if (gtimer() - t0 > spin_limit_ns(err)) {
                                         atomicExch(err, ERR_TIMEOUT);
                                         break;
                                     }

@@ -191,10 +191,18 @@ enum : int {
     ERR_TIMEOUT = 1,   // a bounded spin gave up
     ERR_NO_DIAG = 2,   // a row of the lower triangle lacks its diagonal
     ERR_ROW_TOO_LONG = 3,  // a factor row exceeds the per-warp register budget
+    ERR_PATTERN = 4,   // a caller-given row has a column out of range or columns not ascending
 };
 
 // Spin bound: a wait gives up after this many nanoseconds of %globaltimer.
+// The int after an error word holds the owner's limit in microseconds
+// (SSG_TUNE_SPIN_LIMIT_US); zero, as in freshly cleared scratch, means the
+// default of 4 s.
 constexpr unsigned long long SPIN_LIMIT_NS = 4000000000ull;  // 4 s
+__device__ __forceinline__ unsigned long long spin_limit_ns(const int *err) {
+    const int us = ((const volatile int *)err)[1];
+    return us > 0 ? 1000ull * (unsigned long long)us : SPIN_LIMIT_NS;
+}
 
 __device__ __forceinline__ unsigned long long gtimer() {
     unsigned long long t;

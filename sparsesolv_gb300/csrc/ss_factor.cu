@@ -40,7 +40,7 @@ __device__ __forceinline__ void wait_row_done(const int *done, int c, int *err) 
     while (*f == 0) {
         if ((++polls & 63) == 0) {
             if (*(volatile int *)err) return;
-            if (gtimer() - start > SPIN_LIMIT_NS) {
+            if (gtimer() - start > spin_limit_ns(err)) {
                 atomicExch(err, ERR_TIMEOUT);
                 return;
             }
@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(256) k_ic_factor(int n, const int *perm, const
                     while (*f == 0) {
                         if ((++polls & 63) == 0) {
                             if (*(volatile int *)err) break;
-                            if (gtimer() - start > SPIN_LIMIT_NS) {
+                            if (gtimer() - start > spin_limit_ns(err)) {
                                 atomicExch(err, ERR_TIMEOUT);
                                 break;
                             }
@@ -268,12 +268,15 @@ __global__ void __launch_bounds__(ff_warps<T>() * 32) k_ic_factor_fast(int n, co
         const int c = have ? pci[a + lane] : INT_MAX;
         T v = have ? lval[a + lane] : Sc<T>::zero();
         const int last_c = __shfl_sync(0xffffffffu, c, (m - 1) & 31);
-        // caller-given pattern (natural order): off-diagonal columns must lie in [0, i)
-        const bool bad_col = NAT && __any_sync(0xffffffffu, have && lane < m - 1 && (c < 0 || c >= i));
+        // caller-given pattern (natural order): off-diagonal columns must lie in [0, i) and
+        // ascend strictly (the merge below walks both rows in column order)
+        const int prev_c = __shfl_up_sync(0xffffffffu, c, 1);
+        const bool bad_col =
+            NAT && __any_sync(0xffffffffu, have && ((lane < m - 1 && (c < 0 || c >= i)) || (lane > 0 && prev_c >= c)));
         if (m < 1 || m > FF_MAXROW || last_c != i || bad_col) {
-            // no diagonal last (src/SprsPreconditioner.cpp:88-94) or too long for this kernel
+            // no diagonal last (src/SprsPreconditioner.cpp:88-94), a bad caller pattern, or too long
             if (lane == 0) {
-                atomicExch(err, m > FF_MAXROW ? ERR_ROW_TOO_LONG : ERR_NO_DIAG);
+                atomicExch(err, m > FF_MAXROW ? ERR_ROW_TOO_LONG : (bad_col && last_c == i) ? ERR_PATTERN : ERR_NO_DIAG);
                 D[i] = Sc<T>::one();
             }
             __syncwarp();
@@ -293,7 +296,7 @@ __global__ void __launch_bounds__(ff_warps<T>() * 32) k_ic_factor_fast(int n, co
                     if (backoff_ns) __nanosleep(backoff_ns);
                     if ((++polls & 15) == 0) {
                         if (*(volatile int *)err) break;
-                        if (gtimer() - start > SPIN_LIMIT_NS) {
+                        if (gtimer() - start > spin_limit_ns(err)) {
                             atomicExch(err, ERR_TIMEOUT);
                             break;
                         }
@@ -552,12 +555,23 @@ static cudaError_t noalloc_launch(int n, const int *lrp, const int *lci, void *l
 
 // Natural-order IC(0) with the scratch above. Every failure returns a code;
 // nothing here allocates, host or device, on the way to a result.
+static bool aligned_to(const void *p, size_t a) { return ((uintptr_t)p % a) == 0; }
+
 int ic_factor_noalloc(int n, int nnz, const int *lrp, const int *lci, const void *val, void *lval, void *D,
                       double alpha, int vtype, cudaStream_t s) {
     if (n < 0 || nnz < 0 || n > SSG_NOALLOC_MAX_ROWS) return SSG_ERR_ARG;
     if (!(alpha > 0.0) || (vtype != SSG_REAL && vtype != SSG_COMPLEX)) return SSG_ERR_ARG;
     if (n == 0) return SSG_OK;
     if (!lrp || !lci || !val || !lval || !D || nnz < n) return SSG_ERR_ARG;
+    // the kernel reads a complex value as one 16-byte load, a real one as 8 bytes
+    const size_t va = vtype == SSG_COMPLEX ? 16 : 8;
+    if (!aligned_to(lrp, 4) || !aligned_to(lci, 4) || !aligned_to(val, va) || !aligned_to(lval, va) ||
+        !aligned_to(D, va))
+        return SSG_ERR_ARG;
+    // the call reads its error word back and waits for the stream: not inside a capture
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return SSG_ERR_CUDA;
+    if (cap != cudaStreamCaptureStatusNone) return SSG_ERR_STATE;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return SSG_ERR_CUDA;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return SSG_ERR_CUDA;
@@ -571,20 +585,27 @@ int ic_factor_noalloc(int n, int nnz, const int *lrp, const int *lci, const void
     if (cudaMemsetAsync(scr, 0, sizeof(int) * (NA_HEAD + (size_t)n), s) != cudaSuccess) return SSG_ERR_CUDA;
     const cudaError_t le = vtype == SSG_COMPLEX ? noalloc_launch<cplx>(n, lrp, lci, lval, D, alpha, scr, sms, s)
                                                 : noalloc_launch<double>(n, lrp, lci, lval, D, alpha, scr, sms, s);
-    if (le != cudaSuccess) return SSG_ERR_CUDA;
+    // from here on a failure waits for the queued work first, so the shared scratch is
+    // idle when the call returns, whatever the outcome
+    auto fail = [&](int code) {
+        (void)cudaStreamSynchronize(s);
+        return code;
+    };
+    if (le != cudaSuccess) return fail(SSG_ERR_CUDA);
     try {
         note_launch();
     } catch (...) {
-        return SSG_ERR_CUDA;
+        return fail(SSG_ERR_CUDA);
     }
     int err = 0;
-    if (cudaMemcpyAsync(&err, scr + 1, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return SSG_ERR_CUDA;
+    if (cudaMemcpyAsync(&err, scr + 1, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return fail(SSG_ERR_CUDA);
     if (cudaStreamSynchronize(s) != cudaSuccess) return SSG_ERR_CUDA;
     switch (err) {
         case ERR_NONE: return SSG_OK;
         case ERR_TIMEOUT: return SSG_ERR_TIMEOUT;
         case ERR_NO_DIAG: return SSG_ERR_NO_DIAGONAL;
-        default: return SSG_ERR_ARG;  // a row longer than the kernel's 32 entries
+        default: return SSG_ERR_ARG;  // a row longer than 32 entries, or a bad column pattern
     }
 }
 

@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(LV_THREADS) k_levels(int n, const int *rp, con
                             __nanosleep(32);
                             if ((++polls & 63) == 0) {
                                 if (*(volatile int *)err) { v = 0; break; }
-                                if (gtimer() - start > SPIN_LIMIT_NS) {
+                                if (gtimer() - start > spin_limit_ns(err)) {
                                     atomicExch(err, ERR_TIMEOUT);
                                     v = 0;
                                     break;

@@ -96,6 +96,12 @@ Handle::~Handle() {
     // the stream itself goes with sg, after the buffers have been freed on it
 }
 
+void Handle::set_spin_limit(int us) {
+    spin_limit_us = us;
+    SSG_CUDA(cudaMemcpyAsync(err() + 1, &spin_limit_us, sizeof(int), cudaMemcpyHostToDevice, stream));
+    SSG_CUDA(cudaStreamSynchronize(stream));
+}
+
 void Handle::check_err(const char *where) {
     int herr = 0;
     SSG_CUDA(cudaMemcpyAsync(&herr, err(), sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -105,6 +111,7 @@ void Handle::check_err(const char *where) {
     SSG_CUDA(cudaStreamSynchronize(stream));
     if (herr == ERR_TIMEOUT) throw Error{SSG_ERR_TIMEOUT, std::string(where) + ": a bounded device wait timed out"};
     if (herr == ERR_NO_DIAG) throw Error{SSG_ERR_NO_DIAGONAL, "there is not diagonal element!"};
+    if (herr == ERR_PATTERN) throw Error{SSG_ERR_ARG, std::string(where) + ": bad column pattern"};
     if (herr == ERR_ROW_TOO_LONG)
         throw Error{SSG_ERR_ARG, std::string(where) + ": a row of the lower triangle is longer than the kernel takes"};
     throw Error{SSG_ERR_STATE, std::string(where) + ": device error " + std::to_string(herr)};
@@ -231,6 +238,7 @@ template <typename T>
 void Handle::ensure_factor(double alpha, bool scaled) {
     ensure_patterns(true, false);
     if (fac_valid && fac_version == version && fac_alpha_req == alpha && fac_scaled == (int)scaled) return;
+    fac_valid = false;  // a factorisation that throws leaves no stale factor marked valid
     const T *aval = A_val.as<T>();
     if (scaled) {
         ensure_scaled<T>();

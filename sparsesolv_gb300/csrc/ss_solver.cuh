@@ -132,7 +132,9 @@ struct Handle {
     }
 
     int *ticket() { return small.as<int>(); }
-    int *err() { return small.as<int>() + 4; }
+    int *err() { return small.as<int>() + 4; }  // err()[1]: spin limit of the bounded waits (us, 0: 4 s)
+    int spin_limit_us = 0;                      // SSG_TUNE_SPIN_LIMIT_US
+    void set_spin_limit(int us);
     double *dscal() { return (double *)(small.as<char>() + 64); }
     KState *st() { return state.as<KState>(); }
 

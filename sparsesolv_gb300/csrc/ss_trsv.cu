@@ -80,7 +80,7 @@ __device__ __forceinline__ T wait_value(const T *p, int *err, int backoff_ns) {
         if (backoff_ns) __nanosleep(backoff_ns);
         if ((++polls & 31) == 0) {
             if (*(volatile int *)err) return Ready<T>::nan();
-            if (gtimer() - start > SPIN_LIMIT_NS) {
+            if (gtimer() - start > spin_limit_ns(err)) {
                 atomicExch(err, ERR_TIMEOUT);
                 return Ready<T>::nan();
             }

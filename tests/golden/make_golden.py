@@ -1,8 +1,9 @@
 """Generate the golden fixtures from the reference itself.
 
 Runs the reference's own solver classes, compiled from its sources into
-oracle/_ref/ by oracle/Makefile (needs the SparseSolv checkout, default
-/root/reference), on seeded systems from sparsesolv_gb300.voxel and on the 5x5
+oracle/_ref/ by oracle/Makefile (needs the SparseSolv checkout, named by the
+SPARSESOLV_REFERENCE environment variable or the Makefile's default), on
+seeded systems from sparsesolv_gb300.voxel and on the 5x5
 example matrix of the reference's documentation (docs/html/Introduction.md of
 SparseSolv). Writes tests/golden/golden.npz (residual logs, solutions, IC
 factors) and tests/golden/golden.json (iteration counts, convergence flags,

@@ -134,3 +134,36 @@ def test_edge_case_against_oracle(handle, oracle, name, method, pt):
         assert np.allclose(log[:k], o.log[:k], rtol=1e-6, atol=1e-13 * o.log[0])
         assert np.linalg.norm(x - o.x) <= 1e-6 * np.linalg.norm(o.x)
         assert np.linalg.norm(b - A @ x) < 1e-7 * np.linalg.norm(b)
+
+
+def test_timeout_reports_error_and_handle_stays_usable(handle, oracle):
+    """A bounded wait that runs out: with the spin limit at 1 us the sync-free
+    sweep over the 50,000-row chain (each row waits on the one before it, held
+    by another warp) gives up, the call returns SSG_ERR_TIMEOUT, and with the
+    default limit restored the next solve on the same handle meets the parity
+    bar again. No fault and no hang: the wait is cut short, not broken."""
+    rp, ci, va, b = case("chain")
+    s = Settings(accel_factor=1.1, is_save_residual_log=True)
+    o = oracle.solve("iccg", rp, ci, va, b, s, maxit=20000)
+    try:
+        handle.set_tuning(_capi.TUNE_SWEEP_MODE, 1)
+        ok, x, log, iters = solve(handle, "iccg", rp, ci, va, b, s)   # pattern and factor cached
+        assert ok and iters == o.iters
+        handle.set_tuning(_capi.TUNE_SPIN_LIMIT_US, 1)
+        with pytest.raises(_capi.SolverError) as e:
+            handle.apply_precond(b)
+        assert e.value.code == _capi.SSG_ERR_TIMEOUT
+        # a solve that uploads the matrix again re-runs the pattern analysis and the factor,
+        # whose waits (level schedule, factor row flags) time out the same way
+        with pytest.raises(_capi.SolverError) as e:
+            solve(handle, "iccg", rp, ci, va, b, s)
+        assert e.value.code == _capi.SSG_ERR_TIMEOUT
+    finally:
+        handle.set_tuning(_capi.TUNE_SPIN_LIMIT_US, 0)
+    try:
+        ok, x, log, iters = solve(handle, "iccg", rp, ci, va, b, s)
+    finally:
+        handle.set_tuning(_capi.TUNE_SWEEP_MODE, 0)
+    assert ok and iters == o.iters
+    assert np.allclose(log, o.log, rtol=1e-6, atol=1e-13 * o.log[0])
+    assert np.linalg.norm(x - o.x) <= 1e-6 * np.linalg.norm(o.x)
