@@ -9,23 +9,31 @@ update, which keeps only the pattern analysis), then the iterations run to
 tolerance. ``value`` is solves per second over the whole job with the matrix
 and b resident in HBM; ``e2e`` is the same through the C ABI with host
 buffers (values, b and x0 copied in, x copied out inside the timed region).
+The line also carries, for the same matrix on the same GPU: the solution's
+distance from a full FP64 solve of the oracle (``parity``), the mixed-precision
+solve against this plain FP64 one (``mixed``), the serving stream against the
+plain path one request at a time (``serving``), and the first solve of a new
+sparsity pattern (``new_pattern``).
 
     python bench.py [--steps K] [--warmup W] [--method iccg|sgs|mrtr_ic]
-                    [--workload cfg2|cfg1] [--sweep-mode 0|1|2] [--impl reference]
+                    [--workload cfg2|cfg1|cfg3|cfg4|cfg5] [--sweep-mode 0..4]
+                    [--impl reference]
 
 Under torchrun (--gpus N > 1) every rank solves its own replica (the path
 does not shard; "replicas only") and value sums the ranks' solves.
---impl reference times the reference algorithm on the host cores instead:
-the reference built from its sources (oracle/_ref) where that build exists,
-else the oracle's C restatement of it, on a bounded sample of each step
-(factorisation plus a fixed number of iterations, scaled to the iteration
-count of a full solve).
+--impl reference times the reference algorithm on the host cores and touches
+no GPU: every step is one full solve to tolerance (factorisation plus every
+iteration), by the reference built from its sources (oracle/_ref) where that
+build exists, else by the oracle's C restatement of it, with the SpMV on all
+host cores as the reference's OpenMP build runs it; one more solve on one
+thread is reported beside it.
 """
 from __future__ import annotations
 
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -40,7 +48,7 @@ sys.path.insert(0, HERE)
 METRIC = "time-to-1e-8 residual (s), solves/s, p50/p99 latency vs plain FP64 GPU ICCG"
 TOL = 1e-8
 ALPHA = 1.1
-CPU_SAMPLE_ITERS = 10
+MAXIT = 20000
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel, from one ncu
@@ -73,14 +81,17 @@ def parse():
                     help="mixed: FP32 inner solves inside FP64 refinement on the true residual "
                          "(default: mixed for the serving stream, fp64 otherwise)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="leave the mixed-precision comparison out of the line")
+    ap.add_argument("--no-serving", action="store_true", help="leave the serving stream out of the line")
     ap.add_argument("--cpu-threads", type=int, default=0,
                     help="OpenMP threads of the CPU path (reference arm and cpu_baseline); 0: all host cores")
     ap.add_argument("--autotune", action="store_true",
                     help="time the sweep schedules on the workload first (ssg_autotune) and keep the fastest")
     ap.add_argument("--batch-group", type=int, default=0, choices=[0, 4, 8, 16],
                     help="lanes a row in the sweeps of the handle's internal batch (mixed precision, --rhs); 0 auto")
-    ap.add_argument("--sweep-mode", type=int, default=0, choices=[0, 1, 2, 3],
-                    help="triangular sweeps: 0 automatic, 1 sync-free, 2 one-cluster level-synchronous")
+    ap.add_argument("--sweep-mode", type=int, default=0, choices=[0, 1, 2, 3, 4],
+                    help="triangular sweeps: 0 automatic, 1 sync-free, 2 one-cluster level-synchronous, "
+                         "3 one-cluster neighbour-synchronised, 4 one-cluster push")
     return ap.parse_args()
 
 
@@ -167,78 +178,150 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def cpu_time_sample(rp, ci, val, b, method, pt, sample_iters, full_iters, use_ref):
-    """Seconds per full solve on the host: factorisation + sample_iters
-    iterations of the reference algorithm, scaled to full_iters."""
-    from oracle.oracle import Oracle, Reference, Settings
-    eng = Reference() if use_ref else Oracle()
-    s = Settings(accel_factor=ALPHA, precondition_type=pt, is_save_residual_log=True)
-    m = "iccg" if method == "iccg" else "mrtr"
-    t0 = time.perf_counter()
-    eng.solve(m, rp, ci, val, b, s, conv=TOL, maxit=0)
-    t_setup = time.perf_counter() - t0      # factorisation (and set-up) only
-    t0 = time.perf_counter()
-    eng.solve(m, rp, ci, val, b, s, conv=TOL, maxit=sample_iters)
-    t_sample = time.perf_counter() - t0
-    per_iter = max(t_sample - t_setup, 1e-9) / sample_iters
-    return t_setup + per_iter * full_iters, t_setup, per_iter, eng.threads()
+def host_info():
+    """Host cores and CPU model of the machine the CPU path runs on."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+                             timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"nproc": os.cpu_count(), "cpu_model": model or platform.processor() or platform.machine(),
+            "machine": platform.machine()}
+
+
+def workload_config(label, n, nnz, mname, precision, K):
+    """The workload as both arms name it (the same dict in both lines)."""
+    return {"workload": label, "n": n, "nnz": nnz, "method": mname, "alpha": ALPHA, "tolerance": TOL,
+            "precision": precision, "right_hand_sides": K, "x0": "zero", "factor": "recomputed every step",
+            "l2": "inputs larger than L2 (matrix %.0f MB)" % ((12.0 * nnz) / 1e6)}
+
+
+def extra_rhs(rp, ci, val, b, K):
+    """b followed by K - 1 right-hand sides in the range of A (the curl-curl
+    systems are singular), each of the norm of b, seeded."""
+    if K <= 1:
+        return [b]
+    n = len(b)
+    cplx = np.iscomplexobj(val)
+    rng = np.random.default_rng(2024)
+    out = [b]
+    for _ in range(K - 1):
+        v = rng.standard_normal(n) + (1j * rng.standard_normal(n) if cplx else 0.0)
+        e = _spmv_host(rp, ci, val, v)
+        out.append(e * (np.linalg.norm(b) / np.linalg.norm(e)))
+    return out
+
+
+class CpuPath:
+    """The reference algorithm on the host cores: the reference built from its
+    sources (oracle/_ref) where that build exists, else the oracle's C
+    restatement. Both run the SpMV row-parallel on OpenMP threads, as the
+    reference's Eigen product does; the factorisation, sweeps and vector work
+    are serial, as in the reference."""
+
+    def __init__(self, method, pt):
+        from oracle.oracle import Oracle, Reference, Settings, build
+        build()
+        self.orc = Oracle()
+        self.use_ref = Reference.available()
+        self.eng = Reference() if self.use_ref else self.orc
+        self.kind = "reference" if self.use_ref else "port"
+        self.m = "iccg" if method == "iccg" else "mrtr"
+        self.settings = Settings(accel_factor=ALPHA, precondition_type=pt, is_save_residual_log=True)
+
+    def solve(self, rp, ci, val, b, threads):
+        """One full solve to tolerance: (result, total s, set-up s or None)."""
+        self.orc.set_threads(threads)  # the OpenMP runtime is shared with the reference build
+        t0 = time.perf_counter()
+        res = self.eng.solve(self.m, rp, ci, val, b, self.settings, conv=TOL, maxit=MAXIT)
+        total = time.perf_counter() - t0
+        setup = self.orc.last_timings()[0] if not self.use_ref else None
+        return res, total, setup
+
+    def setup_seconds(self, rp, ci, val, b, threads):
+        """Set-up alone (scaling, factor, transpose): a solve stopped before its
+        first iteration (its "not converged" message kept off stdout, which
+        carries the JSON line)."""
+        self.orc.set_threads(threads)
+        sys.stdout.flush()
+        saved = os.dup(1)
+        devnull = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(devnull, 1)
+        try:
+            t0 = time.perf_counter()
+            self.eng.solve(self.m, rp, ci, val, b, self.settings, conv=TOL, maxit=0)
+            return time.perf_counter() - t0
+        finally:
+            os.dup2(saved, 1)
+            os.close(saved)
+            os.close(devnull)
+
+
+def phases(res, total, setup):
+    it = max(int(res.iters), 1)
+    return {"total_s": total, "setup_s": setup, "per_iteration_s": (total - setup) / it if setup is not None else None,
+            "iterations": int(res.iters), "converged": bool(res.converged)}
 
 
 def run_reference(args):
+    """The reference's CPU path on the host cores, full solves; no GPU is touched."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    from oracle.oracle import Reference, build
-    build()
+    if args.workload not in ("cfg1", "cfg2", "cfg3"):
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU arm times single-system workloads "
+                          "(cfg1, cfg2, cfg3); %s has no reference counterpart to time" % args.workload}),
+              flush=True)
+        return
     label, rp, ci, val, b = workload(args.workload)
     _, pt, mname = method_args(args.method)
-    use_ref = Reference.available()
-    full_iters = reference_iterations(args, rp, ci, val, b, pt)
-    times = []
+    n, nnz = len(rp) - 1, len(ci)
+    K = max(1, args.rhs)
+    bs = extra_rhs(rp, ci, val, b, K)
+    cpu = CpuPath(args.method, pt)
+    threads = args.cpu_threads or os.cpu_count() or 1
+    times, last = [], None
     for k in range(args.warmup + args.steps):
-        t, ts, ti, cores = cpu_time_sample(rp, ci, val, b, args.method, pt, CPU_SAMPLE_ITERS, full_iters, use_ref)
+        t_step = 0.0
+        for bj in bs:
+            res, total, setup = cpu.solve(rp, ci, val, bj, threads)
+            t_step += total
+            if bj is b:
+                last = (res, total, setup)
         if k >= args.warmup:
-            times.append(t)
+            times.append(t_step)
+    res, total, setup = last
+    if setup is None:
+        setup = cpu.setup_seconds(rp, ci, val, b, threads)
+    true_res = float(np.linalg.norm(b - _spmv_host(rp, ci, val, res.x)) / np.linalg.norm(b))
+    r1, t1, s1 = cpu.solve(rp, ci, val, b, 1)
+    if s1 is None:
+        s1 = cpu.setup_seconds(rp, ci, val, b, 1)
     sec = sum(times) / len(times)
-    value = 1.0 / sec
-    kind = "reference" if use_ref else "port"
-    sample = ("%s: IC(0) factorisation + %d iterations of the %s per step, scaled to the %d iterations of a "
-              "full solve; SpMV row-parallel on %d OpenMP threads as in the reference, the rest serial"
-              % (label, CPU_SAMPLE_ITERS, mname, full_iters, cores))
+    value = K / sec
+    sample = ("%s: every step %d full solve(s) to %g (factorisation and all iterations) by the %s, SpMV on %d "
+              "OpenMP threads, the rest serial as in the reference" %
+              (label, K, TOL, "reference built from its sources" if cpu.use_ref else "oracle's C restatement",
+               threads))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded voxel generator)",
-            "config": {"workload": label, "method": mname, "alpha": ALPHA, "tolerance": TOL},
-            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": kind, "sample": sample},
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128" if np.iscomplexobj(val) else "f64",
+            "data": "synthetic (seeded voxel generator)",
+            "config": workload_config(label, n, nnz, mname, "fp64", K),
+            "time_to_tolerance_s": total,
+            "latency_ms": {"p50": float(np.percentile(times, 50) * 1e3), "p99": float(np.percentile(times, 99) * 1e3),
+                           "steps": len(times)},
+            "phases": dict(phases(res, total, setup), threads=threads, true_relative_residual=true_res),
+            "one_thread": dict(phases(r1, t1, s1), solves_per_s=1.0 / t1),
+            "host": host_info(),
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": cpu.kind, "sample": sample},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
-
-
-def reference_iterations(args, rp, ci, val, b, pt):
-    """Iterations of a full solve: the GPU arm's parity is within 3% of the
-    reference, so the count is taken from one GPU solve when a GPU is
-    present, else from the oracle itself."""
-    try:
-        import torch
-        if torch.cuda.is_available():
-            from sparsesolv_gb300 import _capi
-            h = _capi.Handle(0)
-            o = h.default_options()
-            o.accel_factor = ALPHA
-            o.precondition_type = pt
-            h.set_options(o)
-            h.set_matrix(rp, ci, val)
-            x = np.zeros_like(b)
-            meth, _, _ = method_args(args.method)
-            h.solve(meth, b, x, conv=TOL, max_ite=20000)
-            it = h.iters()
-            h.close()
-            return it
-    except Exception:
-        pass
-    from oracle.oracle import Oracle, Settings
-    m = "iccg" if args.method == "iccg" else "mrtr"
-    return Oracle().solve(m, rp, ci, val, b, Settings(accel_factor=ALPHA, precondition_type=pt), conv=TOL).iters
 
 
 def run_ours(args):
@@ -256,16 +339,8 @@ def run_ours(args):
     cplx = np.iscomplexobj(val)
     tdt = torch.complex128 if cplx else torch.float64
     K = max(1, args.rhs)
-    b1 = b  # the workload's own right-hand side (the CPU baseline solves it)
-    if K > 1:
-        # further right-hand sides in the range of A (the curl-curl systems are singular), |b| each
-        rng = np.random.default_rng(2024)
-        extra = []
-        for _ in range(K - 1):
-            v = rng.standard_normal(n) + (1j * rng.standard_normal(n) if cplx else 0.0)
-            e = _spmv_host(rp, ci, val, v)
-            extra.append(e * (np.linalg.norm(b) / np.linalg.norm(e)))
-        b = np.ascontiguousarray(np.concatenate([b] + extra))
+    b1 = b  # the workload's own right-hand side (the CPU path solves it)
+    b = np.ascontiguousarray(np.concatenate(extra_rhs(rp, ci, val, b, K)))
     # device-resident inputs
     val_d = torch.from_numpy(val).to(dev)
     b_d = torch.from_numpy(b).to(dev)
@@ -292,8 +367,8 @@ def run_ours(args):
     def step_device():
         h.update_values_device(val_d.data_ptr())
         if K == 1:
-            return h.solve_device(meth, b_d.data_ptr(), x_d.data_ptr(), conv=TOL, max_ite=20000)
-        ok_m, it_m, _ = h.solve_multi_device(meth, K, b_d.data_ptr(), x_d.data_ptr(), conv=TOL, max_ite=20000)
+            return h.solve_device(meth, b_d.data_ptr(), x_d.data_ptr(), conv=TOL, max_ite=MAXIT)
+        ok_m, it_m, _ = h.solve_multi_device(meth, K, b_d.data_ptr(), x_d.data_ptr(), conv=TOL, max_ite=MAXIT)
         multi_iters[:] = it_m.tolist()
         return ok_m
 
@@ -302,8 +377,8 @@ def run_ours(args):
         xh = x_h.numpy()
         xh[:] = 0.0
         if K == 1:
-            return h.solve(meth, b_h.numpy(), xh, conv=TOL, max_ite=20000)
-        return h.solve_multi(meth, b_h.numpy().reshape(K, n), xh.reshape(K, n), conv=TOL, max_ite=20000)[0]
+            return h.solve(meth, b_h.numpy(), xh, conv=TOL, max_ite=MAXIT)
+        return h.solve_multi(meth, b_h.numpy().reshape(K, n), xh.reshape(K, n), conv=TOL, max_ite=MAXIT)[0]
 
     for _ in range(args.warmup):
         ok = step_device()
@@ -349,7 +424,8 @@ def run_ours(args):
     f1.record(stream)
     barrier()
     ms_e2e = f0.elapsed_time(f1)
-    xs = x_h.numpy().reshape(K, n)
+    gpu_log = h.residual_log()
+    xs = x_h.numpy().reshape(K, n).copy()
     bs = b.reshape(K, n)
     true_res = max(float(np.linalg.norm(bs[j] - _spmv_host(rp, ci, val, xs[j])) / np.linalg.norm(bs[j]))
                    for j in range(K))
@@ -364,23 +440,18 @@ def run_ours(args):
     dms, dlaunch, dbytes = stats[dom]
     achieved = (dbytes / dlaunch) / (dms / dlaunch / 1e3) / 1e9 if dlaunch else 0.0
     peak, peak_kind = peaks()
-    if rank != 0:
-        torch.distributed.destroy_process_group()
-        return
+    modes = ["automatic", "sync-free", "one-cluster", "one-cluster neighbour-synchronised", "one-cluster push"]
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
         "dtype": ("c128" if cplx else "f64") + ("+fp32-inner" if args.precision == "mixed" else ""),
         "data": "synthetic (seeded voxel generator)",
-        "config": {"workload": label, "n": n, "nnz": nnz, "method": mname, "alpha": ALPHA, "tolerance": TOL,
-                   "precision": args.precision, "right_hand_sides": K,
-                   "iterations": iters, "parallelism": "replicas only" if ws > 1 else "single GPU",
-                   "factor": "recomputed every step",
-                   "sweep_mode": ["automatic", "sync-free", "one-cluster", "one-cluster neighbour-synchronised"][
-                       args.sweep_mode] if tuned is None else "autotuned: %s" % json.dumps(tuned), "level_schedule": "computed once per sparsity pattern",
-                   "l2": "inputs larger than L2 (matrix %.0f MB)" % ((12.0 * nnz) / 1e6),
-                   "true_relative_residual": true_res},
+        "config": workload_config(label, n, nnz, mname, args.precision, K),
+        "solver": {"iterations": iters, "true_relative_residual": true_res,
+                   "parallelism": "replicas only" if ws > 1 else "single GPU",
+                   "sweep_mode": modes[args.sweep_mode] if tuned is None else "autotuned: %s" % json.dumps(tuned),
+                   "level_schedule": "computed once per sparsity pattern"},
         "time_to_tolerance_s": ms_max / args.steps / 1e3,
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
                        "steps": len(step_ms)},
@@ -391,27 +462,137 @@ def run_ours(args):
                      "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_kind == "measured" else "fallback 6.8 TB/s",
                      "traffic": None if K > 1 else NCU_TRAFFIC.get((args.workload, args.precision,
-                                                 {1: "sync-free", 3: "neighbour"}.get(
+                                                 {1: "sync-free", 3: "neighbour", 4: "push"}.get(
                                                      tuned["mode"] if tuned else args.sweep_mode, "cluster"), dom)),
                      "traffic_source": "ncu capture in profiles/ (per launch)", "algorithmic_bytes": dbytes / max(dlaunch, 1),
                      "launch_ms": dms / max(dlaunch, 1), "launches": dlaunch},
         "kernel_ms_per_step": {k: v[0] / args.steps for k, v in stats.items()},
         "clocks": clk, "host_s": t_host,
     }
-    if not args.no_cpu_baseline and ws == 1:
-        from oracle.oracle import Reference, build
-        build()
-        use_ref = Reference.available()
-        it1 = iters if K == 1 else iters[0]
-        sec, ts, ti, cores = cpu_time_sample(rp, ci, val, b1, args.method, pt, CPU_SAMPLE_ITERS, it1, use_ref)
-        line["cpu_baseline"] = {
-            "value": 1.0 / sec, "unit": "solves/s", "cores": cores,
-            "kind": "reference" if use_ref else "port",
-            "sample": "IC(0) factorisation (%.2f s) + %d iterations (%.3f s each), scaled to %d iterations"
-                      % (ts, CPU_SAMPLE_ITERS, ti, it1)}
+    if rank != 0:
+        h.close()
+        torch.distributed.destroy_process_group()
+        return
+    if ws == 1:
+        line["new_pattern"] = new_pattern_solve(local, meth, pt, rp, ci, val, b1)
+        ref = None
+        if not args.no_cpu_baseline:
+            ref = cpu_baseline(line, rp, ci, val, b1, args.method, pt, args.cpu_threads)
+            line["parity"] = parity_summary(rp, ci, val, b1, xs[0], iters if K == 1 else iters[0], gpu_log, ref)
+        if not args.no_mixed and K == 1 and args.method != "sgs" and args.precision == "fp64":
+            line["mixed"] = mixed_vs_fp64(h, o, step_device, stream, dev, x_d, args, ms_max / args.steps,
+                                          rp, ci, val, b1, xs[0], ref)
+        if not args.no_serving and args.workload == "cfg2" and K == 1:
+            line["serving"] = serving_measure(local, args.requests, args.slots, args.share, None, warm_runs=1,
+                                              sweep=False)
+    h.close()
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def new_pattern_solve(device, meth, pt, rp, ci, val, b):
+    """The first solve of a sparsity pattern the library has not seen, through
+    the C ABI with host buffers: upload, pattern analysis (triangles, level
+    schedules, sweep plans), factor and iterations, on a second handle once
+    this process's CUDA modules are loaded; then the same solve again."""
+    from sparsesolv_gb300 import _capi
+    h2 = _capi.Handle(device)
+    o2 = h2.default_options()
+    o2.accel_factor = ALPHA
+    o2.precondition_type = pt
+    h2.set_options(o2)
+    x = np.zeros_like(b)
+    t0 = time.perf_counter()
+    h2.set_matrix(rp, ci, val)
+    ok = h2.solve(meth, np.ascontiguousarray(b), x, conv=TOL, max_ite=MAXIT)
+    first = time.perf_counter() - t0
+    x[:] = 0.0
+    t0 = time.perf_counter()
+    h2.solve(meth, np.ascontiguousarray(b), x, conv=TOL, max_ite=MAXIT)
+    again = time.perf_counter() - t0
+    h2.close()
+    return {"first_solve_s": first, "same_pattern_again_s": again, "converged": bool(ok),
+            "what": "ssg_set_matrix + ssg_solve with host buffers on a fresh handle: upload, pattern analysis, "
+                    "factor, iterations; then the same solve again (pattern and factor cached)"}
+
+
+def cpu_baseline(line, rp, ci, val, b, method, pt, cpu_threads):
+    """A bounded sample of the CPU path (one full solve on all host cores, one
+    on a single thread when the first took under 15 s); returns the all-core
+    result, whose x also serves as the FP64 oracle solution for the parity and
+    mixed-precision error figures."""
+    cpu = CpuPath(method, pt)
+    threads = cpu_threads or os.cpu_count() or 1
+    res, total, setup = cpu.solve(rp, ci, val, b, threads)
+    if setup is None:
+        setup = cpu.setup_seconds(rp, ci, val, b, threads)
+    entry = {"value": 1.0 / total, "unit": "solves/s", "cores": threads, "kind": cpu.kind,
+             "sample": "one full solve to %g (factorisation %.2f s + %d iterations, %.1f ms each) on %d threads%s"
+                       % (TOL, setup, res.iters, 1e3 * (total - setup) / max(res.iters, 1), threads,
+                          "" if cpu.use_ref else ", the oracle's C restatement of the reference"),
+             "phases": phases(res, total, setup), "host": host_info()}
+    if total < 15.0 and threads > 1:
+        r1, t1, s1 = cpu.solve(rp, ci, val, b, 1)
+        if s1 is None:
+            s1 = cpu.setup_seconds(rp, ci, val, b, 1)
+        entry["one_thread"] = dict(phases(r1, t1, s1), solves_per_s=1.0 / t1)
+    line["cpu_baseline"] = entry
+    return res
+
+
+def parity_summary(rp, ci, val, b, x, iters, gpu_log, ref):
+    """The bench solve against the FP64 oracle solve of the same method, shift and
+    right-hand side: iteration counts, residual-log prefix, distance of x."""
+    k = min(len(gpu_log), len(ref.log), 40)
+    lg = np.asarray(gpu_log[:k])
+    rl = np.asarray(ref.log[:k])
+    A_dx = _spmv_host(rp, ci, val, x - ref.x)
+    return {"oracle": "FP64 oracle solve of the same system, method, shift and tolerance (cpu_baseline's solve)",
+            "oracle_iterations": int(ref.iters), "gpu_iterations": int(iters),
+            "iterations_rel_diff": abs(int(iters) - int(ref.iters)) / max(int(ref.iters), 1),
+            "log_prefix_entries": int(k),
+            "log_prefix_max_rel_diff": float(np.max(np.abs(lg - rl) / np.abs(rl))) if k else None,
+            "x_rel_diff": float(np.linalg.norm(x - ref.x) / np.linalg.norm(ref.x)),
+            "A_dx_over_b": float(np.linalg.norm(A_dx) / np.linalg.norm(b))}
+
+
+def mixed_vs_fp64(h, o, step_device, stream, dev, x_d, args, fp64_ms, rp, ci, val, b, x64, ref):
+    """The same solve in mixed precision (FP32 inner ICCG / IC-MRTR inside FP64
+    refinement on the true residual) on the same handle and matrix."""
+    import torch
+    from sparsesolv_gb300 import _capi
+    o.precision = _capi.PREC_MIXED
+    h.set_options(o)
+    try:
+        for _ in range(2):
+            ok = step_device()
+        M = max(3, args.steps // 4)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(M):
+            ok = step_device() and ok
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / M
+        inner = h.iters()
+        outer = len(h.residual_log()) - 1
+        xm = x_d.cpu().numpy()[:len(b)].copy()
+    finally:
+        o.precision = _capi.PREC_FP64
+        h.set_options(o)
+    nb = np.linalg.norm(b)
+    out = {"time_to_tolerance_s": ms / 1e3, "solves_per_s": 1e3 / ms, "steps": M, "converged": bool(ok),
+           "speedup_vs_fp64": fp64_ms / ms, "inner_iterations": int(inner), "refinement_steps": int(outer),
+           "true_relative_residual": float(np.linalg.norm(b - _spmv_host(rp, ci, val, xm)) / nb),
+           "vs_gpu_fp64": {"x_rel_diff": float(np.linalg.norm(xm - x64) / np.linalg.norm(x64)),
+                           "A_dx_over_b": float(np.linalg.norm(_spmv_host(rp, ci, val, xm - x64)) / nb)}}
+    if ref is not None:
+        out["vs_fp64_oracle"] = {"x_rel_diff": float(np.linalg.norm(xm - ref.x) / np.linalg.norm(ref.x)),
+                                 "A_dx_over_b": float(np.linalg.norm(_spmv_host(rp, ci, val, xm - ref.x)) / nb)}
+    return out
 
 
 def run_batch(args):
@@ -440,11 +621,11 @@ def run_batch(args):
     inst = sum(len(B) for _, _, _, B in systems)
     tuned = bt.autotune() if args.autotune else None
     t0 = time.perf_counter()
-    bt.start(_capi.METHOD_ICCG, ALPHA, conv=TOL, max_ite=20000)
+    bt.start(_capi.METHOD_ICCG, ALPHA, conv=TOL, max_ite=MAXIT)
     bt.wait()
     t_first = time.perf_counter() - t0
     for _ in range(max(0, args.warmup - 1)):
-        bt.start(_capi.METHOD_ICCG, ALPHA, conv=TOL, max_ite=20000)
+        bt.start(_capi.METHOD_ICCG, ALPHA, conv=TOL, max_ite=MAXIT)
         bt.wait()
     stream = torch.cuda.ExternalStream(bt.stream(), device=dev)
 
@@ -460,7 +641,7 @@ def run_batch(args):
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     ev[0].record(stream)
     for k in range(args.steps):
-        bt.start(_capi.METHOD_ICCG, ALPHA, conv=TOL, max_ite=20000)
+        bt.start(_capi.METHOD_ICCG, ALPHA, conv=TOL, max_ite=MAXIT)
         bt.wait()
         ev[k + 1].record(stream)
     barrier()
@@ -469,7 +650,7 @@ def run_batch(args):
     launches = bt.lib.ssg_launch_count() - launches0
     clk = clocks.stop()
     bt.set_profiling(True)
-    bt.start(_capi.METHOD_ICCG, ALPHA, conv=TOL, max_ite=20000)
+    bt.start(_capi.METHOD_ICCG, ALPHA, conv=TOL, max_ite=MAXIT)
     bt.wait()
     stats = bt.kernel_stats()
     bt.set_profiling(False)
@@ -486,7 +667,7 @@ def run_batch(args):
         for k, (_, _, _, B) in enumerate(systems):
             bt.set_rhs(k, B)
             h2d += B.nbytes
-        bt.start(_capi.METHOD_ICCG, ALPHA, conv=TOL, max_ite=20000)
+        bt.start(_capi.METHOD_ICCG, ALPHA, conv=TOL, max_ite=MAXIT)
         bt.wait()
         for k in range(len(systems)):
             X = bt.result(k)[0]
@@ -511,7 +692,7 @@ def run_batch(args):
             x = np.zeros_like(B[j])
             torch.cuda.synchronize(dev)
             t0 = time.perf_counter()
-            h.solve(_capi.METHOD_ICCG, np.ascontiguousarray(B[j]), x, conv=TOL, max_ite=20000)
+            h.solve(_capi.METHOD_ICCG, np.ascontiguousarray(B[j]), x, conv=TOL, max_ite=MAXIT)
             t_seq += time.perf_counter() - t0
             n_seq += 1
     h.close()
@@ -548,23 +729,21 @@ def run_batch(args):
         torch.distributed.destroy_process_group()
 
 
-def run_serving(args):
+def serving_measure(local, requests, slots, share, precision, warm_runs=1, sweep=True):
     """Serving stream: requests log-uniform over 1k-500k unknowns, 70% real
-    ICCG / 30% complex IC-MRTR, continuous batching in mixed precision to 1e-8.
-    value = solves/s with every request queued at t = 0 (saturation); the rate
-    sweep replays the same requests as Poisson arrivals at fractions of that
-    rate and reports p50/p99 latency. The plain FP64 GPU path solves the same
+    ICCG / 30% complex IC-MRTR, continuous batching to 1e-8 (mixed precision
+    for real requests, FP64 for complex ones unless precision says fp64 for
+    all). solves/s and p50/p99 latency with every request queued at t = 0
+    (saturation); with sweep, the same requests again as Poisson arrivals at
+    1/4, 1/2 and 1 x that rate. The plain FP64 GPU path solves the same
     requests one after another through a handle."""
     import torch
+    import scipy.sparse as sp
     from sparsesolv_gb300 import _capi, serving
-    ws, rank, local = dist_env()
-    if rank != 0:
-        return  # one GPU serves the stream; replicas would split it by request
     torch.cuda.set_device(local)
-    base = serving.synthetic_stream(args.requests, rate=0.0, seed=11)
+    base = serving.synthetic_stream(requests, rate=0.0, seed=11)
     kinds = [r.kind for r in base]
-    # mixed: per kind (real ICCG mixed, complex IC-MRTR FP64, see serving.GpuBackend); fp64: everything FP64
-    be = serving.GpuBackend(local, precision=None if args.precision != "fp64" else _capi.PREC_FP64)
+    be = serving.GpuBackend(local, precision=None if precision != "fp64" else _capi.PREC_FP64)
 
     def fresh(rate, seed):
         rng = np.random.default_rng(seed)
@@ -576,29 +755,32 @@ def run_serving(args):
         return out
 
     def check(reqs):
-        import scipy.sparse as sp
         worst = 0.0
         for r in reqs:
             A = sp.csr_matrix((r.val, r.col, r.row_ptr))
             worst = max(worst, float(np.linalg.norm(r.b - A @ r.x) / np.linalg.norm(r.b)))
         return worst
 
-    ns = [int(v) for v in args.slots.split(",")]
+    ns = [int(v) for v in slots.split(",")]
     srv = serving.Server(be, serving.ServerConfig(slots={serving.KIND_REAL_ICCG: ns[0],
-                                                        serving.KIND_COMPLEX_MRTR: ns[1]}, share=args.share))
-    for _ in range(max(1, args.warmup - 2)):  # warm the slots (buffers, modules)
+                                                        serving.KIND_COMPLEX_MRTR: ns[1]}, share=share))
+    for _ in range(max(1, warm_runs)):  # warm the slots (buffers, modules)
         srv.run(fresh(0.0, 0))
+    clocks = Clocks(local)
+    clocks.start()
     sat = srv.run(fresh(0.0, 0))
+    clk = clocks.stop()
     st_sat = serving.latency_stats(sat)
     worst = check(sat)
-    sweep = []
-    for frac in (0.25, 0.5, 1.0):
-        rate = frac * st_sat["solves_per_s"]
-        reqs = srv.run(fresh(rate, 1 + int(frac * 100)))
-        st = serving.latency_stats(reqs)
-        st["arrival_rate"] = rate
-        sweep.append(st)
-        worst = max(worst, check(reqs))
+    rates = []
+    if sweep:
+        for frac in (0.25, 0.5, 1.0):
+            rate = frac * st_sat["solves_per_s"]
+            reqs = srv.run(fresh(rate, 1 + int(frac * 100)))
+            st = serving.latency_stats(reqs)
+            st["arrival_rate"] = rate
+            rates.append(st)
+            worst = max(worst, check(reqs))
     srv.close()
     # plain FP64 GPU path: one request after another through a handle
     h = _capi.Handle(local)
@@ -614,30 +796,49 @@ def run_serving(args):
         h.set_matrix(r.row_ptr, r.col, r.val)
         x = np.zeros_like(r.b)
         meth = _capi.METHOD_ICCG if r.kind == serving.KIND_REAL_ICCG else _capi.METHOD_MRTR
-        h.solve(meth, np.ascontiguousarray(r.b), x, conv=TOL, max_ite=20000)
+        h.solve(meth, np.ascontiguousarray(r.b), x, conv=TOL, max_ite=MAXIT)
         plain_lat.append(time.perf_counter() - t1)
     t_plain = time.perf_counter() - t0
     h.close()
     plain_rate = len(base) / t_plain
+    out = {"workload": "request stream, sizes log-uniform 1k-500k unknowns, 70% real curl-curl ICCG, "
+                       "30% complex eddy-current IC-MRTR, all queued at t = 0",
+           "requests": len(base), "real": kinds.count(serving.KIND_REAL_ICCG),
+           "complex": kinds.count(serving.KIND_COMPLEX_MRTR), "rows": int(sum(r.n for r in base)),
+           "precision": ("real ICCG mixed, complex IC-MRTR fp64" if precision != "fp64" else "fp64"),
+           "slots": {k: v for k, v in srv.cfg.slots.items()}, "share": share,
+           "solves_per_s": st_sat["solves_per_s"], "p50_ms": st_sat["p50_ms"], "p99_ms": st_sat["p99_ms"],
+           "worst_true_relative_residual": worst,
+           "plain_gpu_sequential": {"solves_per_s": plain_rate,
+                                    "p50_ms": float(np.percentile(plain_lat, 50) * 1e3),
+                                    "p99_ms": float(np.percentile(plain_lat, 99) * 1e3)},
+           "ratio_vs_plain": st_sat["solves_per_s"] / plain_rate, "clocks": clk}
+    if sweep:
+        out["rate_sweep"] = rates
+    return out
+
+
+def run_serving(args):
+    """The serving stream as its own bench line (--workload cfg5)."""
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return  # one GPU serves the stream; replicas would split it by request
+    m = serving_measure(local, args.requests, args.slots, args.share, args.precision,
+                        warm_runs=max(1, args.warmup - 2), sweep=True)
     line = {
-        "metric": "serving solves/s at saturation, p50/p99 latency (ms) over a rate sweep", "value": st_sat["solves_per_s"],
-        "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": args.warmup, "higher_is_better": True,
-        "scaling": "strong", "vs_baseline": None,
+        "metric": "serving solves/s at saturation, p50/p99 latency (ms) over a rate sweep",
+        "value": m["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": args.warmup,
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
         "dtype": "f64/c128" + ("+fp32-inner" if args.precision != "fp64" else ""),
         "data": "synthetic (seeded voxel generator)",
-        "config": {"workload": "request stream, sizes log-uniform 1k-500k unknowns, 70% real curl-curl ICCG, "
-                               "30% complex eddy-current IC-MRTR", "requests": len(base),
-                   "real": kinds.count(serving.KIND_REAL_ICCG), "complex": kinds.count(serving.KIND_COMPLEX_MRTR),
-                   "rows": int(sum(r.n for r in base)), "tolerance": TOL, "alpha": 1.1,
-                   "precision": ("real ICCG mixed, complex IC-MRTR fp64" if args.precision != "fp64" else "fp64"),
-                   "slots": {k: v for k, v in srv.cfg.slots.items()}, "share": args.share,
-                   "worst_true_relative_residual": worst},
-        "latency_ms": {"p50": st_sat["p50_ms"], "p99": st_sat["p99_ms"]},
-        "rate_sweep": sweep,
-        "plain_gpu_sequential": {"value": plain_rate, "unit": "solves/s",
-                                 "p50_ms": float(np.percentile(plain_lat, 50) * 1e3),
-                                 "p99_ms": float(np.percentile(plain_lat, 99) * 1e3),
-                                 "ratio": st_sat["solves_per_s"] / plain_rate},
+        "config": {"workload": m["workload"], "requests": m["requests"], "real": m["real"],
+                   "complex": m["complex"], "rows": m["rows"], "tolerance": TOL, "alpha": 1.1,
+                   "precision": m["precision"], "slots": m["slots"], "share": m["share"],
+                   "worst_true_relative_residual": m["worst_true_relative_residual"]},
+        "latency_ms": {"p50": m["p50_ms"], "p99": m["p99_ms"]},
+        "rate_sweep": m["rate_sweep"],
+        "plain_gpu_sequential": dict(m["plain_gpu_sequential"], ratio=m["ratio_vs_plain"]),
+        "clocks": m["clocks"],
     }
     print(json.dumps(line), flush=True)
 

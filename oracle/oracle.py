@@ -119,6 +119,16 @@ class Oracle(_Base):
         """Host threads of the row-parallel SpMV (1 when built without OpenMP)."""
         return int(self.lib.or_threads())
 
+    def set_threads(self, k):
+        """Threads of the row-parallel SpMV for the following solves."""
+        self.lib.or_set_threads(ctypes.c_int(int(k)))
+
+    def last_timings(self):
+        """Seconds of the last solve: (set-up incl. the IC factor, iterations, total)."""
+        t = np.zeros(3)
+        self.lib.or_last_timings(_p(t))
+        return float(t[0]), float(t[1]), float(t[2])
+
     def solve(self, method, rp, ci, val, b, settings=None, x0=None, normB=None, conv=1e-8, maxit=10000):
         """method: 'iccg' or 'mrtr' (settings.precondition_type picks IC=0 / SGS=1)."""
         s = settings or Settings()

@@ -464,6 +464,8 @@ done_early:
 int FN(or_solve)(const or_opts *o, int method, int n, const int *rp, const int *ci, const T *va,
                  const T *b, double normB, double conv_cri, int max_ite, T *x,
                  double *log, int log_cap, int *log_len, int *iters) {
+    const double t_start = or_now();
+    double t_iter = t_start;
     or_csr A = {n, (int *)rp, (int *)ci};
     FN(logger) lg = {o, log, log_cap, 0};
     int rc = 0;
@@ -496,6 +498,7 @@ int FN(or_solve)(const or_opts *o, int method, int n, const int *rp, const int *
         T *vu = (T *)malloc(sizeof(T) * (size_t)(Uc.rp[n] + 1));
         or_gather_values(&Lc, vA, sizeof(T), vl);
         or_gather_values(&Uc, vA, sizeof(T), vu);
+        t_iter = or_now();
         rc = FN(sgs_mrtr_main)(o, &lg, &A, vA, &Lc, vl, &Uc, vu, normB, conv_cri, max_ite, bb, x, iters);
         or_free(&Lc); or_free(&Uc); free(vl); free(vu);
     } else {
@@ -509,6 +512,7 @@ int FN(or_solve)(const or_opts *o, int method, int n, const int *rp, const int *
         if (or_transpose(&L, &Lt)) { rc = -1; free(D); free(vl); goto out; }
         vlt = (T *)malloc(sizeof(T) * (size_t)(Lt.rp[n] + 1));
         or_permute_values(&Lt, vl, sizeof(T), vlt);
+        t_iter = or_now();
         if (method == 0)
             rc = FN(iccg_main)(o, &lg, &A, vA, &L, vl, &Lt, vlt, D, normB, conv_cri, max_ite, bb, x, iters);
         else
@@ -520,6 +524,12 @@ int FN(or_solve)(const or_opts *o, int method, int n, const int *rp, const int *
 out:
     free(d); free(bs); free(vs);
     *log_len = lg.log_len;
+    {
+        const double t_end = or_now();
+        or_timing[0] = t_iter - t_start;
+        or_timing[1] = t_end - t_iter;
+        or_timing[2] = t_end - t_start;
+    }
     return rc;
 }
 

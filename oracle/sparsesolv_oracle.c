@@ -23,6 +23,7 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -34,6 +35,27 @@ int or_threads(void) {
 #else
     return 1;
 #endif
+}
+
+/* threads of the row-parallel SpMV for the following solves (no effect without OpenMP) */
+void or_set_threads(int k) {
+#ifdef _OPENMP
+    if (k > 0) omp_set_num_threads(k);
+#else
+    (void)k;
+#endif
+}
+
+/* wall time of the last or_solve call: [0] set-up before the iterations (scaling,
+ * lower triangle, IC factor, transpose), [1] the iterations, [2] the whole call */
+static double or_timing[3];
+static double or_now(void) {
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
+void or_last_timings(double *out) {
+    for (int k = 0; k < 3; ++k) out[k] = or_timing[k];
 }
 
 typedef struct {
