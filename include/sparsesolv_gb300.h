@@ -215,8 +215,11 @@ long long ssg_launch_count(void);
 #define SSG_TUNE_SWEEP_BACKOFF_NS 2  /* sleep between polls of an unsolved entry */
 #define SSG_TUNE_FACTOR_BACKOFF_NS 3 /* sleep between polls of an unfinished factor row */
 #define SSG_TUNE_RECIPROCAL_DIAG 4   /* 1 (default): multiply by precomputed 1/diagonal in the sweeps */
-#define SSG_TUNE_SWEEP_MODE 5        /* 0 auto (default: cluster when its plan fits), 1 sync-free, 2 one-cluster level-synchronous,
-                                        3 one-cluster neighbour-synchronised (IC sweeps; others as 2) */
+#define SSG_TUNE_SWEEP_MODE 5        /* 0 auto (default: for real values the push sweep, else the one-cluster
+                                        sweep, where their plans fit), 1 sync-free, 2 one-cluster level-synchronous,
+                                        3 one-cluster neighbour-synchronised (IC sweeps; others as 2), 4 one-cluster
+                                        push: no cluster-wide barrier, each value pushed to the CTAs that read it,
+                                        rows summed in dependency-level order (IC sweeps; others as 2) */
 #define SSG_TUNE_CLUSTER_RING_KB 6   /* distributed shared-memory ring per CTA of the cluster sweep (KB) */
 #define SSG_TUNE_CLUSTER_GROUP 7     /* lanes per row in the cluster sweep: 4 (default), 8, 16, 32 */
 #define SSG_TUNE_SPMV_GROUP 9        /* lanes per row in the SpMV: 0 (default: about 8 entries a lane for real

@@ -41,6 +41,8 @@ CUDA_SOURCES = [
     "ss_batch.cu",
     "ss_build.cu",
     "ss_post.cu",
+    "ss_push.cu",
+    "ss_push_plan.cpp",
     "ss_capi.cu",
 ]
 
@@ -74,7 +76,7 @@ def build_voxel(force=False):
 def build_solver(force=False, verbose=False):
     """Compile the CUDA library for sm_103a (cross-compiles without a GPU)."""
     srcs = [os.path.join(CSRC, s) for s in CUDA_SOURCES]
-    hdrs = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
+    hdrs = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h", ".hpp"))]
     hdrs.append(os.path.join(INCLUDE, "sparsesolv_gb300.h"))
     if not force and _newer(SOLVER_LIB, srcs + hdrs):
         return SOLVER_LIB

@@ -382,7 +382,7 @@ int ssg_set_tuning(ssg_handle hd, int key, int value) {
                 h.use_inv_diag = value != 0;
                 break;
             case SSG_TUNE_SWEEP_MODE:
-                if (value < 0 || value > 3) return SSG_ERR_ARG;
+                if (value < 0 || value > 4) return SSG_ERR_ARG;
                 h.sweep_mode = value;
                 break;
             case SSG_TUNE_CLUSTER_RING_KB:

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "ss_common.cuh"
+#include "ss_push_plan.hpp"
 
 namespace ssg {
 
@@ -60,6 +61,23 @@ struct DBuf {
     U *as() const { return (U *)p; }
 };
 
+// ---------------------------------------------------------------- push sweep plan (ss_push.cu)
+// One-cluster push schedule of a level-ordered triangle (ss_push_plan.hpp): every
+// CTA owns a contiguous chunk of each level, sums each row's entries oldest
+// dependency first, and pushes each finished value into the shared memory of the
+// CTAs that read it, so no barrier spans the cluster per level.
+struct PushPlan {
+    bool ready = false;
+    int fail = 0;                 // value sizes found infeasible (bit 0: 4 bytes, 1: 8, 2: 16)
+    int elem = 0, C = 0, nent = 0, npush = 0;
+    PushLayout lay{};
+    DBuf tab;                     // per (level, CTA) int4 {record offset / 16, record bytes / 16, bytes received, 0}
+    DBuf rec;                     // the level records; values refilled per factor and per sweep
+    DBuf vmap, dval, dlv, drhs, perm;  // where the factor's values, 1/diagonal or D, and the rhs go in rec
+    const void *key_val = nullptr, *key_lv = nullptr;
+    unsigned long long key_epoch = ~0ull;
+};
+
 // ---------------------------------------------------------------- level-scheduled triangle
 // One triangular factor in the layout the sweeps stream: rows in level order
 // (level, then row id), each row's entries contiguous and in the original
@@ -79,6 +97,7 @@ struct Tri {
     int cl_C = 0, cl_S = 0, cl_elem = 0, cl_ring_bytes = 0, cl_cap_r = 0, cl_cap_e = 0;
     DBuf cl_code;                // per level-ordered entry: row id, or -1 - (owner << 20 | ring slot)
     DBuf cl_tab;                 // per (level, CTA): rows [rs, re) and entries [e0, e1) of the chunk
+    PushPlan push;               // push sweep plan (ss_push.cu)
 };
 
 // ss_levels.cu
@@ -154,6 +173,15 @@ struct KState;
 template <typename T>
 void sweep_cluster(const Tri &tri, const T *val, int mode, const T *rhs, const T *aux, const T *lvec, T *out, T *out2,
                    const KState *st, int group, int *err, cudaStream_t s);
+
+// ss_push.cu: one-cluster push sweeps (IC pair: SW_FWD_DIV with lvec = 1/diagonal, SW_BWD_IC with lvec = D)
+// plan once per pattern and value size; false when the schedule does not fit (then another sweep serves)
+bool push_plan(Tri &T, size_t elem_bytes, cudaStream_t s);
+// val: the triangle's values in its level-ordered layout, lvec: per level-ordered row; epoch changes whenever
+// the values behind val / lvec change (the records are refilled then)
+template <typename T>
+void sweep_push(Tri &tri, const T *val, int mode, const T *rhs, const T *lvec, unsigned long long epoch, T *out,
+                const KState *st, int *err, cudaStream_t s);
 
 // ss_spmv_vec.cu -- see the Krylov state there
 struct KState;

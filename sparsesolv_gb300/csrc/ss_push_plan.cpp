@@ -1,0 +1,293 @@
+// ss_push_plan.cpp -- the push sweep's schedule (see ss_push.cu for the kernel).
+//
+// Partition: CTA c owns the c-th contiguous chunk of every level (rows in level
+// order, then row id), as the lockstep cluster sweep does. Each row's
+// off-diagonal entries are sorted by (dependency level, column); the entries of
+// the level just before the row's are the row's "new" part, summed after the
+// wait, the others its "old" part, summed a level early.
+//
+// Per entry of row t (level lt, owner c) reading row j (level lj, owner cj,
+// production index oj within cj):
+//   cj == c and slot oj % S_own not reused before the end of level lt: own ring;
+//   cj != c and lt - lj <= LEAD + 1: the receive ring (j is pushed to c);
+//   otherwise: the output vector in memory (cj == c: stored by this CTA at an
+//   earlier step; cj != c: the producer's progress, acquired by the LEAD check,
+//   covers the store).
+// New entries must come from shared memory, else the plan is infeasible.
+// Receive slots are assigned per consumer in (producer level, producer
+// position) order around the ring; a slot is reused only by a value pushed at a
+// level at least LEAD + 1 after the consumer's last read of the previous one, so
+// the LEAD bound orders the read first.
+#include "ss_push_plan.hpp"
+
+#include <algorithm>
+
+namespace ssg {
+
+PushLayout push_layout(int S_own, int S_recv, int cap_rec, int elem, int NB) {
+    PushLayout L{};
+    L.S_own = S_own;
+    L.S_recv = S_recv;
+    L.R = PS_R;
+    L.NB = NB;
+    L.LEAD = PS_LEAD;
+    L.cap_rec = cap_rec;
+    int o = 0;
+    L.o_x = o;
+    o += ps_al16((S_own + S_recv) * elem);
+    L.o_base = o;  // partial sums handed from the older-entry group to the newest-entry group, two levels
+    o += ps_al16(2 * PS_MAXQ * PS_CT * elem);
+    L.o_mbr = o;
+    o += ps_al16(8 * L.R);
+    L.o_mbs = o;
+    o += ps_al16(8 * NB);
+    L.o_prog = o;
+    o += 16;
+    L.o_tabring = o;  // two rings of 4 table entries (16 bytes each)
+    o += 128;
+    L.o_buf = o;
+    o += NB * ps_al16(cap_rec);
+    L.total = o;
+    return L;
+}
+
+static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *prp, const int *pci,
+                                  const int *perm, const int *level, const int *ipos, int C, int elem, int S_own,
+                                  int NB) {
+    PushPlanHost P;
+    auto fail = [&](const char *why) {
+        P.ok = false;
+        P.why = why;
+        return P;
+    };
+    if (C <= 0 || n <= 0 || nlev < 2) return fail("no cluster, no rows or a single level");
+    if (C > 64) return fail("cluster too large");
+    const int LEAD = PS_LEAD;
+    auto chunk_of = [&](int l, int c, int &rs, int &re) {
+        const int L0 = lptr[l], L1 = lptr[l + 1];
+        const int chunk = (L1 - L0 + C - 1) / C;
+        rs = std::min(L0 + c * chunk, L1);
+        re = std::min(rs + chunk, L1);
+    };
+    // partition and production order
+    std::vector<unsigned char> owner(n);
+    std::vector<int> ordc(n);
+    std::vector<std::vector<int>> levof(C);  // level of each production index, per CTA
+    int cap_r = 1;
+    for (int l = 0; l < nlev; ++l)
+        for (int c = 0; c < C; ++c) {
+            int rs, re;
+            chunk_of(l, c, rs, re);
+            cap_r = std::max(cap_r, re - rs);
+            for (int t = rs; t < re; ++t) {
+                owner[t] = (unsigned char)c;
+                ordc[t] = (int)levof[c].size();
+                levof[c].push_back(l);
+            }
+        }
+    if (cap_r > PS_CT * PS_MAXQ) return fail("a level chunk has more rows than the CTA holds");
+    if (2 * cap_r > S_own) return fail("own ring smaller than two levels");
+    // entries (off-diagonal) sorted per row by (dependency level, column)
+    std::vector<int> sprp(n + 1, 0), nsp(n, 0), &vmap = P.vmap;
+    vmap.reserve(prp[n]);
+    std::vector<int> dep;
+    dep.reserve(prp[n]);
+    std::vector<std::pair<long long, int>> row;  // (level << 32 | column, entry)
+    for (int t = 0; t < n; ++t) {
+        const int i = perm[t], lt = level[i];
+        row.clear();
+        for (int k = prp[t]; k < prp[t + 1]; ++k) {
+            const int j = pci[k];
+            if (j == i) continue;
+            if (j < 0 || j >= n || level[j] >= lt) return fail("an entry is not a dependency of its row");
+            row.push_back({((long long)level[j] << 32) | (unsigned)j, k});
+        }
+        std::sort(row.begin(), row.end());
+        int nold = 0;
+        for (auto &e : row) {
+            if ((int)(e.first >> 32) < lt - 1) ++nold;
+            vmap.push_back(e.second);
+            dep.push_back((int)(e.first & 0xFFFFFFFF));
+        }
+        nsp[t] = nold;
+        sprp[t + 1] = (int)vmap.size();
+        if (sprp[t + 1] - sprp[t] > 0xFFFF) return fail("a row longer than 65535 entries");
+    }
+    const int nent = (int)vmap.size();
+    // codes; reads through the receive ring collected per consumer
+    std::vector<int> code(nent, 0);
+    struct Req {
+        long long key;  // consumer << 58 | producer level << 32 | producer position
+        int entry, use;
+        bool operator<(const Req &o) const { return key < o.key || (key == o.key && entry < o.entry); }
+    };
+    std::vector<Req> reqs;
+    for (int t = 0; t < n; ++t) {
+        const int c = owner[t], lt = level[perm[t]];
+        for (int k = sprp[t]; k < sprp[t + 1]; ++k) {
+            const int j = dep[k], lj = level[j], pj = ipos[j], cj = owner[pj], oj = ordc[pj];
+            const bool newest = (lj == lt - 1);
+            if (cj == c) {
+                const int reuse = oj + S_own;
+                const bool in_ring = reuse >= (int)levof[c].size() || levof[c][reuse] >= lt + 1;
+                if (in_ring) code[k] = -1 - (oj % S_own);
+                else if (!newest) code[k] = j;
+                else return fail("a newest own dependency left the own ring");
+            } else if (lt - lj <= LEAD + 1) {
+                reqs.push_back({((long long)c << 58) | ((long long)lj << 32) | (unsigned)pj, k, lt});
+            } else {
+                code[k] = j;
+            }
+        }
+    }
+    std::sort(reqs.begin(), reqs.end());
+    struct Push {
+        int c, pj, lp, last_use;
+    };
+    std::vector<Push> pushes;
+    std::vector<int> pushof(reqs.size());
+    for (size_t q = 0; q < reqs.size(); ++q) {
+        const long long key = reqs[q].key;
+        const int c = (int)(key >> 58), lp = (int)((key >> 32) & 0x3FFFFFF), pj = (int)(key & 0xFFFFFFFF);
+        if (pushes.empty() || pushes.back().c != c || pushes.back().pj != pj) pushes.push_back({c, pj, lp, reqs[q].use});
+        else pushes.back().last_use = std::max(pushes.back().last_use, reqs[q].use);
+        pushof[q] = (int)pushes.size() - 1;
+    }
+    std::vector<int> pptr(n + 1, 0);
+    for (auto &p : pushes) pptr[p.pj + 1]++;
+    for (int t = 0; t < n; ++t) pptr[t + 1] += pptr[t];
+    // records: per (pass, warp) slab widths; sizes; the largest
+    std::vector<int> K;
+    auto slab_widths = [&](int rs, int re) {
+        const int cnt = re - rs, npass = (cnt + PS_CT - 1) / PS_CT;
+        K.assign((size_t)npass * 4, 0);
+        for (int q = 0; q < cnt; ++q) {
+            const int j = q / PS_CT, w = (q % PS_CT) / 32;
+            K[j * 4 + w] = std::max(K[j * 4 + w], sprp[rs + q + 1] - sprp[rs + q]);
+        }
+        int ne = 0;
+        for (int v : K) ne += 32 * v;
+        return ne;
+    };
+    int cap_rec = 16, cnt_max = 0;
+    for (int l = 0; l < nlev; ++l)
+        for (int c = 0; c < C; ++c) {
+            int rs, re;
+            chunk_of(l, c, rs, re);
+            const int ne = slab_widths(rs, re);
+            const PsRec r = ps_rec((re - rs + PS_CT - 1) / PS_CT, ne, pptr[re] - pptr[rs], elem);
+            cap_rec = std::max(cap_rec, r.size);
+            cnt_max = std::max(cnt_max, re - rs);
+        }
+    // the receive ring takes the shared memory left next to the staged records
+    PushLayout lay = push_layout(S_own, 0, cap_rec, elem, NB);
+    int S_recv = std::min(1 << 16, (PS_SMEM_MAX - lay.total) / elem - 16);
+    S_recv = (S_recv / 64) * 64;
+    if (S_recv < 512) return fail("no shared memory left for the receive ring");
+    lay = push_layout(S_own, S_recv, cap_rec, elem, NB);
+    if (lay.total > PS_SMEM_MAX) return fail("layout exceeds shared memory");
+    // receive slots per consumer, and the reuse proof
+    std::vector<int> slot(pushes.size());
+    {
+        std::vector<int> run(C, 0);
+        std::vector<std::vector<int>> hist(C);
+        for (size_t q = 0; q < pushes.size(); ++q) {
+            const int c = pushes[q].c;
+            const int k = run[c]++;
+            slot[q] = k % S_recv;
+            hist[c].push_back((int)q);
+            if (k >= S_recv) {
+                const Push &old = pushes[hist[c][k - S_recv]];
+                if (old.last_use + 1 > pushes[q].lp - LEAD) return fail("a receive slot is reused too early");
+            }
+        }
+    }
+    for (size_t q = 0; q < reqs.size(); ++q) code[reqs[q].entry] = -1 - (S_own + slot[pushof[q]]);
+    std::vector<int> plist(pushes.size());
+    {
+        std::vector<int> fillp(pptr.begin(), pptr.end() - 1);
+        for (size_t q = 0; q < pushes.size(); ++q) plist[fillp[pushes[q].pj]++] = (pushes[q].c << 24) | slot[q];
+    }
+    std::vector<long long> bin((size_t)nlev * C, 0);
+    for (auto &p : pushes) bin[(size_t)p.lp * C + p.c] += elem;
+    // the records, in (level, CTA) order
+    std::vector<int> &tab = P.tab, &rec = P.rec, &dval = P.dval, &dlv = P.dlv, &drhs = P.drhs;
+    tab.assign((size_t)nlev * C * 4, 0);
+    dval.assign(nent, 0);
+    dlv.assign(n, 0);
+    drhs.assign(n, 0);
+    long long off = 0;
+    for (int l = 0; l < nlev; ++l)
+        for (int c = 0; c < C; ++c) {
+            int rs, re;
+            chunk_of(l, c, rs, re);
+            const int cnt = re - rs, npass = (cnt + PS_CT - 1) / PS_CT, np = pptr[re] - pptr[rs];
+            const int ne = slab_widths(rs, re);
+            const PsRec r = ps_rec(npass, ne, np, elem);
+            if (off + r.size >= (1ll << 31)) return fail("records exceed 2 GB");
+            if (bin[(size_t)l * C + c] >= (1 << 20)) return fail("a level pushes more bytes than a barrier counts");
+            int *tr = &tab[((size_t)l * C + c) * 4];
+            tr[0] = (int)(off / 16);
+            tr[1] = r.size / 16;
+            tr[2] = (int)bin[(size_t)l * C + c];
+            const size_t w0 = (size_t)(off / 4);
+            rec.resize(w0 + r.size / 4, 0);
+            rec[w0 + 0] = cnt;
+            rec[w0 + 1] = ne;
+            rec[w0 + 2] = np;
+            rec[w0 + 3] = npass;
+            const int slots = npass * PS_CT;
+            std::vector<int> slab(npass * 4, 0);  // first entry slot of each (pass, warp) slab
+            for (int i = 0, acc = 0; i < npass * 4; ++i) {
+                slab[i] = acc;
+                acc += 32 * K[i];
+            }
+            int pnext = 0;
+            for (int q = 0; q <= slots; ++q) {
+                int *ri = &rec[w0 + (r.o_info + 16 * q) / 4];
+                ri[3] = pnext;
+                if (q == slots || q >= cnt) {
+                    ri[0] = q == slots ? ne : 0;
+                    ri[1] = 0;
+                    ri[2] = -1;
+                    continue;
+                }
+                const int j = q / PS_CT, w = (q % PS_CT) / 32, lane = q % 32;
+                const int t = rs + q, e0 = sprp[t], len = sprp[t + 1] - e0;
+                const int first = slab[j * 4 + w] + lane;
+                ri[0] = first;
+                ri[1] = nsp[t] | (len << 16);
+                ri[2] = perm[t];
+                for (int k = 0; k < len; ++k) {
+                    rec[w0 + r.o_code / 4 + first + 32 * k] = code[e0 + k];
+                    dval[e0 + k] = (int)((off + r.o_val) / elem) + first + 32 * k;
+                }
+                for (int k = pptr[t]; k < pptr[t + 1]; ++k) rec[w0 + r.o_push / 4 + pnext++] = plist[k];
+                dlv[t] = (int)((off + r.o_lv) / elem) + q;
+                drhs[t] = (int)((off + r.o_rhs) / elem) + q;
+            }
+            off += r.size;
+        }
+    rec.resize(rec.size() + 16, 0);  // a copy never reads past the buffer
+    P.C = C;
+    P.nent = nent;
+    P.npush = (int)pushes.size();
+    P.cnt_max = cnt_max;
+    P.lay = lay;
+    P.ok = true;
+    return P;
+}
+
+PushPlanHost push_plan_host(int n, int nlev, const int *lptr, const int *prp, const int *pci, const int *perm,
+                            const int *level, const int *ipos, int C, int elem) {
+    PushPlanHost best;
+    for (int S_own : {PS_S_OWN, PS_S_OWN / 2, PS_S_OWN / 4, PS_S_OWN / 8})
+        for (int NB = PS_NB; NB >= 3; --NB) {
+            PushPlanHost P = push_plan_try(n, nlev, lptr, prp, pci, perm, level, ipos, C, elem, S_own, NB);
+            if (P.ok) return P;
+            best = std::move(P);
+        }
+    return best;
+}
+
+}  // namespace ssg

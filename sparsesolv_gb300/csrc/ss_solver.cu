@@ -295,6 +295,7 @@ void Handle::ensure_factor(double alpha, bool scaled) {
     D_lev.ensure(sizeof(T) * (size_t)(n + 1));
     gather_values<T>(Lf.perm.as<int>(), invL.as<T>(), invL_lev.as<T>(), n, stream);
     gather_values<T>(Ltb.perm.as<int>(), Dvec.as<T>(), D_lev.as<T>(), n, stream);
+    ++fac_epoch;
     fac_valid = true;
     fac_version = version;
     fac_alpha_req = alpha;
@@ -357,11 +358,30 @@ bool Handle::cluster_ok(Tri &t, size_t elem, bool ic) {
     return t.cl_ready && (ic || !t.cl_p2p);
 }
 
+// the push sweep (IC pair, with the reciprocal diagonal): forced by mode 4; the automatic
+// choice for real values wherever the one-cluster sweep would be and the push plan fits
+bool Handle::push_ok(Tri &t, size_t elem) {
+    if (!use_inv_diag || t.n == 0) return false;
+    if (sweep_mode != 4 && sweep_mode != 0) return false;
+    if (sweep_mode == 0 && (vtype == SSG_COMPLEX || (double)t.n > kAutoClusterRowsPerLevel * (double)t.nlev))
+        return false;
+    return push_plan(t, elem, stream);
+}
+
 // z = (L D L^T)^{-1} r using vec[10] as the forward result
 template <typename T>
 void Handle::apply_precond(const T *d_r, T *d_z, const KState *stp) {
     T *y = vec[10].as<T>();
     const size_t v = sizeof(T);
+    if (push_ok(Lf, v) && push_ok(Ltb, v)) {
+        timed(PC_FWD, tri_bytes(Lf, v, 2), [&] {
+            sweep_push<T>(Lf, Lval.as<T>(), SW_FWD_DIV, d_r, invL_lev.as<T>(), fac_epoch, y, stp, err(), stream);
+        });
+        timed(PC_BWD, tri_bytes(Ltb, v, 3), [&] {
+            sweep_push<T>(Ltb, Ltval.as<T>(), SW_BWD_IC, y, D_lev.as<T>(), fac_epoch, d_z, stp, err(), stream);
+        });
+        return;
+    }
     if (cluster_ok(Lf, v, true) && cluster_ok(Ltb, v, true)) {
         timed(PC_FWD, tri_bytes(Lf, v, 2), [&] {
             sweep_cluster<T>(Lf, Lval.as<T>(), SW_FWD_DIV, d_r, nullptr, use_inv_diag ? invL_lev.as<T>() : nullptr, y,
@@ -653,6 +673,9 @@ Handle::TuneChoice Handle::autotune(bool keep_group) {
             cand.push_back({2, g, 0, 0.0});
             cand.push_back({3, g, 0, 0.0});
         }
+    // the push sweep sums each row in dependency-level order, not by lanes: a candidate
+    // only when the summation order is free to change
+    if (!keep_group) cand.push_back({4, 1, 0, 0.0});
     const TuneChoice before{sweep_mode, swcfg.group, swcfg.cta_per_sm, 0.0};
     const int cl_before = cl_group;
     const bool prof_on = prof.on;
@@ -676,7 +699,9 @@ Handle::TuneChoice Handle::autotune(bool keep_group) {
             cl_group = c.group;
             swcfg.cta_per_sm = c.cta_per_sm;
             // a cluster candidate whose plan does not fit would time the sync-free sweep again
-            if (c.mode >= 2 && !(cluster_ok(Lf, sizeof(T), true) && cluster_ok(Ltb, sizeof(T), true))) continue;
+            if (c.mode == 4 && !(push_ok(Lf, sizeof(T)) && push_ok(Ltb, sizeof(T)))) continue;
+            if ((c.mode == 2 || c.mode == 3) && !(cluster_ok(Lf, sizeof(T), true) && cluster_ok(Ltb, sizeof(T), true)))
+                continue;
             if (c.mode == 3 && !(Lf.cl_p2p && Ltb.cl_p2p)) continue;
             apply_precond<T>(r, z, nullptr);
             check_err("autotune");

@@ -102,7 +102,9 @@ struct Handle {
     SweepCfg swcfg;
     int fac_backoff_ns = 0;
     bool use_inv_diag = true;
-    int sweep_mode = 0;            // 0 auto (default), 1 sync-free, 2 cluster, 3 neighbour-synchronised cluster
+    int sweep_mode = 0;            // 0 auto (default), 1 sync-free, 2 cluster, 3 neighbour-synchronised cluster,
+                                   // 4 push (one cluster, no cluster-wide barrier; IC pair)
+    unsigned long long fac_epoch = 0;  // bumped whenever the factor values change (push records refill)
     int batch_group = 0;           // lanes a row in the sweeps of the owning C handle's internal batch (0: auto)
     int spmv_group_req = 0;        // lanes a row in the SpMV (0: from the mean row length)
     int spmv_lanes() const { return spmv_group_req ? spmv_group_req : spmv_group(n, nnz, vtype == SSG_COMPLEX); }
@@ -119,6 +121,7 @@ struct Handle {
     int cl_group = 4;              // lanes per row in the cluster sweep
     // ic: an IC sweep (the only kind the neighbour-synchronised plan serves)
     bool cluster_ok(Tri &t, size_t elem, bool ic);
+    bool push_ok(Tri &t, size_t elem);
 
     Prof prof;
     int prof_begin(int cls);

@@ -1,0 +1,259 @@
+"""The push sweep's schedule, checked and emulated on the CPU.
+
+The plan (sparsesolv_gb300/csrc/ss_push_plan.cpp, compiled here with g++ on
+its own) turns a level-ordered triangle into one record per (level, CTA):
+per-row info, per-entry read codes and values in ELL slabs, per-row push lists.
+Before any of it runs on a GPU this test checks, independently of the plan's
+own reasoning:
+
+  * bounds: every record, code, slot, consumer and section fits the buffers
+    the kernel's shared-memory layout gives it;
+  * that every code names the value the row needs (a tagged model of every
+    CTA's shared memory is replayed level by level: the own ring is written at
+    production, the receive ring by pushes);
+  * the reuse rules the kernel's ordering relies on: an own-ring slot is
+    rewritten only at a level after its last read; a receive slot only by a
+    value pushed at least LEAD + 1 levels after the consumer's last read of
+    the previous one (so the LEAD bound orders the read first); values of the
+    level just before a row always come from shared memory;
+  * the receive barriers' byte counts, and where the factor's values, the
+    diagonal vector and the right-hand side are filled into the records;
+  * and the emulated sweep through the codes reproduces a triangular solve.
+"""
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+from scipy.sparse.linalg import spsolve_triangular
+
+from sparsesolv_gb300 import voxel
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(REPO, "sparsesolv_gb300", "csrc")
+
+
+@pytest.fixture(scope="module")
+def planlib():
+    d = tempfile.mkdtemp(prefix="pushplan")
+    so = os.path.join(d, "libpushplan.so")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-I", CSRC, "-o", so,
+                    os.path.join(CSRC, "ss_push_plan.cpp"), os.path.join(REPO, "tests", "cpp", "push_plan_capi.cpp")],
+                   check=True)
+    lib = ctypes.CDLL(so)
+    lib.pp_plan.restype = ctypes.c_void_p
+    lib.pp_why.restype = ctypes.c_char_p
+    return lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+LAYOUT = ["S_own", "S_recv", "R", "NB", "LEAD", "cap_rec", "o_x", "o_base", "o_mbr", "o_mbs", "o_prog", "o_tabring",
+          "o_buf", "total"]
+
+
+def plan(lib, tri, C, elem):
+    n, nlev, lptr, prp, pci, perm, level, ipos = tri
+    h = lib.pp_plan(ctypes.c_int(n), ctypes.c_int(nlev), _p(lptr), _p(prp), _p(pci), _p(perm), _p(level), _p(ipos),
+                    ctypes.c_int(C), ctypes.c_int(elem))
+    h = ctypes.c_void_p(h)
+    info = np.zeros(64, np.int32)
+    m = lib.pp_info(h, _p(info), 64)
+    out = {"ok": bool(info[0]), "C": int(info[1]), "nent": int(info[2]), "npush": int(info[3]),
+           "cnt_max": int(info[4]), "why": lib.pp_why(h).decode()}
+    out.update({k: int(v) for k, v in zip(LAYOUT, info[5:m])})
+    for which, name in enumerate(["tab", "rec", "vmap", "dval", "dlv", "drhs"]):
+        k = lib.pp_get(h, which, None)
+        a = np.zeros(max(k, 1), np.int32)
+        lib.pp_get(h, which, _p(a))
+        out[name] = a[:k]
+    consts = np.zeros(8, np.int32)
+    lib.pp_consts(_p(consts))
+    out["consts"] = dict(zip(["CT", "MAXQ", "SMEM_MAX", "LEAD", "NB", "S_OWN", "R"], consts[:7].tolist()))
+    lib.pp_free(h)
+    return out
+
+
+def rec_layout(lib, npass, ne, np_, elem):
+    o = np.zeros(7, np.int32)
+    lib.pp_rec(ctypes.c_int(npass), ctypes.c_int(ne), ctypes.c_int(np_), ctypes.c_int(elem), _p(o))
+    return dict(zip(["info", "code", "push", "val", "lv", "rhs", "size"], o.tolist()))
+
+
+def level_ordered(oracle, rp, ci, lower):
+    """The triangle (diagonal included) in the layout the library's level
+    schedule gives it: rows in level order, then row id; columns ascending."""
+    n = len(rp) - 1
+    trp, tci, _ = oracle.triangle(rp, ci, lower)
+    level, perm, lptr = oracle.levels(rp, ci, lower)
+    ipos = np.empty(n, np.int32)
+    ipos[perm] = np.arange(n, dtype=np.int32)
+    lens = np.diff(trp)[perm]
+    prp = np.zeros(n + 1, np.int32)
+    np.cumsum(lens, out=prp[1:])
+    starts = trp[perm]
+    idx = np.repeat(starts - prp[:-1], lens) + np.arange(prp[-1])
+    pci = np.ascontiguousarray(tci[idx], np.int32)
+    return (n, len(lptr) - 1, np.ascontiguousarray(lptr, np.int32), prp, pci, np.ascontiguousarray(perm, np.int32),
+            np.ascontiguousarray(level, np.int32), ipos), idx, trp, tci
+
+
+def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
+    n, nlev, lptr, prp, pci, perm, level, ipos = tri
+    assert P["ok"], P["why"]
+    C, S_own, S_recv, LEAD, R = P["C"], P["S_own"], P["S_recv"], P["LEAD"], P["R"]
+    k = P["consts"]
+    NS = S_own + S_recv
+    assert R >= LEAD + 2 and P["total"] <= k["SMEM_MAX"] and P["cnt_max"] <= k["CT"] * k["MAXQ"]
+    assert P["o_buf"] + P["NB"] * (-(-P["cap_rec"] // 16) * 16) == P["total"] and P["o_x"] % 16 == 0
+    assert P["o_base"] >= NS * elem and P["o_mbr"] - P["o_base"] >= 2 * k["MAXQ"] * k["CT"] * elem
+    assert P["o_buf"] % 16 == 0
+    tab = P["tab"].reshape(nlev, C, 4)
+    rec = P["rec"]
+    owner = np.empty(n, np.int64)
+    for l in range(nlev):
+        L0, L1 = lptr[l], lptr[l + 1]
+        ch = -(-(L1 - L0) // C)
+        for c in range(C):
+            owner[min(L0 + c * ch, L1):min(L0 + c * ch + ch, L1)] = c
+    vmap, dval, dlv, drhs = P["vmap"], P["dval"], P["dlv"], P["drhs"]
+    assert len(vmap) == prp[-1] - n and len(np.unique(vmap)) == len(vmap)
+    sprp_g = np.concatenate([[0], np.cumsum(np.diff(prp) - 1)])  # sorted entries of level-ordered row t
+    # diagonal of each level-ordered row, for the emulated division
+    tr = np.repeat(np.arange(n), np.diff(prp))
+    isdiag = pci == perm[tr]
+    diag_at = np.empty(n, np.int64)
+    diag_at[tr[isdiag]] = np.flatnonzero(isdiag)
+    # tagged shared memory per CTA: which row's value each slot holds
+    tag = np.full((C, NS), -1, np.int64)
+    lastread = {}   # (c, slot, tag) -> last level read
+    writes = []     # (c, slot, old tag, level written, own?)
+    y = np.full(n, np.nan)
+    produced = np.zeros(C, np.int64)
+    push_bytes = np.zeros((nlev, C), np.int64)
+    prev_end = 0
+    for l in range(nlev):
+        L0, L1 = lptr[l], lptr[l + 1]
+        ch = -(-(L1 - L0) // C)
+        pending = []
+        for c in range(C):
+            rs, re = min(L0 + c * ch, L1), min(L0 + c * ch + ch, L1)
+            off, size = tab[l, c, 0] * 16, tab[l, c, 1] * 16
+            assert size <= P["cap_rec"] and off + size <= 4 * len(rec) and off >= prev_end
+            prev_end = off + size
+            w = off // 4
+            cnt, ne, np_, npass = rec[w], rec[w + 1], rec[w + 2], rec[w + 3]
+            assert cnt == re - rs and npass == -(-cnt // k["CT"])
+            Lr = rec_layout(lib, npass, ne, np_, elem)
+            assert Lr["size"] == size
+            slots = npass * k["CT"]
+            info = rec[w + Lr["info"] // 4: w + Lr["info"] // 4 + 4 * (slots + 1)].reshape(slots + 1, 4)
+            assert tuple(info[slots]) == (ne, 0, -1, np_)
+            code = rec[w + Lr["code"] // 4: w + Lr["code"] // 4 + ne]
+            push = rec[w + Lr["push"] // 4: w + Lr["push"] // 4 + np_]
+            assert np.all(np.diff(info[:, 3]) >= 0)
+            assert np.all(code >= -NS) and np.all(code < n)
+            cons, slot = push >> 24, push & 0xFFFFFF
+            assert np.all((cons >= 0) & (cons < C) & (cons != c)) and np.all(slot < S_recv)
+            for q in range(slots):
+                first, nl, rid, p0 = info[q]
+                if q >= cnt:
+                    assert rid == -1 and info[q + 1, 3] == p0
+                    continue
+                t = rs + q
+                i = perm[t]
+                assert rid == i
+                lt = level[i]
+                nold, ln = nl & 0xFFFF, nl >> 16
+                assert first % 32 == q % 32 and (ln == 0 or first + 32 * (ln - 1) < ne)
+                eidx = first + 32 * np.arange(ln)
+                g0 = sprp_g[t]
+                assert np.array_equal(dval[g0:g0 + ln], (off + Lr["val"]) // elem + eidx)
+                assert dlv[t] == (off + Lr["lv"]) // elem + q and drhs[t] == (off + Lr["rhs"]) // elem + q
+                deps = pci[vmap[g0:g0 + ln]]
+                assert np.all(level[deps] < lt) and np.all(deps != i)
+                ld = level[deps]
+                assert np.all(np.diff(ld.astype(np.int64) * (n + 1) + deps) > 0)  # sorted (level, column)
+                assert np.all(ld[:nold] < lt - 1) and np.all(ld[nold:] == lt - 1)
+                s_ = r[i]
+                for kk, d_ in enumerate(deps):
+                    cd = code[eidx[kk]]
+                    if cd >= 0:
+                        assert cd == d_ and ld[kk] < lt - 1  # memory only for older entries
+                        if owner[ipos[d_]] != c:
+                            assert lt - level[d_] >= LEAD + 2
+                    else:
+                        sl = -1 - cd
+                        assert tag[c, sl] == d_, (l, c, q, sl)
+                        key = (c, sl, d_)
+                        lastread[key] = max(lastread.get(key, -1), lt)
+                    s_ -= vals_lo[vmap[g0 + kk]] * y[d_]
+                osl = (produced[c] + q) % S_own
+                writes.append((c, osl, tag[c, osl], l, True))
+                tag[c, osl] = i
+                y[i] = s_ / vals_lo[diag_at[t]]
+                for pk in range(p0, info[q + 1, 3]):
+                    pending.append((int(cons[pk]), S_own + int(slot[pk]), i))
+                    push_bytes[l, cons[pk]] += elem
+            produced[c] += cnt
+        for (c2, sl, i) in pending:  # pushes land before the consumers' next level
+            writes.append((c2, sl, tag[c2, sl], l, False))
+            tag[c2, sl] = i
+    assert np.array_equal(push_bytes, tab[:, :, 2])
+    # reuse: the previous occupant's last read comes before the write (own ring: an
+    # earlier level; receive ring: at least LEAD + 1 levels earlier, the LEAD bound)
+    for (c, sl, old, lw, own) in writes:
+        if old < 0:
+            continue
+        lr = lastread.get((c, sl, old), -1)
+        assert lr <= lw - (1 if own else LEAD + 1), (c, sl, old, lr, lw, own)
+    assert np.all(np.isfinite(y))
+    assert np.linalg.norm(y - ref) <= 1e-10 * np.linalg.norm(ref)
+
+
+CASES = {
+    "cc10": lambda: voxel.curl_curl_case(10, seed=11).assemble(),
+    "cfg1": lambda: voxel.config1().assemble(),
+    "cc32": lambda: voxel.curl_curl_case(32, seed=5, n_iron=2, iron_size=5).assemble(),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("lower", [True, False])
+@pytest.mark.parametrize("elem", [8, 4, 16])
+def test_push_plan_checks_and_emulates(planlib, oracle, name, lower, elem):
+    if elem != 8 and name == "cc32":
+        pytest.skip("the large case once, at FP64")
+    rp, ci, va, b = CASES[name]()
+    tri, idx, trp, tci = level_ordered(oracle, rp, ci, lower)
+    P = plan(planlib, tri, 16, elem)
+    n = tri[0]
+    _, _, tsrc = oracle.triangle(rp, ci, lower)
+    vals_lo = va[tsrc][idx]
+    T = sp.csr_matrix((va[tsrc], tci, trp), shape=(n, n))
+    r = np.random.default_rng(1).standard_normal(n)
+    ref = spsolve_triangular(T.tocsr(), r, lower=lower)
+    check_and_emulate(planlib, P, tri, vals_lo, r, ref, elem)
+
+
+def test_push_plan_edge_shapes(planlib, oracle):
+    """A chain (one row per level) plans and emulates; a diagonal matrix (one
+    level) has no plan and is served by the other sweeps."""
+    n = 3000
+    A = sp.diags([-np.ones(n - 1), 2.5 * np.ones(n), -np.ones(n - 1)], [-1, 0, 1]).tocsr()
+    A.sort_indices()
+    rp, ci, va = A.indptr.astype(np.int32), A.indices.astype(np.int32), A.data
+    tri, idx, trp, tci = level_ordered(oracle, rp, ci, True)
+    P = plan(planlib, tri, 16, 8)
+    _, _, tsrc = oracle.triangle(rp, ci, True)
+    T = sp.csr_matrix((va[tsrc], tci, trp), shape=(n, n))
+    r = np.random.default_rng(2).standard_normal(n)
+    check_and_emulate(planlib, P, tri, va[tsrc][idx], r, spsolve_triangular(T, r, lower=True), 8)
+    D = sp.diags(np.arange(1.0, 11.0)).tocsr()
+    tri, _, _, _ = level_ordered(oracle, D.indptr.astype(np.int32), D.indices.astype(np.int32), True)
+    assert not plan(planlib, tri, 16, 8)["ok"]
