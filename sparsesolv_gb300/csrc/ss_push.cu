@@ -256,7 +256,8 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
         }
         unsigned char *rb = ps_smem + L.o_buf + b * bufb;
         const int *hd = (const int *)rb;
-        const int npass = hd[3];
+        const int npass = hd[3] & 0xFFFF;
+        const bool hasg = (hd[3] >> 16) != 0;
         const PsRec R = ps_rec(npass, hd[1], hd[2], VB);
         const int4 *info = (const int4 *)(rb + R.o_info);
         const int *code = (const int *)(rb + R.o_code);
@@ -273,17 +274,31 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
             const int e = ri.x, nold = ri.y & 0xFFFF, len = ri.y >> 16;
             T s0 = (MODE == SW_FWD_DIV) ? rhs[p] : Sc<T>::zero(), s1 = Sc<T>::zero();
             int k = 0;
-            for (; k + 2 <= nold; k += 2) {
-                const int i0 = e + 32 * k;
-                const int c0 = code[i0], c1 = code[i0 + 32];
-                const T x0 = c0 < 0 ? X[-1 - c0] : ps_ldg(out + c0);
-                const T x1 = c1 < 0 ? X[-1 - c1] : ps_ldg(out + c1);
-                s0 = madd(s0, -val[i0], x0);
-                s1 = madd(s1, -val[i0 + 32], x1);
-            }
-            if (k < nold) {
-                const int i = e + 32 * k, c = code[i];
-                s0 = madd(s0, -val[i], c < 0 ? X[-1 - c] : ps_ldg(out + c));
+            if (!hasg) {
+                // every read from shared memory: no branch, the loads run ahead of the sums
+#pragma unroll 2
+                for (; k + 2 <= nold; k += 2) {
+                    const int i0 = e + 32 * k;
+                    s0 = madd(s0, -val[i0], X[-1 - code[i0]]);
+                    s1 = madd(s1, -val[i0 + 32], X[-1 - code[i0 + 32]]);
+                }
+                if (k < nold) {
+                    const int i = e + 32 * k;
+                    s0 = madd(s0, -val[i], X[-1 - code[i]]);
+                }
+            } else {
+                for (; k + 2 <= nold; k += 2) {
+                    const int i0 = e + 32 * k;
+                    const int c0 = code[i0], c1 = code[i0 + 32];
+                    const T x0 = c0 < 0 ? X[-1 - c0] : ps_ldg(out + c0);
+                    const T x1 = c1 < 0 ? X[-1 - c1] : ps_ldg(out + c1);
+                    s0 = madd(s0, -val[i0], x0);
+                    s1 = madd(s1, -val[i0 + 32], x1);
+                }
+                if (k < nold) {
+                    const int i = e + 32 * k, c = code[i];
+                    s0 = madd(s0, -val[i], c < 0 ? X[-1 - c] : ps_ldg(out + c));
+                }
             }
             const T sum = s0 + s1;
             const T d = lv[p];
@@ -351,7 +366,7 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
         const int b = l % L.NB;
         const unsigned char *rb = ps_smem + L.o_buf + b * bufb;
         const int *hd = (const int *)rb;
-        const int cnt = hd[0], npass = hd[3];
+        const int cnt = hd[0], npass = hd[3] & 0xFFFF;
         const PsRec R = ps_rec(npass, hd[1], hd[2], VB);
         const int4 *info = (const int4 *)(rb + R.o_info);
         const int *code = (const int *)(rb + R.o_code);
@@ -367,9 +382,10 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
             if (ri.z < 0) continue;
             const int e = ri.x, nold = ri.y & 0xFFFF, len = ri.y >> 16;
             T res = hb[p];
+            // the newest entries always come from shared memory (the plan guarantees it)
             for (int k = nold; k < len; ++k) {
-                const int i = e + 32 * k, c = code[i];
-                res = madd(res, val[i], c < 0 ? X[-1 - c] : ps_ldg(out + c));
+                const int i = e + 32 * k;
+                res = madd(res, val[i], X[-1 - code[i]]);
             }
             X[(produced + p) % L.S_own] = res;
             const int pe = info[p + 1].w;

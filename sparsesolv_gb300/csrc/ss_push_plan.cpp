@@ -235,7 +235,10 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
             rec[w0 + 0] = cnt;
             rec[w0 + 1] = ne;
             rec[w0 + 2] = np;
-            rec[w0 + 3] = npass;
+            bool hasg = false;  // an older entry read from the output vector (the kernel's slow path)
+            for (int t = rs; t < re; ++t)
+                for (int k = sprp[t]; k < sprp[t + 1]; ++k) hasg = hasg || code[k] >= 0;
+            rec[w0 + 3] = npass | ((hasg ? 1 : 0) << 16);
             const int slots = npass * PS_CT;
             std::vector<int> slab(npass * 4, 0);  // first entry slot of each (pass, warp) slab
             for (int i = 0, acc = 0; i < npass * 4; ++i) {

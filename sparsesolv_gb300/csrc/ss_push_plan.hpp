@@ -33,7 +33,8 @@ SSG_HD inline int ps_al16(int x) { return (x + 15) & ~15; }
 // instructions. Each warp's entries form a slab, entry k of lane's row at
 // slab + 32 * k + lane (ELL order: a warp's reads of entry k are consecutive).
 // Byte offsets from the record's start, each section 16-byte aligned:
-//   [0]       header: rows cnt, entry slots ne, pushes np, passes npass
+//   [0]       header: rows cnt, entry slots ne, pushes np, passes npass | (some entry
+//             read from memory) << 16
 //   [16]      row info, npass * PS_CT int4 by row: {first entry slot, old | all entries << 16,
 //             row id (-1: no row), first push}; a row's pushes run to the next row's
 //             first push (one closing int4 after the last slot)

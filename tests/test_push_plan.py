@@ -147,7 +147,7 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
             assert size <= P["cap_rec"] and off + size <= 4 * len(rec) and off >= prev_end
             prev_end = off + size
             w = off // 4
-            cnt, ne, np_, npass = rec[w], rec[w + 1], rec[w + 2], rec[w + 3]
+            cnt, ne, np_, npass = rec[w], rec[w + 1], rec[w + 2], rec[w + 3] & 0xFFFF
             assert cnt == re - rs and npass == -(-cnt // k["CT"])
             Lr = rec_layout(lib, npass, ne, np_, elem)
             assert Lr["size"] == size
@@ -155,6 +155,8 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
             info = rec[w + Lr["info"] // 4: w + Lr["info"] // 4 + 4 * (slots + 1)].reshape(slots + 1, 4)
             assert tuple(info[slots]) == (ne, 0, -1, np_)
             code = rec[w + Lr["code"] // 4: w + Lr["code"] // 4 + ne]
+            hasg = any(code[info[q, 0] + 32 * kk] >= 0 for q in range(cnt) for kk in range(info[q, 1] >> 16))
+            assert (rec[w + 3] >> 16) == int(hasg)  # the record's flag: some entry read from memory
             push = rec[w + Lr["push"] // 4: w + Lr["push"] // 4 + np_]
             assert np.all(np.diff(info[:, 3]) >= 0)
             assert np.all(code >= -NS) and np.all(code < n)
