@@ -6,7 +6,10 @@ solution within 1e-6 relative of the FP64 oracle solve with the same method,
 shift and preconditioner (the curl-curl system is singular, so x is compared
 method to method), true residual |b - A x| / |b| below 1e-7.
 Complex (COCG / complex MRTR on singular eddy-current systems): iteration
-count within 10%, first log entries within 1e-8, A x within 5e-8 |b|."""
+count within 3% of the reference's, or within the range the reference itself
+gives when every entry of b moves by one unit in the last place (sensitivity
+runs in tests/golden/golden_large.json) widened by 3%; first 10 log entries
+within 1e-8, first 20 within 1e-6; A x within 5e-8 |b|."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -21,7 +24,27 @@ METHOD = {"iccg": _capi.METHOD_ICCG, "mrtr": _capi.METHOD_MRTR}
 
 
 def iter_slack(iters, is_complex):
-    return max(2, int((0.10 if is_complex else 0.03) * iters + 0.999))
+    return max(2, int(0.03 * iters + 0.999))
+
+
+def _sensitivity():
+    import json
+    import os
+    p = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden_large.json")
+    with open(p) as f:
+        return json.load(f).get("sensitivity", {})
+
+
+SENS = _sensitivity()
+
+
+def complex_iters_ok(key, iters, ref_iters):
+    """Within 3% of the reference's count, or inside the reference's own spread
+    under one-ulp changes of b, widened by 3%."""
+    sens = SENS.get(key)
+    lo, hi = (min(ref_iters, sens["min"]), max(ref_iters, sens["max"])) if sens else (ref_iters, ref_iters)
+    slack = iter_slack(ref_iters, True)
+    return lo - slack <= iters <= hi + slack
 
 
 @pytest.fixture(scope="module")
@@ -93,9 +116,11 @@ def test_complex_against_reference_golden(handle, golden, golden_cases, key):
     s = Settings(**run["settings"])
     ok, x, log, iters = gpu_solve(handle, run["method"], rp, ci, va, b, s)
     assert ok == run["converged"]
-    assert abs(iters - run["iters"]) <= iter_slack(run["iters"], True)
+    assert complex_iters_ok(key, iters, run["iters"]), (iters, run["iters"], SENS.get(key))
     glog = data[key + "/log"]
     assert np.allclose(log[:10], glog[:10], rtol=1e-8)
+    k = min(20, len(log), len(glog))
+    assert np.allclose(log[:k], glog[:k], rtol=1e-6)
     if run["method"] == "iccg":
         A = sp.csr_matrix((va, ci, rp))
         gx = data[key + "/x"]
@@ -158,7 +183,7 @@ def test_zero_rhs_and_early_exit(handle, golden_cases):
     assert ok2 and iters2 == 0 and len(log2) == 0
 
 
-@pytest.mark.parametrize("mode", [1, 2, 3])
+@pytest.mark.parametrize("mode", [1, 2, 3, 4])
 @pytest.mark.parametrize("key", ["cfg1/iccg", "cfg1/mrtr_ic", "cfg1/mrtr_sgs", "ec8/iccg"])
 def test_sweep_modes_solve_alike(handle, golden, golden_cases, key, mode):
     """Both sweep schedules (sync-free and one-cluster) reach the reference's
@@ -172,7 +197,10 @@ def test_sweep_modes_solve_alike(handle, golden, golden_cases, key, mode):
     finally:
         handle.set_tuning(_capi.TUNE_SWEEP_MODE, 0)
     assert ok == run["converged"]
-    assert abs(iters - run["iters"]) <= iter_slack(run["iters"], np.iscomplexobj(va))
+    if np.iscomplexobj(va):
+        assert complex_iters_ok(key, iters, run["iters"]), (iters, run["iters"])
+    else:
+        assert abs(iters - run["iters"]) <= iter_slack(run["iters"], False)
 
 
 def test_deterministic_and_factor_reuse(handle, golden_cases):
