@@ -663,7 +663,9 @@ int ssg_batch_autotune(ssg_batch bd, int *mode, int *group, int *cta_per_sm, dou
     return bguarded(bd, [&](ssg::Batch &b) {
         if (b.running) return SSG_ERR_STATE;
         if (!b.assembled) b.assemble();
-        const Handle::TuneChoice c = b.vtype == SSG_COMPLEX ? b.h.autotune<cplx>(false) : b.h.autotune<double>(false);
+        // the batch engine runs its own sweeps (sync-free and one-cluster), not the push sweep
+        const Handle::TuneChoice c =
+            b.vtype == SSG_COMPLEX ? b.h.autotune<cplx>(false, false) : b.h.autotune<double>(false, false);
         b.drop_graph();  // the captured iterations used the previous schedule
         if (mode) *mode = c.mode;
         if (group) *group = c.group;

@@ -381,6 +381,12 @@ void build_tri(Tri &T, int n, int nnz, const int *rp, const int *ci, const int *
     T.cl_ready = false;
     T.cl_fail = 0;
     T.cl_elem = 0;
+    // a new pattern: the push plan (records, codes, slots) belongs to the old one
+    T.push.ready = false;
+    T.push.fail = 0;
+    T.push.elem = 0;
+    T.push.key_val = T.push.key_lv = nullptr;
+    T.push.key_epoch = ~0ull;
     T.level.ensure(sizeof(int) * (size_t)n);
     T.perm.ensure(sizeof(int) * (size_t)n);
     T.ipos.ensure(sizeof(int) * (size_t)n);

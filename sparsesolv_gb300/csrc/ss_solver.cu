@@ -652,7 +652,7 @@ int Handle::solve(int method, double conv_cri, int max_ite, double normB, const 
 // a different order, so results change at rounding level). Each candidate is
 // run once to build its plans, then timed over three applications (median).
 template <typename T>
-Handle::TuneChoice Handle::autotune(bool keep_group) {
+Handle::TuneChoice Handle::autotune(bool keep_group, bool with_push) {
     if (vtype < 0) throw Error{SSG_ERR_STATE, "no matrix set"};
     if (n == 0) return TuneChoice{sweep_mode, swcfg.group, swcfg.cta_per_sm, 0.0};
     ensure_factor<T>(opt.accel_factor, opt.is_diag_scale != 0);
@@ -675,7 +675,7 @@ Handle::TuneChoice Handle::autotune(bool keep_group) {
         }
     // the push sweep sums each row in dependency-level order, not by lanes: a candidate
     // only when the summation order is free to change
-    if (!keep_group) cand.push_back({4, 1, 0, 0.0});
+    if (!keep_group && with_push) cand.push_back({4, 1, 0, 0.0});
     const TuneChoice before{sweep_mode, swcfg.group, swcfg.cta_per_sm, 0.0};
     const int cl_before = cl_group;
     const bool prof_on = prof.on;
@@ -730,8 +730,8 @@ Handle::TuneChoice Handle::autotune(bool keep_group) {
     return best;
 }
 
-template Handle::TuneChoice Handle::autotune<double>(bool);
-template Handle::TuneChoice Handle::autotune<cplx>(bool);
+template Handle::TuneChoice Handle::autotune<double>(bool, bool);
+template Handle::TuneChoice Handle::autotune<cplx>(bool, bool);
 template int Handle::solve<double>(int, double, int, double, const double *, double *);
 template int Handle::solve<cplx>(int, double, int, double, const cplx *, cplx *);
 template void Handle::ensure_factor<double>(double, bool);

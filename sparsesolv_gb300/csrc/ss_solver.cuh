@@ -170,7 +170,7 @@ struct Handle {
         double ms;
     };
     template <typename T>
-    TuneChoice autotune(bool keep_group);
+    TuneChoice autotune(bool keep_group, bool with_push = true);
 };
 
 // flux density B = curl A per voxel element (ss_post.cu)

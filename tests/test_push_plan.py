@@ -259,3 +259,38 @@ def test_push_plan_edge_shapes(planlib, oracle):
     D = sp.diags(np.arange(1.0, 11.0)).tocsr()
     tri, _, _, _ = level_ordered(oracle, D.indptr.astype(np.int32), D.indices.astype(np.int32), True)
     assert not plan(planlib, tri, 16, 8)["ok"]
+
+
+def test_push_plan_on_edge_matrices(planlib, oracle):
+    """The irregular matrices of the GPU edge-case tests: a randomly permuted
+    sparse SPD matrix (plans and emulates), and an arrow matrix whose dense row
+    does not fit a CTA's staged record (no plan: another sweep serves it)."""
+    rng = np.random.default_rng(7)
+    n = 20_000
+    S = sp.random(n, n, density=5.0 / n, random_state=np.random.RandomState(3), format="csr")
+    S = S + S.T
+    S.data = -np.abs(S.data)
+    d = -np.asarray(S.sum(axis=1)).ravel() + rng.uniform(0.01, 0.1, n)
+    A = S + sp.diags(d)
+    p = rng.permutation(n)
+    A = sp.csr_matrix(A)[p][:, p]
+    A.sort_indices()
+    rp, ci, va = A.indptr.astype(np.int32), A.indices.astype(np.int32), A.data.copy()
+    for lower in (True, False):
+        tri, idx, trp, tci = level_ordered(oracle, rp, ci, lower)
+        P = plan(planlib, tri, 16, 8)
+        _, _, tsrc = oracle.triangle(rp, ci, lower)
+        T = sp.csr_matrix((va[tsrc], tci, trp), shape=(n, n))
+        r = rng.standard_normal(n)
+        check_and_emulate(planlib, P, tri, va[tsrc][idx], r, spsolve_triangular(T, r, lower=lower), 8)
+    n = 3000
+    Ar = sp.lil_matrix((n, n))
+    Ar.setdiag(2.0)
+    w = rng.uniform(-1.0, 1.0, n - 1) / n
+    Ar[n - 1, : n - 1] = w
+    Ar[: n - 1, n - 1] = w[:, None]
+    Ar = sp.csr_matrix(Ar)
+    Ar.sort_indices()
+    tri, _, _, _ = level_ordered(oracle, Ar.indptr.astype(np.int32), Ar.indices.astype(np.int32), True)
+    P = plan(planlib, tri, 16, 8)
+    assert not P["ok"] and "shared memory" in P["why"]
