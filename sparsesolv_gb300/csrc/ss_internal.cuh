@@ -70,6 +70,7 @@ struct PushPlan {
     bool ready = false;
     int fail = 0;                 // value sizes found infeasible (bit 0: 4 bytes, 1: 8, 2: 16)
     int elem = 0, C = 0, nent = 0, npush = 0;
+    int n = -1, nnz = -1, nlev = -1;  // shape of the triangle the plan was made for
     PushLayout lay{};
     DBuf tab;                     // per (level, CTA) int4 {record offset / 16, record bytes / 16, bytes received, 0}
     DBuf rec;                     // the level records; values refilled per factor and per sweep

@@ -385,6 +385,7 @@ void build_tri(Tri &T, int n, int nnz, const int *rp, const int *ci, const int *
     T.push.ready = false;
     T.push.fail = 0;
     T.push.elem = 0;
+    T.push.n = T.push.nnz = T.push.nlev = -1;
     T.push.key_val = T.push.key_lv = nullptr;
     T.push.key_epoch = ~0ull;
     T.level.ensure(sizeof(int) * (size_t)n);

@@ -488,7 +488,9 @@ bool push_plan(Tri &T, size_t elem_bytes, cudaStream_t s) {
     PushPlan &P = T.push;
     const int elem = (int)elem_bytes;
     const int ebit = elem == 4 ? 1 : elem == 8 ? 2 : 4;
-    if (P.ready && P.elem == elem) return true;
+    const bool same = P.n == T.n && P.nnz == T.nnz && P.nlev == T.nlev;
+    if (P.ready && P.elem == elem && same) return true;
+    if (!same) P.fail = 0;
     if (P.fail & ebit) return false;
     P.ready = false;
     const int C = push_cluster_size();
@@ -521,6 +523,9 @@ bool push_plan(Tri &T, size_t elem_bytes, cudaStream_t s) {
     P.key_val = P.key_lv = nullptr;
     P.key_epoch = ~0ull;
     P.elem = elem;
+    P.n = T.n;
+    P.nnz = T.nnz;
+    P.nlev = T.nlev;
     P.C = C;
     P.nent = H.nent;
     P.npush = H.npush;
@@ -534,7 +539,8 @@ void sweep_push(Tri &tri, const T *val, int mode, const T *rhs, const T *lvec, u
                 const KState *st, int *err, cudaStream_t s) {
     PushPlan &P = tri.push;
     if (tri.n == 0) return;
-    if (!P.ready || P.elem != (int)sizeof(T)) throw Error{SSG_ERR_STATE, "push sweep without a plan"};
+    if (!P.ready || P.elem != (int)sizeof(T) || P.n != tri.n || P.nnz != tri.nnz || P.nlev != tri.nlev)
+        throw Error{SSG_ERR_STATE, "push sweep without a plan for this triangle"};
     T *rec = P.rec.as<T>();
     if (P.key_val != val || P.key_lv != lvec || P.key_epoch != epoch) {
         const int m = std::max(P.nent, tri.n);
