@@ -4,11 +4,26 @@
  *
  * Storage is row-major CSR with sorted columns and summed duplicates, the
  * layout of Eigen::SparseMatrix<T, RowMajor> after setFromTriplets
- * (src/SparseMat.cpp:54-122). Eigen itself is not a dependency here: the
- * reference's mat() accessor is replaced by rowPtr()/getColPtr()/
- * getValuePtr(); getCols, getSize, getMaxCol, resetMat and printMat keep
- * their meaning. Every mutation bumps version(), which the solvers use to
- * decide when the device copy and its factor must be refreshed.
+ * (src/SparseMat.cpp:54-122). Eigen is not a dependency: without it the
+ * matrix is read through rowPtr()/getColPtr()/getValuePtr(). Every mutation
+ * bumps version(), which the solvers use to decide when the device copy and
+ * its factor must be refreshed.
+ *
+ * Always available, as in the reference: the builder, COO and CSR
+ * constructors, build, getSize, getTrueSize, getMaxCol, getCols, getColPtr,
+ * getValuePtr, resetMat, add (coefficient +=, inserting a missing entry),
+ * compressed, isInclude, getTargetRowVal, getTargetColVal, prune, printMat,
+ * print and readMat (src/SparseMat.cpp:188-409).
+ *
+ * With Eigen included before this header (<Eigen/Sparse>, or define
+ * SPARSESOLV_WITH_EIGEN to have it included here): the constructors from an
+ * Eigen::SparseMatrix<T, RowMajor> and from std::vector<Eigen::Triplet<T>>,
+ * setMatrix, and mat(). mat() returns an Eigen::Map of the CSR arrays
+ * (Eigen::Map<Eigen::SparseMatrix<T, RowMajor, int>>) rather than a reference
+ * to a stored Eigen matrix: it serves every expression the reference builds on
+ * mat() (products, sums, transpose, triangularView, cast, coeff, nonZeros) and
+ * writes to existing coefficients; a structural change goes through add(),
+ * prune() or setMatrix(). The non-const mat() bumps version().
  */
 #ifndef SPARSESOLV_GB300_SPARSEMAT_HPP
 #define SPARSESOLV_GB300_SPARSEMAT_HPP
@@ -20,9 +35,17 @@
 #include <numeric>
 #include <stdexcept>
 #include <string>
+#include <tuple>
+#include <utility>
 #include <vector>
 
 #include "SparseBuilder.hpp"
+
+#if defined(SPARSESOLV_WITH_EIGEN) && !defined(EIGEN_SPARSECORE_MODULE_H)
+#include <Eigen/Sparse>
+#endif
+#include <cmath>
+#include <iostream>
 
 namespace JPMRspace {
 namespace SparseSolv {
@@ -88,6 +111,173 @@ class SparseMatTMPL {
         ++ver;
     }
     uint64_t version() const { return ver; }
+    int64_t getNumCols() const { return ncols; }  // (addition) column count
+
+    /* coefficient += val, inserting the entry when the pattern lacks it (Eigen coeffRef) */
+    void add(slv_int gyo, slv_int retu, DType val) {
+        if (gyo < 0 || gyo >= nrows || retu < 0 || retu >= ncols)
+            throw std::out_of_range("SparseMat::add: (row, column) outside the matrix");
+        auto b = ci.begin() + rp[gyo], e = ci.begin() + rp[gyo + 1];
+        auto it = std::lower_bound(b, e, retu);
+        const size_t k = (size_t)(it - ci.begin());
+        if (it != e && *it == retu) {
+            va[k] += val;
+        } else {
+            ci.insert(it, retu);
+            va.insert(va.begin() + k, DType{} + val);
+            for (int64_t i = gyo + 1; i <= nrows; ++i) ++rp[i];
+        }
+        ++ver;
+    }
+    /* the storage is always compressed (Eigen makeCompressed is a no-op here) */
+    void compressed() {}
+
+    /* does row gyo hold column target_r? result_retu = its offset within the row (0 if not) */
+    bool isInclude(slv_int gyo, slv_int target_r, slv_int &result_retu) const {
+        if (gyo >= 0 && gyo < nrows)
+            for (slv_int k = rp[gyo]; k < rp[gyo + 1]; ++k)
+                if (ci[k] == target_r) {
+                    result_retu = k - rp[gyo];
+                    return true;
+                }
+        result_retu = 0;
+        return false;
+    }
+    /* rows and values of the entries in column target, in row order */
+    void getTargetRowVal(slv_int target, std::vector<slv_int> &row_pos, std::vector<DType> &row_val) const {
+        row_pos.clear();
+        row_val.clear();
+        for (int64_t i = 0; i < nrows; ++i)
+            for (slv_int k = rp[i]; k < rp[i + 1]; ++k)
+                if (ci[k] == target) {
+                    row_pos.push_back((slv_int)i);
+                    row_val.push_back(va[k]);
+                }
+    }
+    /* columns and values of the entries of row target */
+    void getTargetColVal(slv_int target, std::vector<slv_int> &col_pos, std::vector<DType> &col_val) const {
+        if (target < 0 || target >= nrows) throw std::out_of_range("SparseMat::getTargetColVal: row outside the matrix");
+        col_pos.assign(ci.begin() + rp[target], ci.begin() + rp[target + 1]);
+        col_val.assign(va.begin() + rp[target], va.begin() + rp[target + 1]);
+    }
+    /* drop the entries with |v| <= |thres| * 1e-12 (Eigen's pruned(thres) with its default
+     * double precision 1e-12, src/SparseMat.cpp:288-291) */
+    void prune(double thres) {
+        const double cut = std::abs(thres) * 1e-12;
+        slv_int w = 0;
+        std::vector<slv_int> nrp(rp.size(), 0);
+        for (int64_t i = 0; i < nrows; ++i) {
+            for (slv_int k = rp[i]; k < rp[i + 1]; ++k)
+                if (std::abs(va[k]) > cut) {
+                    ci[w] = ci[k];
+                    va[w] = va[k];
+                    ++w;
+                }
+            nrp[i + 1] = w;
+        }
+        rp.swap(nrp);
+        ci.resize(w);
+        va.resize(w);
+        ++ver;
+    }
+    /* the matrix as rows of dense text (with Eigen present: Eigen's own printout) */
+    void print() const {
+#if defined(EIGEN_SPARSECORE_MODULE_H)
+        std::cout << Eigen::SparseMatrix<DType, Eigen::RowMajor>(mat()) << std::endl;
+#else
+        for (int64_t i = 0; i < nrows; ++i) {
+            slv_int k = rp[i];
+            for (int64_t j = 0; j < ncols; ++j) {
+                const DType v = (k < rp[i + 1] && ci[k] == j) ? va[k++] : DType{};
+                std::cout << v << (j + 1 < ncols ? " " : "");
+            }
+            std::cout << "\n";
+        }
+        std::cout << std::endl;
+#endif
+    }
+    /* read the printMat format (src/SparseMat.cpp:353-409): the row count, the entries per
+     * row, the columns of each row (-1 for an empty row), then the values row by row; the
+     * column count is the largest column + 1 */
+    void readMat(const std::string &filename) {
+        std::ifstream fp(filename);
+        if (!fp) throw std::runtime_error("SparseMat::readMat: cannot open " + filename);
+        std::string w1, w2, w3;
+        slv_int size = 0;
+        fp >> w1 >> w2 >> w3 >> size;
+        if (!fp || size < 0) throw std::runtime_error("SparseMat::readMat: bad header in " + filename);
+        std::vector<slv_int> cnt(size);
+        for (auto &c : cnt) fp >> c;
+        fp >> w1 >> w2;
+        std::vector<std::vector<slv_int>> cols(size);
+        for (slv_int i = 0; i < size; ++i) {
+            if (cnt[i] == 0) {
+                slv_int skip;
+                fp >> skip;
+            } else {
+                cols[i].resize(cnt[i]);
+                for (auto &c : cols[i]) fp >> c;
+            }
+        }
+        fp >> w1 >> w2 >> w3;
+        SparseBuilderTMPL<DType> builder(size);
+        for (slv_int i = 0; i < size; ++i)
+            for (slv_int j = 0; j < cnt[i]; ++j) {
+                DType v;
+                fp >> v;
+                builder.add(i, cols[i][j], v);
+            }
+        if (!fp) throw std::runtime_error("SparseMat::readMat: truncated file " + filename);
+        std::vector<typename SparseBuilderTMPL<DType>::Triplet> t;
+        const slv_int max_retu = builder.build(t, false);
+        from_triplets(t, size, max_retu);
+    }
+
+#if defined(EIGEN_SPARSECORE_MODULE_H)
+    using EigenMat = Eigen::SparseMatrix<DType, Eigen::RowMajor, slv_int>;
+    /* from an Eigen row-major matrix (copied into CSR) */
+    explicit SparseMatTMPL(const EigenMat &M) { setMatrix(EigenMat(M)); }
+    /* from Eigen triplets: rows = largest row + 1, columns = largest column + 1, duplicates
+     * summed (src/SparseMat.cpp:54-70) */
+    explicit SparseMatTMPL(const std::vector<Eigen::Triplet<DType>> &sparse_data) {
+        std::vector<typename SparseBuilderTMPL<DType>::Triplet> t;
+        t.reserve(sparse_data.size());
+        slv_int mr = 0, mc = 0;
+        for (const auto &e : sparse_data) {
+            t.push_back({(slv_int)e.row(), (slv_int)e.col(), e.value()});
+            mr = std::max(mr, (slv_int)e.row());
+            mc = std::max(mc, (slv_int)e.col());
+        }
+        from_triplets(t, mr + 1, mc + 1);
+    }
+    void setMatrix(EigenMat &&M) {
+        M.makeCompressed();
+        nrows = M.rows();
+        ncols = M.cols();
+        rp.assign(M.outerIndexPtr(), M.outerIndexPtr() + nrows + 1);
+        ci.assign(M.innerIndexPtr(), M.innerIndexPtr() + M.nonZeros());
+        va.assign(M.valuePtr(), M.valuePtr() + M.nonZeros());
+        for (int64_t i = 0; i < nrows; ++i) {  // Eigen keeps inner indices sorted; make sure
+            std::vector<std::pair<slv_int, DType>> row;
+            for (slv_int k = rp[i]; k < rp[i + 1]; ++k) row.emplace_back(ci[k], va[k]);
+            if (std::is_sorted(row.begin(), row.end(), [](const auto &a, const auto &b) { return a.first < b.first; }))
+                continue;
+            std::stable_sort(row.begin(), row.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+            for (slv_int k = rp[i]; k < rp[i + 1]; ++k) std::tie(ci[k], va[k]) = row[k - rp[i]];
+        }
+        ++ver;
+    }
+    /* the CSR arrays as an Eigen sparse matrix (a map: no copy) */
+    Eigen::Map<EigenMat> mat() {
+        ++ver;  // the caller may write coefficients through it
+        return Eigen::Map<EigenMat>((typename EigenMat::Index)nrows, (typename EigenMat::Index)ncols,
+                                    (typename EigenMat::Index)ci.size(), rp.data(), ci.data(), va.data());
+    }
+    Eigen::Map<const EigenMat> mat() const {
+        return Eigen::Map<const EigenMat>((typename EigenMat::Index)nrows, (typename EigenMat::Index)ncols,
+                                          (typename EigenMat::Index)ci.size(), rp.data(), ci.data(), va.data());
+    }
+#endif
     void printMat(const std::string &str = "Mat.csv") const {
         std::ofstream fp(str);
         fp << "Column size : " << nrows << "\n";

@@ -1047,6 +1047,15 @@ void Batch::precond32(const Ti *r, Ti *z, const KState *stp) {
     const int n = h.n;
     Ti *y = v32[10].as<Ti>();
     const double fb = (4.0 + v) * h.Lf.nnz + 4.0 * (n + 1) + 2.0 * v * n;
+    if (h.push_ok(h.Lf, v) && h.push_ok(h.Ltb, v)) {
+        h.timed(PC_FWD, fb, [&] {
+            sweep_push<Ti>(h.Lf, L32.as<Ti>(), SW_FWD_DIV, r, invL32_lev.as<Ti>(), mix_epoch, y, stp, h.err(), s);
+        });
+        h.timed(PC_BWD, fb + v * n, [&] {
+            sweep_push<Ti>(h.Ltb, Lt32.as<Ti>(), SW_BWD_IC, y, D32_lev.as<Ti>(), mix_epoch, z, stp, h.err(), s);
+        });
+        return;
+    }
     if (h.cluster_ok(h.Lf, v, true) && h.cluster_ok(h.Ltb, v, true)) {
         h.timed(PC_FWD, fb, [&] {
             sweep_cluster<Ti>(h.Lf, L32.as<Ti>(), SW_FWD_DIV, r, nullptr, h.use_inv_diag ? invL32_lev.as<Ti>() : nullptr,
@@ -1121,6 +1130,7 @@ void Batch::start_mixed(double alpha, double conv) {
         narrow_copy(h.Dvec, D32, (size_t)n);
         narrow_copy(h.D_lev, D32_lev, (size_t)n);
     });
+    ++mix_epoch;
     BDev B = dev_view();
     k_bmix_begin<<<1, BT, 0, s>>>(B, d_ost.as<OState>(), octl(), eff_inner_tol(), max_ite);
     SSG_LAUNCHED();

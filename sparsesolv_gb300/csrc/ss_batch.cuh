@@ -79,6 +79,7 @@ struct Batch {
     double inner_tol = 0.0;  // inner solves reduce the scaled residual by this factor (0: 1e-4 real, 1e-2 complex)
     double eff_inner_tol() const { return inner_tol > 0.0 ? inner_tol : (vtype == SSG_COMPLEX ? 1.0e-2 : 1.0e-4); }
     DBuf d_ost, d_octl, A32, L32, Lt32, invL32, invL32_lev, D32, D32_lev, v32[11];
+    unsigned long long mix_epoch = 0;  // bumped whenever the FP32 factor copies are rewritten
     OState *h_ost = nullptr;
     KState *h_octl = nullptr;
     KState *octl() { return d_octl.as<KState>(); }

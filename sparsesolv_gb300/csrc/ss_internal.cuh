@@ -98,7 +98,7 @@ struct Tri {
     int cl_C = 0, cl_S = 0, cl_elem = 0, cl_ring_bytes = 0, cl_cap_r = 0, cl_cap_e = 0;
     DBuf cl_code;                // per level-ordered entry: row id, or -1 - (owner << 20 | ring slot)
     DBuf cl_tab;                 // per (level, CTA): rows [rs, re) and entries [e0, e1) of the chunk
-    PushPlan push;               // push sweep plan (ss_push.cu)
+    PushPlan push[3];            // push sweep plans (ss_push.cu), one per value size: 4, 8, 16 bytes
 };
 
 // ss_levels.cu

@@ -382,12 +382,14 @@ void build_tri(Tri &T, int n, int nnz, const int *rp, const int *ci, const int *
     T.cl_fail = 0;
     T.cl_elem = 0;
     // a new pattern: the push plan (records, codes, slots) belongs to the old one
-    T.push.ready = false;
-    T.push.fail = 0;
-    T.push.elem = 0;
-    T.push.n = T.push.nnz = T.push.nlev = -1;
-    T.push.key_val = T.push.key_lv = nullptr;
-    T.push.key_epoch = ~0ull;
+    for (PushPlan &P : T.push) {
+        P.ready = false;
+        P.fail = 0;
+        P.elem = 0;
+        P.n = P.nnz = P.nlev = -1;
+        P.key_val = P.key_lv = nullptr;
+        P.key_epoch = ~0ull;
+    }
     T.level.ensure(sizeof(int) * (size_t)n);
     T.perm.ensure(sizeof(int) * (size_t)n);
     T.ipos.ensure(sizeof(int) * (size_t)n);

@@ -485,12 +485,19 @@ static void upload(DBuf &d, const std::vector<I> &h, size_t pad_elems, cudaStrea
 
 // The plan: once per pattern and value size, on the host (ss_push_plan.cpp).
 bool push_plan(Tri &T, size_t elem_bytes, cudaStream_t s) {
-    PushPlan &P = T.push;
     const int elem = (int)elem_bytes;
     const int ebit = elem == 4 ? 1 : elem == 8 ? 2 : 4;
-    const bool same = P.n == T.n && P.nnz == T.nnz && P.nlev == T.nlev;
-    if (P.ready && P.elem == elem && same) return true;
-    if (!same) P.fail = 0;
+    PushPlan &P = T.push[elem == 4 ? 0 : elem == 8 ? 1 : 2];
+    if (P.n != T.n || P.nnz != T.nnz || P.nlev != T.nlev) {
+        // made for another triangle: start over (the shape is recorded before any attempt,
+        // so an infeasible plan is not retried on every call)
+        P.ready = false;
+        P.fail = 0;
+        P.n = T.n;
+        P.nnz = T.nnz;
+        P.nlev = T.nlev;
+    }
+    if (P.ready && P.elem == elem) return true;
     if (P.fail & ebit) return false;
     P.ready = false;
     const int C = push_cluster_size();
@@ -523,9 +530,6 @@ bool push_plan(Tri &T, size_t elem_bytes, cudaStream_t s) {
     P.key_val = P.key_lv = nullptr;
     P.key_epoch = ~0ull;
     P.elem = elem;
-    P.n = T.n;
-    P.nnz = T.nnz;
-    P.nlev = T.nlev;
     P.C = C;
     P.nent = H.nent;
     P.npush = H.npush;
@@ -537,7 +541,7 @@ bool push_plan(Tri &T, size_t elem_bytes, cudaStream_t s) {
 template <typename T>
 void sweep_push(Tri &tri, const T *val, int mode, const T *rhs, const T *lvec, unsigned long long epoch, T *out,
                 const KState *st, int *err, cudaStream_t s) {
-    PushPlan &P = tri.push;
+    PushPlan &P = tri.push[sizeof(T) == 4 ? 0 : sizeof(T) == 8 ? 1 : 2];
     if (tri.n == 0) return;
     if (!P.ready || P.elem != (int)sizeof(T) || P.n != tri.n || P.nnz != tri.nnz || P.nlev != tri.nlev)
         throw Error{SSG_ERR_STATE, "push sweep without a plan for this triangle"};

@@ -11,17 +11,19 @@ SPARSESOLV_REFERENCE environment variable or the Makefile's default) on:
     Eisenstat SGS-MRTR;
   * the 60^3 complex eddy-current system (voxel.config3, n = 626,580):
     shifted IC-MRTR and COCG at alpha 1.1;
-  * the reference's own sensitivity to rounding on the complex systems: the
-    same solve with every entry of b moved by at most one unit in the last
-    place (seeded), several times; the spread of its iteration counts bounds
-    what another rounding of the same arithmetic can be expected to give.
+  * the reference's own sensitivity to rounding: the same solve with every
+    entry of b moved by at most one unit in the last place (seeded), several
+    times. The spread of its iteration counts (complex systems), and on the
+    real 80^3 runs also of its residual log (per entry, relative to the
+    unperturbed log) and of its solution (relative 2-norm), bounds what another
+    rounding of the same arithmetic can be expected to give.
 
 Writes tests/golden/golden_large.json (iteration counts, convergence, full
 residual logs, the norm and 256 seeded samples of each solution, sha256 of
 every input). The solution vectors themselves are too large to commit; the
 GPU tests compare the full x with an FP64 oracle solve run in the test.
 
-    python tests/golden/make_golden_large.py [--skip-sensitivity]
+    python tests/golden/make_golden_large.py [--skip-sensitivity | --sensitivity-only]
 """
 from __future__ import annotations
 
@@ -75,6 +77,7 @@ RUNS = [
 ]
 # (case, run) whose sensitivity to one-ulp changes of b is measured, and how many times
 SENSITIVITY = [("cfg3", "mrtr_ic_a1.10", 6), ("cfg3", "iccg_a1.10", 6), ("ec8", "iccg", 16), ("ec8", "mrtr_ic", 16)]
+SENSITIVITY += [("cfg2", run, 4) for _, run, _, _, _ in RUNS[:7]]
 
 
 def ulp_perturbed(b, seed):
@@ -98,14 +101,19 @@ def ulp_perturbed(b, seed):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--skip-sensitivity", action="store_true")
+    ap.add_argument("--sensitivity-only", action="store_true",
+                    help="keep the committed runs, measure the sensitivity entries it lacks")
     args = ap.parse_args()
     build()
     ref = Reference()
     meta = {"cases": {}, "runs": {}, "sensitivity": {}, "samples": N_SAMPLES,
             "reference_threads": Reference.threads()}
-    if os.path.exists(OUT) and args.skip_sensitivity:
+    if os.path.exists(OUT) and (args.skip_sensitivity or args.sensitivity_only):
         with open(OUT) as f:
-            meta["sensitivity"] = json.load(f).get("sensitivity", {})
+            old = json.load(f)
+        meta["sensitivity"] = old.get("sensitivity", {})
+        if args.sensitivity_only:
+            meta = old
     systems = {}
     for name, case in cases().items():
         rp, ci, va, b = case.assemble()
@@ -113,6 +121,8 @@ def main():
         meta["cases"][name] = {"n": int(len(rp) - 1), "nnz": int(len(ci)), "complex": bool(np.iscomplexobj(va)),
                                "sha256": digest(rp, ci, va, b)}
     for case, run, method, s, maxit in RUNS:
+        if args.sensitivity_only:
+            break
         rp, ci, va, b = systems[case]
         t0 = time.perf_counter()
         res = ref.solve(method, rp, ci, va, b, s, conv=1e-8, maxit=maxit)
@@ -133,6 +143,8 @@ def main():
         small = make_golden.cases()
         small_runs = {(c, r): (m, s) for c, r, m, s, _ in make_golden.RUNS}
         for case, run, reps in SENSITIVITY:
+            if args.sensitivity_only and case + "/" + run in meta["sensitivity"]:
+                continue
             if case in systems:
                 rp, ci, va, b = systems[case]
                 method, s, maxit = next((m, s, mx) for c, r, m, s, mx in RUNS if c == case and r == run)
@@ -141,10 +153,24 @@ def main():
                 method, s = small_runs[(case, run)]
                 maxit = 5000
             its = []
+            real = not np.iscomplexobj(va) and case in systems
+            if real:
+                base = ref.solve(method, rp, ci, va, b, s, conv=1e-8, maxit=maxit)
+                log_spread = np.zeros(len(base.log))
+                x_spread = 0.0
             for k in range(reps):
                 res = ref.solve(method, rp, ci, va, ulp_perturbed(b, 1000 + k), s, conv=1e-8, maxit=maxit)
                 its.append(int(len(res.log) - 1))
-            meta["sensitivity"][case + "/" + run] = {"perturbed_iters": its, "min": min(its), "max": max(its)}
+                if real:
+                    m = min(len(res.log), len(base.log))
+                    d = np.abs(res.log[:m] - base.log[:m]) / np.abs(base.log[:m])
+                    log_spread[:m] = np.maximum(log_spread[:m], d)
+                    x_spread = max(x_spread, float(np.linalg.norm(res.x - base.x) / np.linalg.norm(base.x)))
+            entry = {"perturbed_iters": its, "min": min(its), "max": max(its)}
+            if real:
+                entry["log_rel_spread"] = [float(v) for v in log_spread]
+                entry["x_rel_spread"] = x_spread
+            meta["sensitivity"][case + "/" + run] = entry
             print("sensitivity", case, run, its, flush=True)
             with open(OUT, "w") as f:
                 json.dump(meta, f, indent=0, sort_keys=True)
