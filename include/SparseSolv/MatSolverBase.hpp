@@ -8,8 +8,8 @@
  *  - a row without its diagonal throws std::runtime_error instead of exit(1);
  *  - the Eigen-vector overloads are templates over any vector type with
  *    data() and size() (Eigen::VectorXd/VectorXcd, std::vector, ...);
- *  - additions: getIterations(), getTimings(), getAccelUsed(), setDevice(),
- *    setPrecision(), setReferenceQuirks().
+ *  - additions: getIterations(), getTimings(), getAccelUsed(), getOptions(),
+ *    setDevice(), setPrecision(), setReferenceQuirks().
  */
 #ifndef SPARSESOLV_GB300_MATSOLVERBASE_HPP
 #define SPARSESOLV_GB300_MATSOLVERBASE_HPP
@@ -75,6 +75,14 @@ class MatSolverBase {
         std::vector<double> t(2, 0.0);
         if (h) ssg_get_timings(h, t.data(), 2);
         return t;
+    }
+    /* the settings the next solve passes to the library (accel_factor and
+     * precondition_type as the derived solver sets them) */
+    ssg_options getOptions() const {
+        ssg_options o = opt;
+        o.accel_factor = accel();
+        o.precondition_type = ptype();
+        return o;
     }
     double getAccelUsed() const {
         double a = 0.0;

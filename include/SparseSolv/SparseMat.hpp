@@ -6,8 +6,10 @@
  * layout of Eigen::SparseMatrix<T, RowMajor> after setFromTriplets
  * (src/SparseMat.cpp:54-122). Eigen is not a dependency: without it the
  * matrix is read through rowPtr()/getColPtr()/getValuePtr(). Every mutation
- * bumps version(), which the solvers use to decide when the device copy and
- * its factor must be refreshed.
+ * takes a new version() from one process-wide counter, so two matrices never
+ * share a version (a matrix built where a freed one lived is not mistaken for
+ * it); the solvers use it to decide when the device copy and its factor must
+ * be refreshed.
  *
  * Always available, as in the reference: the builder, COO and CSR
  * constructors, build, getSize, getTrueSize, getMaxCol, getCols, getColPtr,
@@ -29,6 +31,7 @@
 #define SPARSESOLV_GB300_SPARSEMAT_HPP
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <fstream>
 #include <limits>
@@ -58,6 +61,9 @@ class SparseMatTMPL {
     /* COO constructor: size = largest index + 1, duplicates summed (src/SparseMat.cpp:80-104) */
     SparseMatTMPL(slv_int n_nonZero, const std::vector<slv_int> &rows, const std::vector<slv_int> &cols,
                   const std::vector<DType> &vals) {
+        if (n_nonZero < 0 || (size_t)n_nonZero > rows.size() || (size_t)n_nonZero > cols.size() ||
+            (size_t)n_nonZero > vals.size())
+            throw std::invalid_argument("SparseMat: n_nonzero exceeds the rows/cols/vals given");
         std::vector<typename SparseBuilderTMPL<DType>::Triplet> t;
         t.reserve(n_nonZero);
         slv_int mr = 0, mc = 0;
@@ -101,14 +107,14 @@ class SparseMatTMPL {
     slv_int *getColPtr() { return ci.data(); }
     const slv_int *getColPtr() const { return ci.data(); }
     DType *getValuePtr() {
-        ++ver;  // the caller may write through it
+        ver = next_version();  // the caller may write through it
         return va.data();
     }
     const DType *getValuePtr() const { return va.data(); }
     slv_int nonZeros() const { return (slv_int)ci.size(); }
     void resetMat() {
         std::fill(va.begin(), va.end(), DType{});
-        ++ver;
+        ver = next_version();
     }
     uint64_t version() const { return ver; }
     int64_t getNumCols() const { return ncols; }  // (addition) column count
@@ -127,7 +133,7 @@ class SparseMatTMPL {
             va.insert(va.begin() + k, DType{} + val);
             for (int64_t i = gyo + 1; i <= nrows; ++i) ++rp[i];
         }
-        ++ver;
+        ver = next_version();
     }
     /* the storage is always compressed (Eigen makeCompressed is a no-op here) */
     void compressed() {}
@@ -178,7 +184,7 @@ class SparseMatTMPL {
         rp.swap(nrp);
         ci.resize(w);
         va.resize(w);
-        ++ver;
+        ver = next_version();
     }
     /* the matrix as rows of dense text (with Eigen present: Eigen's own printout) */
     void print() const {
@@ -265,11 +271,11 @@ class SparseMatTMPL {
             std::stable_sort(row.begin(), row.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
             for (slv_int k = rp[i]; k < rp[i + 1]; ++k) std::tie(ci[k], va[k]) = row[k - rp[i]];
         }
-        ++ver;
+        ver = next_version();
     }
     /* the CSR arrays as an Eigen sparse matrix (a map: no copy) */
     Eigen::Map<EigenMat> mat() {
-        ++ver;  // the caller may write coefficients through it
+        ver = next_version();  // the caller may write coefficients through it
         return Eigen::Map<EigenMat>((typename EigenMat::Index)nrows, (typename EigenMat::Index)ncols,
                                     (typename EigenMat::Index)ci.size(), rp.data(), ci.data(), va.data());
     }
@@ -298,6 +304,9 @@ class SparseMatTMPL {
 
    private:
     void from_triplets(std::vector<typename SparseBuilderTMPL<DType>::Triplet> &t, int64_t nr, int64_t nc) {
+        for (const auto &e : t)
+            if (e.row < 0 || e.col < 0 || e.row >= nr || e.col >= nc)
+                throw std::out_of_range("SparseMat: negative or out-of-range index");
         std::stable_sort(t.begin(), t.end(), [](const auto &a, const auto &b) {
             return a.row != b.row ? a.row < b.row : a.col < b.col;
         });
@@ -316,12 +325,16 @@ class SparseMatTMPL {
             rp[t[k].row + 1]++;
         }
         std::partial_sum(rp.begin(), rp.end(), rp.begin());
-        ++ver;
+        ver = next_version();
     }
     std::vector<slv_int> rp, ci;
     std::vector<DType> va;
     int64_t nrows = 0, ncols = 0;
-    uint64_t ver = 0;
+    uint64_t ver = next_version();
+    static uint64_t next_version() {
+        static std::atomic<uint64_t> counter{0};
+        return ++counter;
+    }
 };
 
 using SparseMat = SparseMatTMPL<double>;

@@ -7,7 +7,11 @@ Three shared objects are built in-tree, next to their sources:
   (``nvcc -gencode arch=compute_103a,code=sm_103a``);
 * ``voxel/libvoxelgen.so`` -- the host-side seeded voxel FEM system generator
   (plain C, ``-ffp-contract=off`` so that x86-64 and aarch64 builds produce
-  bit-identical matrices).
+  bit-identical matrices);
+* ``SparseSolvPy<ext>`` -- the compiled Python module (pybind11 bindings of the
+  C++ drop-in classes of ``include/SparseSolv/``, linked against the CUDA
+  library; ``pybind/sparsesolvpy.cpp``). pybind11's headers come from the
+  installed torch (``torch/include``), else from an installed pybind11.
 
 Nothing here falls back to a CPU implementation: :func:`load_solver` raises
 when the CUDA library is missing or cannot be loaded.
@@ -15,9 +19,11 @@ when the CUDA library is missing or cannot be loaded.
 from __future__ import annotations
 
 import ctypes
+import importlib.util
 import os
 import subprocess
 import sys
+import sysconfig
 from concurrent.futures import ThreadPoolExecutor
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
@@ -26,6 +32,8 @@ CSRC = os.path.join(PKG_DIR, "csrc")
 INCLUDE = os.path.join(REPO_DIR, "include")
 SOLVER_LIB = os.path.join(PKG_DIR, "libsparsesolv_gb300.so")
 VOXEL_LIB = os.path.join(PKG_DIR, "voxel", "libvoxelgen.so")
+PYBIND_SRC = os.path.join(PKG_DIR, "pybind", "sparsesolvpy.cpp")
+PYBIND_MOD = os.path.join(PKG_DIR, "SparseSolvPy" + (sysconfig.get_config_var("EXT_SUFFIX") or ".so"))
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -103,9 +111,39 @@ def build_solver(force=False, verbose=False):
     return SOLVER_LIB
 
 
+def _pybind11_include():
+    """pybind11's headers: torch's bundled copy (found without importing torch), else pybind11's own."""
+    spec = importlib.util.find_spec("torch")
+    if spec is not None and spec.submodule_search_locations:
+        inc = os.path.join(list(spec.submodule_search_locations)[0], "include")
+        if os.path.exists(os.path.join(inc, "pybind11", "pybind11.h")):
+            return inc
+    spec = importlib.util.find_spec("pybind11")
+    if spec is not None:
+        import pybind11
+        return pybind11.get_include()
+    raise RuntimeError("sparsesolv_gb300: no pybind11 headers (torch/include or the pybind11 package) found")
+
+
+def build_pybind(force=False):
+    """Compile the SparseSolvPy module (host C++, linked against the CUDA library)."""
+    hdrs = [os.path.join(INCLUDE, "SparseSolv", h) for h in os.listdir(os.path.join(INCLUDE, "SparseSolv"))]
+    deps = [PYBIND_SRC, SOLVER_LIB, os.path.join(INCLUDE, "sparsesolv_gb300.h"), *hdrs]
+    if not force and _newer(PYBIND_MOD, deps):
+        return PYBIND_MOD
+    py_inc = sysconfig.get_paths()["include"]
+    if not os.path.exists(os.path.join(py_inc, "Python.h")):
+        raise RuntimeError("sparsesolv_gb300: Python.h not found under %s; SparseSolvPy cannot be built" % py_inc)
+    _run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-fvisibility=hidden", "-I", INCLUDE, "-I", py_inc,
+          "-I", _pybind11_include(), PYBIND_SRC, "-o", PYBIND_MOD, "-L", PKG_DIR, "-lsparsesolv_gb300",
+          "-Wl,-rpath,$ORIGIN"])
+    return PYBIND_MOD
+
+
 def build_all(force=False, verbose=False):
     build_voxel(force)
     build_solver(force, verbose)
+    build_pybind(force)
 
 
 _solver = None

@@ -1,7 +1,8 @@
 """CPU-side checks of the boundary: the CUDA library builds for sm_103a,
-loads, and exports every entry point the C header declares; the Python mirror
-of SparseSolvPy builds matrices the way the reference's SparseBuilder /
-SparseMat do. No kernel is launched here."""
+loads, and exports every entry point the C header declares; the compiled
+SparseSolvPy module (pybind11 bindings of the C++ drop-in classes) builds
+matrices the way the reference's SparseBuilder / SparseMat do. No kernel is
+launched here."""
 import os
 import re
 import subprocess
@@ -100,6 +101,47 @@ def test_coo_constructor_sums_duplicates_and_sizes():
     assert A.row_ptr.tolist() == [0, 1, 2, 3] and A.val.tolist() == [6.0, 5.0, 4.0]
 
 
+def test_sparsesolvpy_is_the_compiled_module_over_the_cpp_classes():
+    assert ssp.__file__ == _native.PYBIND_MOD and ssp.__file__.endswith(".so")
+    for name in ("SparseBuilder", "SparseBuilderC", "SparseMat", "SparseMatC", "MatSolverBase", "MatSolverICCG",
+                 "MatSolverMRTR"):
+        assert type(getattr(ssp, name)).__name__ == "pybind11_type", name
+    assert issubclass(ssp.MatSolverICCG, ssp.MatSolverBase) and issubclass(ssp.MatSolverMRTR, ssp.MatSolverBase)
+
+
+def test_sparsesolvpy_argument_errors():
+    with pytest.raises(IndexError):
+        ssp.SparseMat(2, [0, -1], [0, 0], [1.0, 2.0])
+    with pytest.raises(ValueError):
+        ssp.SparseMat(3, [0, 1], [0, 1], [1.0, 2.0])
+    b = ssp.SparseBuilder(2)
+    with pytest.raises(IndexError):
+        b.add(2, 0, 1.0)
+    A = ssp.SparseMat(2, [0, 1], [0, 1], [1.0, 2.0])
+    with pytest.raises(IndexError):
+        A.add(0, 5, 1.0)
+    with pytest.raises(ValueError):
+        ssp.SparseMat.from_csr(np.array([0, 2, 1], np.int32), np.array([0, 1], np.int32), np.ones(2))
+    with pytest.raises(ValueError):
+        ssp.SparseMat.from_csr(np.array([0, 2, 2], np.int32), np.array([1, 0], np.int32), np.ones(2))
+
+
+def test_sparsesolvpy_matrix_additions():
+    b = ssp.SparseBuilder(3)
+    b.addMany(np.array([0, 1, 2, 0]), np.array([0, 1, 2, 0]), np.array([1.0, 2.0, 3.0, 4.0]))
+    A = ssp.SparseMat(b)
+    assert A.val.tolist() == [5.0, 2.0, 3.0]
+    A.add(0, 2, -1.0)
+    assert A.row_ptr.tolist() == [0, 2, 3, 4] and A.col.tolist() == [0, 2, 1, 2]
+    assert A.isInclude(0, 2) == (True, 1) and A.isInclude(1, 0) == (False, 0)
+    assert A.getTargetRowVal(2) == ([0, 2], [-1.0, 3.0]) and A.getTargetColVal(0) == ([0, 2], [5.0, -1.0])
+    A.add(1, 1, -2.0)
+    A.prune(1.0)
+    assert A.nonZeros() == 3 and A.col.tolist() == [0, 2, 2]
+    B = ssp.SparseMat.from_csr(A.row_ptr, A.col, A.val)
+    assert B.shape == (3, 3) and B.val.tolist() == A.val.tolist()
+
+
 def test_print_mat(tmp_path):
     A = ssp.SparseMat(3, [0, 1, 1], [0, 0, 1], [1.0, 2.0, 3.0])
     p = tmp_path / "m.csv"
@@ -115,9 +157,13 @@ def test_solver_setters_without_gpu(solver_lib):
     s.setDiagScale(True)
     s.setSaveLog(True)
     s.setDirvegeType(1)
-    assert s._opt.precondition_type == 0 and s._opt.accel_factor == 1.2
-    assert s._opt.is_diag_scale == 1 and s._opt.is_save_residual_log == 1 and s._opt.diverge_judge_type == 1
+    o = s.options
+    assert o["precondition_type"] == 0 and o["accel_factor"] == 1.2
+    assert o["is_diag_scale"] == 1 and o["is_save_residual_log"] == 1 and o["diverge_judge_type"] == 1
     assert s.getResidualLog() == []
+    # defaults of the reference: alpha 1.05, SGS for MRTR, IC for ICCG
+    assert ssp.MatSolverMRTR().options["precondition_type"] == 1
+    assert ssp.MatSolverICCG().options["accel_factor"] == 1.05
 
 
 def test_no_cpu_fallback_when_library_missing(monkeypatch):
