@@ -16,17 +16,21 @@ Each run is solved on the GPU through the C ABI (automatic sweep schedule) and
 by the FP64 oracle (the C restatement of the same method, shift and
 preconditioner) in the test.
 
-Parity bar, real:
+Parity bar, real. Each bound is the larger of a fixed bar and 3x the
+reference's own spread when every entry of b moves by one unit in the last
+place (the fixture's sensitivity runs: per log entry, as a running maximum,
+and for x). These singular systems stagnate near the tolerance, where
+rounding differences between any two correct implementations grow: at
+alpha 1.05 the reference's own last log entries move by up to 10% under such
+a change, and at alpha 1.0 (no shift: the factor's pivots collapse, the
+residual stays at 1 and x near 1e-30) its x moves by 46%.
   * convergence flag equal to the reference's; iteration count within 3%;
   * residual log: first 40 entries within 1e-6 relative of the reference's;
-    every entry within 1e-3 (these singular systems stagnate near the
-    tolerance, where rounding differences between any two correct
-    implementations grow: the oracle and the reference themselves differ by
-    3e-5 in the last entry at alpha 1.1);
-  * x within 1e-6 relative of the oracle's x (the system is singular: x is
-    compared method to method), and the seeded samples of x within 1e-6 of
-    the reference's (IC-MRTR excepted: the reference's p update leaves its x
-    wrong, so its samples are not a solution);
+    every entry within 1e-3 (or the spread);
+  * x within 1e-6 relative (or the spread) of the oracle's x (the system is
+    singular: x is compared method to method), and the seeded samples of x
+    likewise of the reference's (IC-MRTR excepted: the reference's p update
+    leaves its x wrong, so its samples are not a solution);
   * true residual |b - A x| / |b| at most 1.01 x the oracle's (SGS-MRTR tests
     convergence on the diagonally scaled system), and below 1e-8 for ICCG.
 Complex (eddy current): the convergence flag; the iteration count within 3%
@@ -111,16 +115,22 @@ def test_large_against_reference(handle, oracle, systems, key):
     orc = oracle.solve(run["method"], rp, ci, va, b, s, conv=1e-8, maxit=run["maxit"])
     nb = np.linalg.norm(b)
     if not cx:
+        sens = META["sensitivity"][key]
         assert abs(iters - ref_it) <= max(1, int(0.03 * ref_it)), (iters, ref_it)
         m = min(len(log), len(glog))
         rel = np.abs(log[:m] - glog[:m]) / np.abs(glog[:m])
-        assert rel[:40].max() <= 1e-6, rel[:40].max()
-        assert rel.max() <= 1e-3, rel.max()
-        assert np.linalg.norm(x - orc.x) <= 1e-6 * np.linalg.norm(orc.x)
+        spread = np.zeros(m)
+        k = min(m, len(sens["log_rel_spread"]))
+        spread[:k] = np.maximum.accumulate(np.asarray(sens["log_rel_spread"][:k]))
+        spread[k:] = spread[k - 1] if k else 0.0
+        assert np.all(rel[:40] <= np.maximum(1e-6, 3 * spread[:40])), rel[:40].max()
+        assert np.all(rel <= np.maximum(1e-3, 3 * spread)), (rel.max(), spread[np.argmax(rel)])
+        xbar = max(1e-6, 3 * sens["x_rel_spread"])
+        assert np.linalg.norm(x - orc.x) <= xbar * np.linalg.norm(orc.x)
         if not (run["method"] == "mrtr" and run["settings"]["precondition_type"] == 0):
             idx = sample_index(len(b), META["samples"])
             xs = np.asarray(run["x_sample"])
-            assert np.linalg.norm(x[idx] - xs) <= 1e-6 * np.linalg.norm(xs)
+            assert np.linalg.norm(x[idx] - xs) <= xbar * np.linalg.norm(xs)
         tr, tro = np.linalg.norm(b - A @ x) / nb, np.linalg.norm(b - A @ orc.x) / nb
         assert tr <= 1.01 * tro + 1e-12
         if run["converged"] and run["method"] == "iccg":
