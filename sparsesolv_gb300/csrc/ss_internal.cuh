@@ -75,6 +75,8 @@ struct PushPlan {
     DBuf tab;                     // per (level, CTA) int4 {record offset / 16, record bytes / 16, bytes received, 0}
     DBuf rec;                     // the level records; values refilled per factor and per sweep
     DBuf vmap, dval, dlv, drhs, perm;  // where the factor's values, 1/diagonal or D, and the rhs go in rec
+    DBuf dnew;                    // (entry, row) pairs of the newest entries, stored as -(value * lvec[row])
+    int nnew = 0;
     const void *key_val = nullptr, *key_lv = nullptr;
     unsigned long long key_epoch = ~0ull;
 };

@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
         const PsRec R = ps_rec(npass, hd[1], hd[2], VB);
         const int4 *info = (const int4 *)(rb + R.o_info);
         const int *code = (const int *)(rb + R.o_code);
-        T *val = (T *)(rb + R.o_val);
+        const T *val = (const T *)(rb + R.o_val);
         const T *lv = (const T *)(rb + R.o_lv);
         const T *rhs = (const T *)(rb + R.o_rhs);
         T *hb = hand + (l & 1) * (PS_MAXQ * PS_CT);
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
             if (j >= npass) continue;
             const int4 ri = info[p];
             if (ri.z < 0) continue;
-            const int e = ri.x, nold = ri.y & 0xFFFF, len = ri.y >> 16;
+            const int e = ri.x, nold = ri.y & 0xFFFF;
             T s0 = (MODE == SW_FWD_DIV) ? rhs[p] : Sc<T>::zero(), s1 = Sc<T>::zero();
             int k = 0;
             if (!hasg) {
@@ -303,7 +303,6 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
             const T sum = s0 + s1;
             const T d = lv[p];
             hb[p] = (MODE == SW_FWD_DIV) ? sum * d : madd(rhs[p], d, sum);
-            for (int kk = nold; kk < len; ++kk) val[e + 32 * kk] = -(val[e + 32 * kk] * d);
         }
     };
 
@@ -433,6 +432,16 @@ __global__ void k_push_fill(int nent, int n, const int *vmap, const int *dval, c
     if (k < nent) rec[dval[k]] = val[vmap[k]];
     if (k < n) rec[dlv[k]] = lvec[k];
 }
+// the newest entries pre-scaled by their row's 1/L_ii (forward) or D (backward), once per factor,
+// so that each is one fused multiply-add in the sweep: rec[dval[k]] = -(val[vmap[k]] * lvec[t])
+template <typename T>
+__global__ void k_push_scale_newest(int nnew, const int2 *dnew, const int *vmap, const int *dval, const T *val,
+                                    const T *lvec, T *rec) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nnew) return;
+    const int2 kt = dnew[q];
+    rec[dval[kt.x]] = -(val[vmap[kt.x]] * lvec[kt.y]);
+}
 // the right-hand side of one sweep into the records, by level-ordered row: rec[drhs[t]] = v[perm[t]]
 template <typename T>
 __global__ void k_push_rhs(int n, const int *perm, const int *drhs, const T *v, T *rec) {
@@ -526,6 +535,7 @@ bool push_plan(Tri &T, size_t elem_bytes, cudaStream_t s) {
     upload(P.dlv, H.dlv, 4, s);
     upload(P.drhs, H.drhs, 4, s);
     upload(P.perm, perm, 4, s);
+    upload(P.dnew, H.dnew, 4, s);
     SSG_CUDA(cudaStreamSynchronize(s));
     P.key_val = P.key_lv = nullptr;
     P.key_epoch = ~0ull;
@@ -533,6 +543,7 @@ bool push_plan(Tri &T, size_t elem_bytes, cudaStream_t s) {
     P.C = C;
     P.nent = H.nent;
     P.npush = H.npush;
+    P.nnew = (int)(H.dnew.size() / 2);
     P.lay = H.lay;
     P.ready = true;
     return true;
@@ -551,6 +562,11 @@ void sweep_push(Tri &tri, const T *val, int mode, const T *rhs, const T *lvec, u
         k_push_fill<T><<<div_up(std::max(m, 1), 256), 256, 0, s>>>(P.nent, tri.n, P.vmap.as<int>(), P.dval.as<int>(),
                                                                    P.dlv.as<int>(), val, lvec, rec);
         SSG_LAUNCHED();
+        if (P.nnew > 0) {
+            k_push_scale_newest<T><<<div_up(P.nnew, 256), 256, 0, s>>>(P.nnew, P.dnew.as<int2>(), P.vmap.as<int>(),
+                                                                       P.dval.as<int>(), val, lvec, rec);
+            SSG_LAUNCHED();
+        }
         P.key_val = val;
         P.key_lv = lvec;
         P.key_epoch = epoch;

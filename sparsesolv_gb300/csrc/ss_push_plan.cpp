@@ -111,6 +111,10 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
         }
         nsp[t] = nold;
         sprp[t + 1] = (int)vmap.size();
+        for (int k = sprp[t] + nold; k < sprp[t + 1]; ++k) {
+            P.dnew.push_back(k);
+            P.dnew.push_back(t);
+        }
         if (sprp[t + 1] - sprp[t] > 0xFFFF) return fail("a row longer than 65535 entries");
     }
     const int nent = (int)vmap.size();

@@ -76,13 +76,15 @@ PushLayout push_layout(int S_own, int S_recv, int cap_rec, int elem, int NB);
 // rec: the records (static parts filled, values zero), as ints. Per sorted
 // entry k: vmap[k] its index in the triangle's layout, dval[k] the element
 // index of its value in rec (in units of the value size); per level-ordered
-// row t: dlv[t], drhs[t] likewise.
+// row t: dlv[t], drhs[t] likewise. dnew: pairs (entry k, row t) of the newest
+// entries (dependency level one below the row's), whose values the records
+// hold pre-scaled: -(value * lvec[t]).
 struct PushPlanHost {
     bool ok = false;
     const char *why = "";
     int C = 0, nent = 0, npush = 0, cnt_max = 0;
     PushLayout lay{};
-    std::vector<int> tab, rec, vmap, dval, dlv, drhs;
+    std::vector<int> tab, rec, vmap, dval, dlv, drhs, dnew;
 };
 
 // n rows in level order: lptr[nlev+1] level pointers, prp/pci the level-ordered

@@ -30,11 +30,11 @@ int pp_info(void *h, int *info, int cap) {
 
 const char *pp_why(void *h) { return ((const PushPlanHost *)h)->why; }
 
-// which: 0 tab, 1 rec, 2 vmap, 3 dval, 4 dlv, 5 drhs; returns the length
+// which: 0 tab, 1 rec, 2 vmap, 3 dval, 4 dlv, 5 drhs, 6 dnew; returns the length
 int pp_get(void *h, int which, int *dst) {
     const PushPlanHost *P = (const PushPlanHost *)h;
-    const std::vector<int> *a[] = {&P->tab, &P->rec, &P->vmap, &P->dval, &P->dlv, &P->drhs};
-    if (which < 0 || which > 5) return -1;
+    const std::vector<int> *a[] = {&P->tab, &P->rec, &P->vmap, &P->dval, &P->dlv, &P->drhs, &P->dnew};
+    if (which < 0 || which > 6) return -1;
     if (dst && !a[which]->empty()) std::memcpy(dst, a[which]->data(), sizeof(int) * a[which]->size());
     return (int)a[which]->size();
 }

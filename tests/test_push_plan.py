@@ -67,7 +67,7 @@ def plan(lib, tri, C, elem):
     out = {"ok": bool(info[0]), "C": int(info[1]), "nent": int(info[2]), "npush": int(info[3]),
            "cnt_max": int(info[4]), "why": lib.pp_why(h).decode()}
     out.update({k: int(v) for k, v in zip(LAYOUT, info[5:m])})
-    for which, name in enumerate(["tab", "rec", "vmap", "dval", "dlv", "drhs"]):
+    for which, name in enumerate(["tab", "rec", "vmap", "dval", "dlv", "drhs", "dnew"]):
         k = lib.pp_get(h, which, None)
         a = np.zeros(max(k, 1), np.int32)
         lib.pp_get(h, which, _p(a))
@@ -122,6 +122,7 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
         for c in range(C):
             owner[min(L0 + c * ch, L1):min(L0 + c * ch + ch, L1)] = c
     vmap, dval, dlv, drhs = P["vmap"], P["dval"], P["dlv"], P["drhs"]
+    newest = set()  # (entry, row) pairs the emulation finds newest; the plan's list must be exactly these
     assert len(vmap) == prp[-1] - n and len(np.unique(vmap)) == len(vmap)
     sprp_g = np.concatenate([[0], np.cumsum(np.diff(prp) - 1)])  # sorted entries of level-ordered row t
     # diagonal of each level-ordered row, for the emulated division
@@ -182,6 +183,7 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
                 ld = level[deps]
                 assert np.all(np.diff(ld.astype(np.int64) * (n + 1) + deps) > 0)  # sorted (level, column)
                 assert np.all(ld[:nold] < lt - 1) and np.all(ld[nold:] == lt - 1)
+                newest.update((g0 + kk, t) for kk in range(nold, ln))
                 s_ = r[i]
                 for kk, d_ in enumerate(deps):
                     cd = code[eidx[kk]]
@@ -207,6 +209,8 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
             writes.append((c2, sl, tag[c2, sl], l, False))
             tag[c2, sl] = i
     assert np.array_equal(push_bytes, tab[:, :, 2])
+    dn = P["dnew"].reshape(-1, 2)
+    assert len(dn) == len(newest) and set(map(tuple, dn.tolist())) == newest
     # reuse: the previous occupant's last read comes before the write (own ring: an
     # earlier level; receive ring: at least LEAD + 1 levels earlier, the LEAD bound)
     for (c, sl, old, lw, own) in writes:
