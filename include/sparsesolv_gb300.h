@@ -155,6 +155,30 @@ int ssg_flux_density(ssg_handle h, int nx, int ny, int nz, double hx, double hy,
                      const int32_t *ey, const int32_t *ez, int nunk, const void *A, int value_type, void *B,
                      int on_device);
 
+/* The voxel edge-element system assembled on the device straight into the
+ * handle's matrix, with its T-method right-hand side: the system of the
+ * reference's VoxelFEM example (examples/VoxelFEM/VoxelMatrix.cpp:118-201,
+ * :24-114), which the example builds on the host through SparseBuilder; no
+ * counterpart in the library itself. Bit-identical to the host generator
+ * (sparsesolv_gb300/voxel/voxelgen.c):
+ *   K_rc = sum over the elements e holding edges r and c, in ascending element
+ *          index, of nu[e] Ke[k][m] (+ j sig[e] omega Me[k][m] when complex),
+ *   b_r  = sum over the elements holding r of sum_{m = 8..11, tz != 0} Ce[k][m] tz_m,
+ * each product and sum rounded on its own; columns ascending, explicit zeros kept.
+ * nx, ny, nz voxels; ex/ey/ez[(nx+1)(ny+1)(nz+1)]: unknown of the x/y/z edge
+ * starting at node x + (nx+1)(y + (ny+1) z), -1 where there is none; nunk
+ * unknowns; Ke/Me/Ce: the 12 x 12 element matrices (row-major, local edge
+ * l = 4 d + 2 b + a, always host memory); nu[nx ny nz] per element
+ * (x + nx (y + ny z)); sig (may be null), omega; tz[(nx+1)(ny+1) nz] the line
+ * integral of T on the z-edge starting at node x + (nx+1)(y + (ny+1) z) (may be
+ * null: b = 0). value_type SSG_REAL or SSG_COMPLEX; b (may be null) receives
+ * nunk values of that type. ex..tz and b in host memory, or device memory with
+ * on_device = 1. Maps that do not match nunk return SSG_ERR_ARG. */
+int ssg_set_matrix_voxel(ssg_handle h, int nx, int ny, int nz, const int32_t *ex, const int32_t *ey,
+                         const int32_t *ez, int nunk, const double *Ke, const double *Me, const double *Ce,
+                         const double *nu, const double *sig, double omega, const double *tz, int value_type, void *b,
+                         int on_device);
+
 /*
  * One solve() call. b and x are host arrays of n values (x is in/out: the
  * initial guess when is_init = 0, the solution on return). normB < 0 makes

@@ -23,7 +23,7 @@ PREC_MIXED = 1
 
 EXPORTED = [
     "ssg_default_options", "ssg_create", "ssg_destroy", "ssg_last_error", "ssg_set_options", "ssg_set_matrix",
-    "ssg_set_matrix_device", "ssg_set_matrix_coo", "ssg_get_matrix", "ssg_flux_density", "ssg_solve", "ssg_solve_device", "ssg_solve_multi", "ssg_solve_multi_device", "ssg_get_residual_log", "ssg_get_iters",
+    "ssg_set_matrix_device", "ssg_set_matrix_coo", "ssg_get_matrix", "ssg_flux_density", "ssg_set_matrix_voxel", "ssg_solve", "ssg_solve_device", "ssg_solve_multi", "ssg_solve_multi_device", "ssg_get_residual_log", "ssg_get_iters",
     "ssg_get_accel_used", "ssg_get_timings", "ssg_factor", "ssg_apply_precond", "ssg_spmv", "ssg_level_schedule",
     "ssg_update_values", "ssg_update_values_device", "ssg_get_stream", "ssg_set_profiling", "ssg_get_kernel_stats",
     "ssg_launch_count", "ssg_set_tuning", "ssg_autotune", "ssg_ic_factor_noalloc", "ssg_batch_create", "ssg_batch_destroy",
@@ -72,6 +72,7 @@ def declare(lib):
         "ssg_set_matrix_coo": ([H, I, I, P, P, P, I, I], I),
         "ssg_get_matrix": ([H, P, P, P, pI, pI], I),
         "ssg_flux_density": ([H, I, I, I, D, D, D, P, P, P, I, P, I, P, I], I),
+        "ssg_set_matrix_voxel": ([H, I, I, I, P, P, P, I, P, P, P, P, P, D, P, I, P, I], I),
         "ssg_solve": ([H, I, D, I, D, P, P], I),
         "ssg_solve_device": ([H, I, D, I, D, P, P], I),
         "ssg_solve_multi": ([H, I, D, I, I, P, P, P, P], I),
@@ -221,6 +222,29 @@ class Handle:
                                               _p(ex), _p(ey), _p(ez), len(a), _p(a), COMPLEX if cplx else REAL,
                                               _p(B), 0), "ssg_flux_density")
         return B.reshape(case.nz, case.ny, case.nx, 3)
+
+    def set_matrix_voxel(self, case, complex_values=None, coils=None):
+        """Assemble a voxel case's system (sparsesolv_gb300.voxel) on the device into this
+        handle (ssg_set_matrix_voxel); returns its right-hand side b. Bit-identical to
+        case.assemble()."""
+        from . import voxel
+        if complex_values is None:
+            complex_values = case.sigma != 0.0 and case.omega != 0.0 and bool(case.conductors)
+        ex, ey, ez = case.edge_maps()
+        n = int(max(ex.max(), ey.max(), ez.max()) + 1)
+        K, M, C = voxel.element_matrices(case.h)
+        nu = case.nu()
+        sig = case.sig() if complex_values else None
+        tz = np.ascontiguousarray(case.tz(coils), np.float64)
+        b = np.zeros(n, np.complex128 if complex_values else np.float64)
+        self._check(self.lib.ssg_set_matrix_voxel(self.h, case.nx, case.ny, case.nz, _p(ex), _p(ey), _p(ez), n,
+                                                  _p(K), _p(M), _p(C), _p(nu), _p(sig), float(case.omega), _p(tz),
+                                                  COMPLEX if complex_values else REAL, _p(b), 0),
+                    "ssg_set_matrix_voxel")
+        self.n = n
+        self.complex = bool(complex_values)
+        self._mat_key = None
+        return b
 
     def get_matrix(self):
         """(row_ptr, col, val) of the current matrix."""

@@ -49,6 +49,7 @@ CUDA_SOURCES = [
     "ss_batch.cu",
     "ss_build.cu",
     "ss_post.cu",
+    "ss_voxel.cu",
     "ss_push.cu",
     "ss_push_plan.cpp",
     "ss_capi.cu",

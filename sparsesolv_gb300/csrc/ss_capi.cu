@@ -271,6 +271,17 @@ int ssg_flux_density(ssg_handle hd, int nx, int ny, int nz, double hx, double hy
     });
 }
 
+int ssg_set_matrix_voxel(ssg_handle hd, int nx, int ny, int nz, const int32_t *ex, const int32_t *ey,
+                         const int32_t *ez, int nunk, const double *Ke, const double *Me, const double *Ce,
+                         const double *nu, const double *sig, double omega, const double *tz, int value_type, void *b,
+                         int on_device) {
+    return guarded(hd, [&](Handle &h) {
+        ssg::voxel_assemble_any(h, nx, ny, nz, ex, ey, ez, nunk, Ke, Me, Ce, nu, sig, omega, tz, value_type, b,
+                                on_device != 0);
+        return SSG_OK;
+    });
+}
+
 int ssg_get_matrix(ssg_handle hd, int32_t *row_ptr, int32_t *col, double *val, int *n, int *nnz) {
     return guarded(hd, [&](Handle &h) {
         if (h.vtype < 0) return SSG_ERR_STATE;

@@ -174,6 +174,10 @@ struct Handle {
 };
 
 // flux density B = curl A per voxel element (ss_post.cu)
+// ss_voxel.cu: the voxel edge-element system assembled on the device into the handle's matrix
+void voxel_assemble_any(Handle &h, int nx, int ny, int nz, const int *ex, const int *ey, const int *ez, int nunk,
+                        const double *Ke, const double *Me, const double *Ce, const double *nu, const double *sig,
+                        double omega, const double *tz, int vt, void *b, bool on_device);
 void flux_density_any(Handle &h, int nx, int ny, int nz, double hx, double hy, double hz, const int *ex,
                       const int *ey, const int *ez, int nunk, const void *A, int vt, void *B, bool on_device);
 
