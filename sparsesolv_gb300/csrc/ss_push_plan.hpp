@@ -27,34 +27,57 @@ constexpr int PS_S_OWN = 4096;              // own-ring slots at most
 SSG_HD inline int ps_al16(int x) { return (x + 15) & ~15; }
 
 // One level's chunk of one CTA as a contiguous record (staged with one bulk copy).
-// Row q of the chunk is held by thread q % PS_CT in pass q / PS_CT: rows fill warps
-// densely, because GB300's FP64 pipe costs a warp instruction whatever the number
-// of active lanes, so the fewest warps do a level's FP64 work in the fewest
-// instructions. Each warp's entries form a slab, entry k of lane's row at
-// slab + 32 * k + lane (ELL order: a warp's reads of entry k are consecutive).
+// A row's off-diagonal entries split into its newest entries (dependency level
+// one below the row's, summed by the newest-entry group after the wait) and its
+// older entries (summed a level early by the older-entry group).
+//
+// Newest entries: row q of the chunk is held by thread q % PS_CT in pass
+// q / PS_CT (rows fill warps densely: GB300's FP64 pipe costs a warp
+// instruction whatever the number of active lanes); each warp's newest entries
+// form a slab, entry k of lane's row at slab + 32 * k + lane.
+//
+// Older entries: the chunk's W older entries, row after row, each row's in
+// (dependency level, column) order, are dealt to the PS_CT threads in runs of E
+// (thread t: flat entries [t E, t E + E) ∩ [0, W)); entry k of thread t sits at
+// k * PS_CT + t. A thread sums its run into one partial per row segment (a new
+// segment where a row starts inside the run); segments are numbered in flat
+// order, so a row's segments are consecutive, and the row's sum adds them in
+// that order. FP64 work is spread evenly over all four warps instead of
+// following the longest row of each warp.
+//
 // Byte offsets from the record's start, each section 16-byte aligned:
-//   [0]       header: rows cnt, entry slots ne, pushes np, passes npass | (some entry
-//             read from memory) << 16
-//   [16]      row info, npass * PS_CT int4 by row: {first entry slot, old | all entries << 16,
-//             row id (-1: no row), first push}; a row's pushes run to the next row's
-//             first push (one closing int4 after the last slot)
-//   codes     ne ints: >= 0 the output vector's row, < 0 shared-memory slot -1 - code
-//             (own ring [0, S_own), then the receive ring)
+//   [0]       header, 8 ints: rows cnt, newest entry slots ne, pushes np,
+//             passes npass | (some older entry read from memory) << 16, older
+//             entries W, run length E, segments nseg, 0
+//   [32]      row info, npass * PS_CT int4 by row: {first newest slot, newest
+//             entries, row id (-1: no row), first push}; a row's pushes run to
+//             the next row's first push (one closing int4 after the last slot)
+//   sbeg      npass * PS_CT + 1 ints: the first segment of each row
+//   tinfo     PS_CT int4 by thread: {row starts in the run, bits 0..31; bits
+//             32..63; first segment; index in the run of the first entry of
+//             dependency level two below its row's (E: none)}
+//   codes     ne + E * PS_CT ints (newest slab, then the older runs): >= 0 the
+//             output vector's row, < 0 shared-memory slot -1 - code (own ring
+//             [0, S_own), then the receive ring)
 //   pushes    np ints: consumer << 24 | receive slot
-//   vals      ne values
+//   vals      ne + E * PS_CT values, as the codes
 //   lv        npass * PS_CT values: 1 / L_ii (forward) or D_i (backward), by row
 //   rhs       npass * PS_CT values: the right-hand side (forward) or aux (backward)
+constexpr int PS_EMAX = 64;                 // older entries a thread holds per level at most
+constexpr int PS_SEGMAX = PS_CT + PS_CT * PS_MAXQ;  // segments of one record at most
 struct PsRec {
-    int o_info, o_code, o_push, o_val, o_lv, o_rhs, size;
+    int o_info, o_sbeg, o_tinfo, o_code, o_push, o_val, o_lv, o_rhs, size;
 };
-SSG_HD inline PsRec ps_rec(int npass, int ne, int np, int elem) {
+SSG_HD inline PsRec ps_rec(int npass, int ne, int E, int np, int elem) {
     PsRec r;
-    const int slots = npass * PS_CT;
-    r.o_info = 16;
-    r.o_code = r.o_info + 16 * (slots + 1);
-    r.o_push = r.o_code + ps_al16(4 * ne);
+    const int slots = npass * PS_CT, nv = ne + E * PS_CT;
+    r.o_info = 32;
+    r.o_sbeg = r.o_info + 16 * (slots + 1);
+    r.o_tinfo = r.o_sbeg + ps_al16(4 * (slots + 1));
+    r.o_code = r.o_tinfo + 16 * PS_CT;
+    r.o_push = r.o_code + ps_al16(4 * nv);
     r.o_val = r.o_push + ps_al16(4 * np);
-    r.o_lv = r.o_val + ps_al16(elem * ne);
+    r.o_lv = r.o_val + ps_al16(elem * nv);
     r.o_rhs = r.o_lv + ps_al16(elem * slots);
     r.size = r.o_rhs + ps_al16(elem * slots);
     return r;
@@ -66,7 +89,7 @@ struct PushLayout {
     int R, NB, LEAD;              // receive barriers, staged records, most levels a CTA runs ahead
     int cap_rec;                  // bytes of the largest record
     // byte offsets
-    int o_x, o_base, o_mbr, o_mbs, o_prog, o_tabring, o_buf;
+    int o_x, o_base, o_tp, o_mbr, o_mbs, o_prog, o_tabring, o_buf;
     int total;
 };
 PushLayout push_layout(int S_own, int S_recv, int cap_rec, int elem, int NB);
