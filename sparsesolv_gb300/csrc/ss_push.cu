@@ -253,12 +253,12 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
     int produced = 0;  // values this CTA has produced (own ring position)
     // Older entries of level l's rows, by the older-entry group during step l-1 (the
     // entries of levels <= l-2): each thread sums its run of the record's older entries
-    // into one partial per row segment; after the group's barrier, thread q adds row q's
+    // into one partial per piece; after the group's barrier, thread q adds row q's
     // partials in order and scales, so that each newest entry is one fused multiply-add
     // after the wait (the newest values are stored pre-scaled). The receive phase of
-    // level l-2 (the producers of the entries two levels below the row) is waited for
-    // just before the first such entry of the run, or after the run. Every thread of the
-    // group reaches the group barrier, also after a failed wait.
+    // level l-2 (the producers of the entries two levels below the row) is waited for by
+    // each warp just before the first such entry of its lanes' runs, or after the runs.
+    // Every thread of the group reaches the group barrier, also after a failed wait.
     T *tp = (T *)(ps_smem + L.o_tp);
     auto old_part = [&](int l) {
         const int b = l % L.NB;
@@ -273,34 +273,44 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
         const unsigned rbar = mbr + 8u * ((l - 2 + 2 * L.R) % L.R);
         const unsigned rpar = (unsigned)(((l - 2) / L.R) & 1);
         const bool need_recv = l >= 2;
+        const int4 ti = ok ? ((const int4 *)(rb + R.o_tinfo))[ct] : make_int4(0, 0, 0, 0x7FFFFFFF);
+        // the warp waits once, before the first entry any of its lanes reads from level l-2
+        // (every lane of the warp gets here, also after a failed wait)
+        const int kw = __reduce_min_sync(0xffffffffu, ti.w);
         if (ok) {
-            const int4 ti = ((const int4 *)(rb + R.o_tinfo))[ct];
             const unsigned long long mask = (unsigned)ti.x | ((unsigned long long)(unsigned)ti.y << 32);
-            const int nt = max(0, min(E, W - ct * E)), kd2 = ti.w;
-            int seg = ti.z;
+            const int nt = ti.z >> 16;
+            int seg = ti.z & 0xFFFF;
             T acc = Sc<T>::zero();
-            // the run; MEM: some entry of the record is read from the output vector
+            // the run, with entry k+1 loaded before entry k is summed; MEM: some entry of the
+            // record is read from the output vector
             auto run = [&](auto mem) {
-                for (int k = 0; k < nt; ++k) {
-                    if (k == kd2 && need_recv && !wait_phase(rbar, rpar, true)) {
-                        ok = false;
-                        break;
-                    }
-                    if (k > 0 && ((mask >> k) & 1ull)) {
-                        tp[seg++] = acc;
-                        acc = Sc<T>::zero();
-                    }
+                auto fetch = [&](int k, T &x, T &v) {
                     const int i = k * PS_CT + ct, c = code[i];
-                    T x;
+                    v = val[i];
                     if (decltype(mem)::value) x = c < 0 ? X[-1 - c] : ps_ldg(out + c);
                     else x = X[-1 - c];
-                    acc = madd(acc, -val[i], x);
+                };
+                T x = Sc<T>::zero(), v = Sc<T>::zero();
+                if (kw == 0 && need_recv && !wait_phase(rbar, rpar, true)) ok = false;
+                if (ok && nt > 0) fetch(0, x, v);
+                for (int k = 0; k < E && ok; ++k) {
+                    const T xc = x, vc = v;
+                    if (k + 1 == kw && need_recv && !wait_phase(rbar, rpar, true)) ok = false;
+                    if (ok && k + 1 < nt) fetch(k + 1, x, v);
+                    if (k < nt) {
+                        if (k > 0 && ((mask >> k) & 1ull)) {
+                            tp[seg++] = acc;
+                            acc = Sc<T>::zero();
+                        }
+                        acc = madd(acc, -vc, xc);
+                    }
                 }
             };
             if ((hd[3] >> 16) != 0) run(std::true_type{});
             else run(std::false_type{});
             if (ok && nt > 0) tp[seg] = acc;
-            if (ok && kd2 >= nt && need_recv && !wait_phase(rbar, rpar, true)) ok = false;
+            if (ok && kw >= E && need_recv && !wait_phase(rbar, rpar, true)) ok = false;
         }
         // every thread of the group arrives here, also after a failed wait; the next
         // record's runs overwrite the partials only after the next step's CTA barrier

@@ -176,19 +176,25 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
         for (int v : K) ne += 32 * v;
         return ne;
     };
-    // E: at least the even share of the threads, and about the square root of the longest
-    // row's older entries (a row spread over many runs makes a long final sum)
+    // E: the smallest run length with which the chunk's pieces, dealt in order to runs of
+    // at most E entries, fit the PS_CT threads
     auto run_length = [&](int rs, int re, int &W) {
         W = 0;
-        int mx = 0;
-        for (int t = rs; t < re; ++t) {
-            W += nsp[t];
-            mx = std::max(mx, nsp[t]);
-        }
+        for (int t = rs; t < re; ++t) W += nsp[t];
         if (W == 0) return 0;
-        int E = (W + PS_CT - 1) / PS_CT, r = 1;
-        while ((r + 1) * (r + 1) <= mx) ++r;
-        return std::max(E, r);
+        for (int E = std::max(PS_PIECE, (W + PS_CT - 1) / PS_CT);; ++E) {
+            int th = 0, load = 0;
+            for (int t = rs; t < re && th < PS_CT; ++t)
+                for (int k = 0; k < nsp[t]; k += PS_PIECE) {
+                    const int sz = std::min(PS_PIECE, nsp[t] - k);
+                    if (load + sz > E) {
+                        ++th;
+                        load = 0;
+                    }
+                    load += sz;
+                }
+            if (th < PS_CT) return E;
+        }
     };
     int cap_rec = 32, cnt_max = 0;
     for (int l = 0; l < nlev; ++l)
@@ -256,33 +262,53 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
             const size_t w0 = (size_t)(off / 4);
             rec.resize(w0 + r.size / 4, 0);
             const int vbase = (int)((off + r.o_val) / elem);
-            // older entries, flat in row order; runs of E per thread; segments
+            // older entries: pieces in row order, dealt to runs of at most E entries
             flat.clear();
-            for (int t = rs; t < re; ++t)
-                for (int k = sprp[t]; k < sprp[t] + nsp[t]; ++k) flat.push_back(k);
             segrow.clear();
+            std::vector<int> runof;  // thread of each flat entry
+            {
+                int th = 0, load = 0;
+                for (int t = rs; t < re; ++t)
+                    for (int k = 0; k < nsp[t]; k += PS_PIECE) {
+                        const int sz = std::min(PS_PIECE, nsp[t] - k);
+                        if (load + sz > E) {
+                            ++th;
+                            load = 0;
+                        }
+                        load += sz;
+                        segrow.push_back(t - rs);
+                        for (int j = 0; j < sz; ++j) {
+                            flat.push_back(sprp[t] + k + j);
+                            runof.push_back(th);
+                        }
+                    }
+            }
             bool hasg = false;  // an older entry read from the output vector (the kernel's slow path)
-            for (int th = 0; th < PS_CT; ++th) {
-                int *ti = &rec[w0 + (r.o_tinfo + 16 * th) / 4];
-                const int f0 = th * E, nt = std::max(0, std::min(E, W - f0));
-                unsigned long long mask = 0;
-                int kd2 = E;
-                ti[2] = (int)segrow.size();
-                for (int k = 0; k < nt; ++k) {
-                    const int e = flat[f0 + k];
-                    const int t = (int)(std::upper_bound(sprp.begin() + rs, sprp.begin() + re + 1, e) - sprp.begin()) - 1;
-                    const bool starts = e == sprp[t];
-                    if (starts) mask |= 1ull << k;
-                    if (k == 0 || starts) segrow.push_back(t - rs);
-                    if (kd2 == E && level[dep[e]] == level[perm[t]] - 2) kd2 = k;
-                    const int slot = ne + k * PS_CT + th;
-                    rec[w0 + r.o_code / 4 + slot] = code[e];
-                    hasg = hasg || code[e] >= 0;
-                    dval[e] = vbase + slot;
+            {
+                size_t f = 0;
+                int piece = 0;
+                for (int th = 0; th < PS_CT; ++th) {
+                    int *ti = &rec[w0 + (r.o_tinfo + 16 * th) / 4];
+                    unsigned long long mask = 0;
+                    int kd2 = E, nt = 0;
+                    const int seg0 = piece;
+                    for (; f < flat.size() && runof[f] == th; ++f, ++nt) {
+                        const int e = flat[f];
+                        const int t = (int)(std::upper_bound(sprp.begin() + rs, sprp.begin() + re + 1, e) - sprp.begin()) - 1;
+                        if ((e - sprp[t]) % PS_PIECE == 0) mask |= 1ull << nt;
+                        if (kd2 == E && level[dep[e]] == level[perm[t]] - 2) kd2 = nt;
+                        const int slot = ne + nt * PS_CT + th;
+                        rec[w0 + r.o_code / 4 + slot] = code[e];
+                        hasg = hasg || code[e] >= 0;
+                        dval[e] = vbase + slot;
+                    }
+                    piece += __builtin_popcountll(mask);  // a run is whole pieces
+                    ti[0] = (int)(mask & 0xFFFFFFFFu);
+                    ti[1] = (int)(mask >> 32);
+                    ti[2] = seg0 | (nt << 16);
+                    ti[3] = kd2;
                 }
-                ti[0] = (int)(mask & 0xFFFFFFFFu);
-                ti[1] = (int)(mask >> 32);
-                ti[3] = kd2;
+                if (piece != (int)segrow.size()) return fail("piece count mismatch");
             }
             const int nseg = (int)segrow.size();
             if (nseg > PS_SEGMAX) return fail("a record has more segments than the partials hold");

@@ -36,26 +36,28 @@ SSG_HD inline int ps_al16(int x) { return (x + 15) & ~15; }
 // instruction whatever the number of active lanes); each warp's newest entries
 // form a slab, entry k of lane's row at slab + 32 * k + lane.
 //
-// Older entries: the chunk's W older entries, row after row, each row's in
-// (dependency level, column) order, are dealt to the PS_CT threads in runs of E
-// (thread t: flat entries [t E, t E + E) ∩ [0, W)); entry k of thread t sits at
-// k * PS_CT + t. A thread sums its run into one partial per row segment (a new
-// segment where a row starts inside the run); segments are numbered in flat
-// order, so a row's segments are consecutive, and the row's sum adds them in
-// that order. FP64 work is spread evenly over all four warps instead of
-// following the longest row of each warp.
+// Older entries: each row's older entries, in (dependency level, column)
+// order, are cut into pieces of PS_PIECE (the last may be shorter); a piece is
+// summed into one partial, and the row adds its pieces' partials in order. The
+// pieces depend on the row alone, so a row's arithmetic does not depend on what
+// else shares its level (a system gives the same bits alone and in a batch).
+// The chunk's pieces, in row order, are dealt to the PS_CT threads in
+// consecutive runs of at most E entries (the smallest E that fits); entry k of
+// thread t's run sits at k * PS_CT + t. FP64 work is spread over all four warps
+// with full lanes instead of following each warp's longest row.
 //
 // Byte offsets from the record's start, each section 16-byte aligned:
 //   [0]       header, 8 ints: rows cnt, newest entry slots ne, pushes np,
 //             passes npass | (some older entry read from memory) << 16, older
-//             entries W, run length E, segments nseg, 0
+//             entries W, run length E, pieces nseg, 0
 //   [32]      row info, npass * PS_CT int4 by row: {first newest slot, newest
 //             entries, row id (-1: no row), first push}; a row's pushes run to
 //             the next row's first push (one closing int4 after the last slot)
-//   sbeg      npass * PS_CT + 1 ints: the first segment of each row
-//   tinfo     PS_CT int4 by thread: {row starts in the run, bits 0..31; bits
-//             32..63; first segment; index in the run of the first entry of
-//             dependency level two below its row's (E: none)}
+//   sbeg      npass * PS_CT + 1 ints: the first piece of each row
+//   tinfo     PS_CT int4 by thread: {piece starts in the run, bits 0..31; bits
+//             32..63; first piece | entries in the run << 16; index in the run
+//             of the first entry of dependency level two below its row's (E:
+//             none)}
 //   codes     ne + E * PS_CT ints (newest slab, then the older runs): >= 0 the
 //             output vector's row, < 0 shared-memory slot -1 - code (own ring
 //             [0, S_own), then the receive ring)
@@ -64,7 +66,8 @@ SSG_HD inline int ps_al16(int x) { return (x + 15) & ~15; }
 //   lv        npass * PS_CT values: 1 / L_ii (forward) or D_i (backward), by row
 //   rhs       npass * PS_CT values: the right-hand side (forward) or aux (backward)
 constexpr int PS_EMAX = 64;                 // older entries a thread holds per level at most
-constexpr int PS_SEGMAX = PS_CT + PS_CT * PS_MAXQ;  // segments of one record at most
+constexpr int PS_PIECE = 4;                 // older entries summed into one partial
+constexpr int PS_SEGMAX = 1024;             // pieces of one record at most
 struct PsRec {
     int o_info, o_sbeg, o_tinfo, o_code, o_push, o_val, o_lv, o_rhs, size;
 };

@@ -112,7 +112,7 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
     assert R >= LEAD + 2 and P["total"] <= k["SMEM_MAX"] and P["cnt_max"] <= k["CT"] * k["MAXQ"]
     assert P["o_buf"] + P["NB"] * (-(-P["cap_rec"] // 16) * 16) == P["total"] and P["o_x"] % 16 == 0
     assert P["o_base"] >= NS * elem and P["o_tp"] - P["o_base"] >= 2 * k["MAXQ"] * k["CT"] * elem
-    assert P["o_mbr"] - P["o_tp"] >= (k["CT"] + k["CT"] * k["MAXQ"]) * elem
+    assert P["o_mbr"] - P["o_tp"] >= 1024 * elem
     CT = k["CT"]
     assert P["o_buf"] % 16 == 0
     tab = P["tab"].reshape(nlev, C, 4)
@@ -193,44 +193,61 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
                     key = (c, sl, d_)
                     lastread[key] = max(lastread.get(key, -1), lt)
                 return y[d_]
-            # older entries: runs of E per thread, one partial per row segment
-            flat = [(q, kk) for q in range(cnt) for kk in range(rows[q][5])]
-            assert W == len(flat)
-            mx = max([rw[5] for rw in rows], default=0)
-            rr = 1
-            while (rr + 1) * (rr + 1) <= mx:
-                rr += 1
-            assert E == (0 if W == 0 else max(-(-W // CT), rr)) and E <= 64
+            # older entries: pieces of PIECE per row, dealt in order to runs of at most E
+            # entries (the smallest E that fits the CT threads), one partial per piece
+            PIECE = 4
+            pieces = [(q, kk, min(PIECE, rows[q][5] - kk)) for q in range(cnt) for kk in range(0, rows[q][5], PIECE)]
+            W_ = sum(rw[5] for rw in rows)
+            assert W == W_
+            def deal(E_):
+                th_, load, out_ = 0, 0, []
+                for pc in pieces:
+                    if load + pc[2] > E_:
+                        th_, load = th_ + 1, 0
+                    load += pc[2]
+                    out_.append(th_)
+                return out_
+            if W == 0:
+                assert E == 0
+                runs = []
+            else:
+                E_ = max(PIECE, -(-W // CT))
+                while deal(E_)[-1] >= CT:
+                    E_ += 1
+                assert E == E_ and E <= 64
+                runs = deal(E)
             part, segrow, hasg = [], [], False
+            pi = 0
             for th in range(CT):
-                m0, m1, seg0, kd2 = (int(v) for v in tinfo[th])
+                m0, m1, z, kd2 = (int(v) for v in tinfo[th])
                 mask = (m0 & 0xFFFFFFFF) | ((m1 & 0xFFFFFFFF) << 32)
-                f0 = th * E
-                nt = max(0, min(E, W - f0))
+                seg0, nt = z & 0xFFFF, z >> 16
                 assert seg0 == len(part)
-                acc, want_kd2 = 0.0, E
-                for k2 in range(nt):
-                    q, kk = flat[f0 + k2]
+                mine = []
+                while pi < len(pieces) and runs[pi] == th:
+                    mine.append(pieces[pi])
+                    pi += 1
+                assert nt == sum(pc[2] for pc in mine) and nt <= E
+                k2, want_mask, want_kd2 = 0, 0, E
+                for (q, kk0, sz) in mine:
                     t, i, lt, g0, ln, nold, deps = rows[q]
-                    starts = kk == 0
-                    assert bool((mask >> k2) & 1) == starts
-                    if k2 > 0 and starts:
-                        part.append(acc)
-                        acc = 0.0
-                    if k2 == 0 or starts:
-                        segrow.append(q)
-                    if want_kd2 == E and level[deps[kk]] == lt - 2:
-                        want_kd2 = k2
-                    sl_ = ne + k2 * CT + th
-                    cd = code[sl_]
-                    hasg = hasg or cd >= 0
-                    assert dval[g0 + kk] == vbase + sl_
-                    acc -= vals_lo[vmap[g0 + kk]] * read(cd, deps[kk], lt, True)
-                if nt > 0:
+                    want_mask |= 1 << k2
+                    segrow.append(q)
+                    acc = 0.0
+                    for j in range(sz):
+                        kk = kk0 + j
+                        if want_kd2 == E and level[deps[kk]] == lt - 2:
+                            want_kd2 = k2
+                        sl_ = ne + k2 * CT + th
+                        cd = code[sl_]
+                        hasg = hasg or cd >= 0
+                        assert dval[g0 + kk] == vbase + sl_
+                        acc -= vals_lo[vmap[g0 + kk]] * read(cd, deps[kk], lt, True)
+                        k2 += 1
                     part.append(acc)
-                assert kd2 == want_kd2
-                assert mask >> max(nt, 0) == 0 or nt == 64
-            assert nseg == len(part) and nseg <= CT + CT * k["MAXQ"]
+                assert mask == want_mask and kd2 == want_kd2
+            assert pi == len(pieces)
+            assert nseg == len(part) and nseg <= 1024
             assert (rec[w + 3] >> 16) == int(hasg)  # the record's flag: some older entry read from memory
             assert np.all(np.diff(segrow) >= 0)
             for q in range(slots + 1):
