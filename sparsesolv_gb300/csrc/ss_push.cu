@@ -18,13 +18,14 @@
 //     below the row) are summed by one warp group after the wait, one fused
 //     multiply-add each; the older ones by the other warp group a level early,
 //     while the first finishes level l and pushes its results;
-//   * the older entries of a level's chunk are dealt evenly to the group's 128
-//     threads (runs of E, each summed into one partial per row segment, the
-//     row's partials then added in order): GB300 issues one FP64 warp
-//     instruction per ~76 cycles per sub-partition, so the work is spread over
-//     all four sub-partitions with full warps instead of following each warp's
-//     longest row; the wait for the pushes of level l-1 comes only before the
-//     first entry that reads one of them;
+//   * each row's older entries are cut into pieces of four (ss_push_plan.hpp);
+//     a level chunk's pieces are dealt evenly to the group's 128 threads, and a
+//     thread sums four pieces at a time as four independent chains: GB300
+//     issues one FP64 warp instruction per ~19 cycles per SM and a dependent
+//     fused multiply-add takes ~64 cycles or more, so short chains over full
+//     warps, not one long chain per row, keep the FP64 pipe busy; the wait for
+//     the pushes of level l-1 comes only before the first position that reads
+//     one of them;
 //   * the newest entries fill warps densely (row q on thread q % 128);
 //   * each level's chunk is one record (ss_push_plan.hpp) staged by one
 //     cp.async.bulk copy NB - 1 levels ahead;
@@ -34,7 +35,7 @@
 //     plan proves every slot reuse safe under that bound or is infeasible.
 //
 // Per-row arithmetic: the older entries, in (dependency level, column) order,
-// go into one partial sum per run segment; the row adds its partials in order
+// go into one partial sum per piece; the row adds its pieces' partials in order
 // (the forward right-hand side first) and scales (forward: by 1/L_ii;
 // backward: aux + D * sum); each newest entry then adds -(v * 1/L_ii) * x
 // (forward) or -(v * D) * x (backward) with a fused multiply-add. The summation
@@ -170,7 +171,7 @@ struct PsArgs {
 };
 
 template <typename T, int MODE>
-__global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
+__global__ void __launch_bounds__(PS_THREADS, 1) k_sweep_push(PsArgs a) {
     if (a.st && !a.st->active) return;  // uniform across the cluster
     extern __shared__ __align__(16) unsigned char ps_smem[];
     const PushLayout &L = a.L;
@@ -252,13 +253,14 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
     int seen = 0;      // stager lane q: the last progress seen of CTA q
     int produced = 0;  // values this CTA has produced (own ring position)
     // Older entries of level l's rows, by the older-entry group during step l-1 (the
-    // entries of levels <= l-2): each thread sums its run of the record's older entries
-    // into one partial per piece; after the group's barrier, thread q adds row q's
-    // partials in order and scales, so that each newest entry is one fused multiply-add
-    // after the wait (the newest values are stored pre-scaled). The receive phase of
-    // level l-2 (the producers of the entries two levels below the row) is waited for by
-    // each warp just before the first such entry of its lanes' runs, or after the runs.
-    // Every thread of the group reaches the group barrier, also after a failed wait.
+    // entries of levels <= l-2): each thread sums its pieces of the record's older entries,
+    // four at a time (four independent chains), into one partial per piece; after the
+    // group's barrier, thread q adds row q's partials in order and scales, so that each
+    // newest entry is one fused multiply-add after the wait (the newest values are stored
+    // pre-scaled). The receive phase of level l-2 (the producers of the entries two
+    // levels below the row) is waited for by each warp just before the first position
+    // that reads such an entry, or after its pieces. Every thread of the group reaches
+    // the group barrier, also after a failed wait.
     T *tp = (T *)(ps_smem + L.o_tp);
     auto old_part = [&](int l) {
         const int b = l % L.NB;
@@ -266,52 +268,54 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
         const unsigned char *rb = ps_smem + L.o_buf + b * bufb;
         const int *hd = (const int *)rb;
         const int cnt = ok ? hd[0] : 0;
-        const int W = ok ? hd[4] : 0, E = ok ? hd[5] : 0;
-        const PsRec R = ps_rec(hd[3] & 0xFFFF, hd[1], E, hd[2], VB);
+        const PsRec R = ps_rec(hd[3] & 0xFFFF, hd[1], ok ? hd[5] : 0, hd[2], VB);
         const int *code = (const int *)(rb + R.o_code) + hd[1];
         const T *val = (const T *)(rb + R.o_val) + hd[1];
         const unsigned rbar = mbr + 8u * ((l - 2 + 2 * L.R) % L.R);
         const unsigned rpar = (unsigned)(((l - 2) / L.R) & 1);
         const bool need_recv = l >= 2;
-        const int4 ti = ok ? ((const int4 *)(rb + R.o_tinfo))[ct] : make_int4(0, 0, 0, 0x7FFFFFFF);
-        // the warp waits once, before the first entry any of its lanes reads from level l-2
-        // (every lane of the warp gets here, also after a failed wait)
-        const int kw = __reduce_min_sync(0xffffffffu, ti.w);
-        if (ok) {
-            const unsigned long long mask = (unsigned)ti.x | ((unsigned long long)(unsigned)ti.y << 32);
-            const int nt = ti.z >> 16;
-            int seg = ti.z & 0xFFFF;
-            T acc = Sc<T>::zero();
-            // the run, with entry k+1 loaded before entry k is summed; MEM: some entry of the
-            // record is read from the output vector
-            auto run = [&](auto mem) {
-                auto fetch = [&](int k, T &x, T &v) {
-                    const int i = k * PS_CT + ct, c = code[i];
-                    v = val[i];
-                    if (decltype(mem)::value) x = c < 0 ? X[-1 - c] : ps_ldg(out + c);
-                    else x = X[-1 - c];
-                };
-                T x = Sc<T>::zero(), v = Sc<T>::zero();
-                if (kw == 0 && need_recv && !wait_phase(rbar, rpar, true)) ok = false;
-                if (ok && nt > 0) fetch(0, x, v);
-                for (int k = 0; k < E && ok; ++k) {
-                    const T xc = x, vc = v;
-                    if (k + 1 == kw && need_recv && !wait_phase(rbar, rpar, true)) ok = false;
-                    if (ok && k + 1 < nt) fetch(k + 1, x, v);
-                    if (k < nt) {
-                        if (k > 0 && ((mask >> k) & 1ull)) {
-                            tp[seg++] = acc;
-                            acc = Sc<T>::zero();
-                        }
-                        acc = madd(acc, -vc, xc);
+        // this thread's pieces: [ct * npt, ct * npt + my) of the record's npc
+        const int npt = ok ? hd[5] : 0, npc = ok ? hd[6] : 0;
+        const int my = max(0, min(npt, npc - ct * npt));
+        const int4 ti = ok ? ((const int4 *)(rb + R.o_tinfo))[ct] : make_int4(0, 0, 0, 0);
+        const unsigned sizes = (unsigned)ti.x, d2m = (unsigned)ti.y;
+        // every lane of the warp runs the same rounds (also after a failed wait)
+        const int rounds = (__reduce_max_sync(0xffffffffu, npt) + PS_PIECE - 1) / PS_PIECE;
+        bool waited = !need_recv;
+        const bool mem = ok && (hd[3] >> 16) != 0;  // some older entry of the record is in the output vector
+        for (int r4 = 0; r4 < rounds; ++r4) {
+            // the warp waits once, before the first position where one of its lanes reads
+            // an entry of dependency level two below the row (pushed by level l-2)
+            unsigned lm = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) lm |= (d2m >> (4 * (4 * r4 + q))) & 0xFu;
+            const unsigned wm = __reduce_or_sync(0xffffffffu, waited ? 0u : lm);
+            const int jw = waited ? PS_PIECE : (wm ? __ffs(wm) - 1 : PS_PIECE);
+            T a[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) a[q] = Sc<T>::zero();
+#pragma unroll
+            for (int j = 0; j < PS_PIECE; ++j) {
+                if (j == jw) {
+                    if (ok && !wait_phase(rbar, rpar, true)) ok = false;
+                    waited = true;
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int pq = 4 * r4 + q;
+                    const int sz = (int)((sizes >> (2 * pq)) & 3u) + 1;
+                    if (ok && pq < my && j >= PS_PIECE - sz) {
+                        const int i = (PS_PIECE * pq + j) * PS_CT + ct, c = code[i];
+                        const T x = (mem && c >= 0) ? ps_ldg(out + c) : X[-1 - c];
+                        a[q] = madd(a[q], -val[i], x);
                     }
                 }
-            };
-            if ((hd[3] >> 16) != 0) run(std::true_type{});
-            else run(std::false_type{});
-            if (ok && nt > 0) tp[seg] = acc;
-            if (ok && kw >= E && need_recv && !wait_phase(rbar, rpar, true)) ok = false;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (ok && 4 * r4 + q < my) tp[ct * npt + 4 * r4 + q] = a[q];
         }
+        if (!waited && ok && !wait_phase(rbar, rpar, true)) ok = false;
         // every thread of the group arrives here, also after a failed wait; the next
         // record's runs overwrite the partials only after the next step's CTA barrier
         asm volatile("bar.sync 1, %0;" ::"r"(PS_CT) : "memory");

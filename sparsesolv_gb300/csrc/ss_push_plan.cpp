@@ -176,34 +176,24 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
         for (int v : K) ne += 32 * v;
         return ne;
     };
-    // E: the smallest run length with which the chunk's pieces, dealt in order to runs of
-    // at most E entries, fit the PS_CT threads
-    auto run_length = [&](int rs, int re, int &W) {
+    // pieces of the chunk's rows and pieces per thread
+    auto pieces_of = [&](int rs, int re, int &W, int &npc) {
         W = 0;
-        for (int t = rs; t < re; ++t) W += nsp[t];
-        if (W == 0) return 0;
-        for (int E = std::max(PS_PIECE, (W + PS_CT - 1) / PS_CT);; ++E) {
-            int th = 0, load = 0;
-            for (int t = rs; t < re && th < PS_CT; ++t)
-                for (int k = 0; k < nsp[t]; k += PS_PIECE) {
-                    const int sz = std::min(PS_PIECE, nsp[t] - k);
-                    if (load + sz > E) {
-                        ++th;
-                        load = 0;
-                    }
-                    load += sz;
-                }
-            if (th < PS_CT) return E;
+        npc = 0;
+        for (int t = rs; t < re; ++t) {
+            W += nsp[t];
+            npc += (nsp[t] + PS_PIECE - 1) / PS_PIECE;
         }
+        return (npc + PS_CT - 1) / PS_CT;
     };
     int cap_rec = 32, cnt_max = 0;
     for (int l = 0; l < nlev; ++l)
         for (int c = 0; c < C; ++c) {
-            int rs, re, W;
+            int rs, re, W, npc;
             chunk_of(l, c, rs, re);
-            const int ne = slab_widths(rs, re), E = run_length(rs, re, W);
-            if (E > PS_EMAX) return fail("a level chunk has more older entries than the threads hold");
-            const PsRec r = ps_rec((re - rs + PS_CT - 1) / PS_CT, ne, E, pptr[re] - pptr[rs], elem);
+            const int ne = slab_widths(rs, re), npt = pieces_of(rs, re, W, npc);
+            if (npt > PS_NPT) return fail("a level chunk has more older entries than the threads hold");
+            const PsRec r = ps_rec((re - rs + PS_CT - 1) / PS_CT, ne, npt, pptr[re] - pptr[rs], elem);
             cap_rec = std::max(cap_rec, r.size);
             cnt_max = std::max(cnt_max, re - rs);
         }
@@ -245,14 +235,14 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
     dlv.assign(n, 0);
     drhs.assign(n, 0);
     long long off = 0;
-    std::vector<int> flat, segrow;  // per record: entry of each older slot; row of each segment
+    std::vector<int> segrow;  // per record: row of each piece
     for (int l = 0; l < nlev; ++l)
         for (int c = 0; c < C; ++c) {
-            int rs, re, W;
+            int rs, re, W, npc;
             chunk_of(l, c, rs, re);
             const int cnt = re - rs, npass = (cnt + PS_CT - 1) / PS_CT, np = pptr[re] - pptr[rs];
-            const int ne = slab_widths(rs, re), E = run_length(rs, re, W);
-            const PsRec r = ps_rec(npass, ne, E, np, elem);
+            const int ne = slab_widths(rs, re), npt = pieces_of(rs, re, W, npc);
+            const PsRec r = ps_rec(npass, ne, npt, np, elem);
             if (off + r.size >= (1ll << 31)) return fail("records exceed 2 GB");
             if (bin[(size_t)l * C + c] >= (1 << 20)) return fail("a level pushes more bytes than a barrier counts");
             int *tr = &tab[((size_t)l * C + c) * 4];
@@ -262,53 +252,31 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
             const size_t w0 = (size_t)(off / 4);
             rec.resize(w0 + r.size / 4, 0);
             const int vbase = (int)((off + r.o_val) / elem);
-            // older entries: pieces in row order, dealt to runs of at most E entries
-            flat.clear();
+            // older entries: pieces cut from each row's end, right-aligned, dealt npt to a thread
             segrow.clear();
-            std::vector<int> runof;  // thread of each flat entry
-            {
-                int th = 0, load = 0;
-                for (int t = rs; t < re; ++t)
-                    for (int k = 0; k < nsp[t]; k += PS_PIECE) {
-                        const int sz = std::min(PS_PIECE, nsp[t] - k);
-                        if (load + sz > E) {
-                            ++th;
-                            load = 0;
-                        }
-                        load += sz;
-                        segrow.push_back(t - rs);
-                        for (int j = 0; j < sz; ++j) {
-                            flat.push_back(sprp[t] + k + j);
-                            runof.push_back(th);
-                        }
-                    }
-            }
             bool hasg = false;  // an older entry read from the output vector (the kernel's slow path)
             {
-                size_t f = 0;
-                int piece = 0;
-                for (int th = 0; th < PS_CT; ++th) {
-                    int *ti = &rec[w0 + (r.o_tinfo + 16 * th) / 4];
-                    unsigned long long mask = 0;
-                    int kd2 = E, nt = 0;
-                    const int seg0 = piece;
-                    for (; f < flat.size() && runof[f] == th; ++f, ++nt) {
-                        const int e = flat[f];
-                        const int t = (int)(std::upper_bound(sprp.begin() + rs, sprp.begin() + re + 1, e) - sprp.begin()) - 1;
-                        if ((e - sprp[t]) % PS_PIECE == 0) mask |= 1ull << nt;
-                        if (kd2 == E && level[dep[e]] == level[perm[t]] - 2) kd2 = nt;
-                        const int slot = ne + nt * PS_CT + th;
-                        rec[w0 + r.o_code / 4 + slot] = code[e];
-                        hasg = hasg || code[e] >= 0;
-                        dval[e] = vbase + slot;
+                int pc = 0;
+                for (int t = rs; t < re; ++t) {
+                    const int nold = nsp[t], lt = level[perm[t]];
+                    for (int e0 = 0; e0 < nold;) {
+                        const int sz = (e0 == 0 && nold % PS_PIECE) ? nold % PS_PIECE : PS_PIECE;
+                        const int th = pc / npt, q = pc % npt;
+                        int *ti = &rec[w0 + (r.o_tinfo + 16 * th) / 4];
+                        ti[0] |= (sz - 1) << (2 * q);
+                        for (int j = PS_PIECE - sz, e = sprp[t] + e0; j < PS_PIECE; ++j, ++e) {
+                            const int slot = ne + (PS_PIECE * q + j) * PS_CT + th;
+                            rec[w0 + r.o_code / 4 + slot] = code[e];
+                            hasg = hasg || code[e] >= 0;
+                            dval[e] = vbase + slot;
+                            if (level[dep[e]] == lt - 2) ti[1] |= 1 << (PS_PIECE * q + j);
+                        }
+                        segrow.push_back(t - rs);
+                        ++pc;
+                        e0 += sz;
                     }
-                    piece += __builtin_popcountll(mask);  // a run is whole pieces
-                    ti[0] = (int)(mask & 0xFFFFFFFFu);
-                    ti[1] = (int)(mask >> 32);
-                    ti[2] = seg0 | (nt << 16);
-                    ti[3] = kd2;
                 }
-                if (piece != (int)segrow.size()) return fail("piece count mismatch");
+                if (pc != npc) return fail("piece count mismatch");
             }
             const int nseg = (int)segrow.size();
             if (nseg > PS_SEGMAX) return fail("a record has more segments than the partials hold");
@@ -317,7 +285,7 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
             rec[w0 + 2] = np;
             rec[w0 + 3] = npass | ((hasg ? 1 : 0) << 16);
             rec[w0 + 4] = W;
-            rec[w0 + 5] = E;
+            rec[w0 + 5] = npt;
             rec[w0 + 6] = nseg;
             const int slots = npass * PS_CT;
             {

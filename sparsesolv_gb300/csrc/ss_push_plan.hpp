@@ -37,43 +37,46 @@ SSG_HD inline int ps_al16(int x) { return (x + 15) & ~15; }
 // form a slab, entry k of lane's row at slab + 32 * k + lane.
 //
 // Older entries: each row's older entries, in (dependency level, column)
-// order, are cut into pieces of PS_PIECE (the last may be shorter); a piece is
-// summed into one partial, and the row adds its pieces' partials in order. The
-// pieces depend on the row alone, so a row's arithmetic does not depend on what
-// else shares its level (a system gives the same bits alone and in a batch).
-// The chunk's pieces, in row order, are dealt to the PS_CT threads in
-// consecutive runs of at most E entries (the smallest E that fits); entry k of
-// thread t's run sits at k * PS_CT + t. FP64 work is spread over all four warps
-// with full lanes instead of following each warp's longest row.
+// order, are cut into pieces of PS_PIECE from the row's end (the first piece
+// may be shorter); a piece is summed into one partial, and the row adds its
+// pieces' partials in order. The pieces depend on the row alone, so a row's
+// arithmetic does not depend on what else shares its level (a system gives the
+// same bits alone and in a batch). The chunk's pieces, in row order, are dealt
+// to the PS_CT threads, npt consecutive pieces each; a thread sums up to four
+// pieces at a time, entry position j = 0..3 outer, piece inner, so its FP64
+// chain is at most four deep. Pieces are right-aligned (a piece of s entries
+// at positions 4 - s .. 3), which puts the entries of dependency level two
+// below the row (the last of the row) at the highest positions: the wait for
+// them comes late. Entry j of thread t's q-th piece sits at
+// (4 q + j) * PS_CT + t.
 //
 // Byte offsets from the record's start, each section 16-byte aligned:
 //   [0]       header, 8 ints: rows cnt, newest entry slots ne, pushes np,
 //             passes npass | (some older entry read from memory) << 16, older
-//             entries W, run length E, pieces nseg, 0
+//             entries W, pieces per thread npt, pieces nseg, 0
 //   [32]      row info, npass * PS_CT int4 by row: {first newest slot, newest
 //             entries, row id (-1: no row), first push}; a row's pushes run to
 //             the next row's first push (one closing int4 after the last slot)
 //   sbeg      npass * PS_CT + 1 ints: the first piece of each row
-//   tinfo     PS_CT int4 by thread: {piece starts in the run, bits 0..31; bits
-//             32..63; first piece | entries in the run << 16; index in the run
-//             of the first entry of dependency level two below its row's (E:
-//             none)}
-//   codes     ne + E * PS_CT ints (newest slab, then the older runs): >= 0 the
+//   tinfo     PS_CT int4 by thread: {sizes of its pieces (2 bits each, size -
+//             1), entries of dependency level two below the row (bit 4 q + j),
+//             0, 0}
+//   codes     ne + 4 npt * PS_CT ints (newest slab, then the older pieces): >= 0 the
 //             output vector's row, < 0 shared-memory slot -1 - code (own ring
 //             [0, S_own), then the receive ring)
 //   pushes    np ints: consumer << 24 | receive slot
-//   vals      ne + E * PS_CT values, as the codes
+//   vals      ne + 4 npt * PS_CT values, as the codes
 //   lv        npass * PS_CT values: 1 / L_ii (forward) or D_i (backward), by row
 //   rhs       npass * PS_CT values: the right-hand side (forward) or aux (backward)
-constexpr int PS_EMAX = 64;                 // older entries a thread holds per level at most
 constexpr int PS_PIECE = 4;                 // older entries summed into one partial
-constexpr int PS_SEGMAX = 1024;             // pieces of one record at most
+constexpr int PS_NPT = 8;                   // pieces a thread holds per level at most
+constexpr int PS_SEGMAX = PS_NPT * PS_CT;   // pieces of one record at most
 struct PsRec {
     int o_info, o_sbeg, o_tinfo, o_code, o_push, o_val, o_lv, o_rhs, size;
 };
-SSG_HD inline PsRec ps_rec(int npass, int ne, int E, int np, int elem) {
+SSG_HD inline PsRec ps_rec(int npass, int ne, int npt, int np, int elem) {
     PsRec r;
-    const int slots = npass * PS_CT, nv = ne + E * PS_CT;
+    const int slots = npass * PS_CT, nv = ne + PS_PIECE * npt * PS_CT;
     r.o_info = 32;
     r.o_sbeg = r.o_info + 16 * (slots + 1);
     r.o_tinfo = r.o_sbeg + ps_al16(4 * (slots + 1));

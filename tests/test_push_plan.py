@@ -112,7 +112,7 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
     assert R >= LEAD + 2 and P["total"] <= k["SMEM_MAX"] and P["cnt_max"] <= k["CT"] * k["MAXQ"]
     assert P["o_buf"] + P["NB"] * (-(-P["cap_rec"] // 16) * 16) == P["total"] and P["o_x"] % 16 == 0
     assert P["o_base"] >= NS * elem and P["o_tp"] - P["o_base"] >= 2 * k["MAXQ"] * k["CT"] * elem
-    assert P["o_mbr"] - P["o_tp"] >= 1024 * elem
+    assert P["o_mbr"] - P["o_tp"] >= 8 * k["CT"] * elem
     CT = k["CT"]
     assert P["o_buf"] % 16 == 0
     tab = P["tab"].reshape(nlev, C, 4)
@@ -160,7 +160,7 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
             assert tuple(info[slots]) == (ne, 0, -1, np_)
             sbeg = rec[w + Lr["sbeg"] // 4: w + Lr["sbeg"] // 4 + slots + 1]
             tinfo = rec[w + Lr["tinfo"] // 4: w + Lr["tinfo"] // 4 + 4 * CT].reshape(CT, 4)
-            code = rec[w + Lr["code"] // 4: w + Lr["code"] // 4 + ne + E * CT]
+            code = rec[w + Lr["code"] // 4: w + Lr["code"] // 4 + ne + 4 * E * CT]
             push = rec[w + Lr["push"] // 4: w + Lr["push"] // 4 + np_]
             vbase = (off + Lr["val"]) // elem
             assert np.all(np.diff(info[:, 3]) >= 0)
@@ -193,61 +193,43 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
                     key = (c, sl, d_)
                     lastread[key] = max(lastread.get(key, -1), lt)
                 return y[d_]
-            # older entries: pieces of PIECE per row, dealt in order to runs of at most E
-            # entries (the smallest E that fits the CT threads), one partial per piece
+            # older entries: pieces of PIECE cut from each row's end (the first may be
+            # shorter), right-aligned, dealt npt consecutive pieces to a thread
             PIECE = 4
-            pieces = [(q, kk, min(PIECE, rows[q][5] - kk)) for q in range(cnt) for kk in range(0, rows[q][5], PIECE)]
-            W_ = sum(rw[5] for rw in rows)
-            assert W == W_
-            def deal(E_):
-                th_, load, out_ = 0, 0, []
-                for pc in pieces:
-                    if load + pc[2] > E_:
-                        th_, load = th_ + 1, 0
-                    load += pc[2]
-                    out_.append(th_)
-                return out_
-            if W == 0:
-                assert E == 0
-                runs = []
-            else:
-                E_ = max(PIECE, -(-W // CT))
-                while deal(E_)[-1] >= CT:
-                    E_ += 1
-                assert E == E_ and E <= 64
-                runs = deal(E)
+            pieces = []
+            for q in range(cnt):
+                nold_ = rows[q][5]
+                e0 = 0
+                while e0 < nold_:
+                    sz = nold_ % PIECE if (e0 == 0 and nold_ % PIECE) else PIECE
+                    pieces.append((q, e0, sz))
+                    e0 += sz
+            assert W == sum(rw[5] for rw in rows)
+            npt_ = -(-len(pieces) // CT)
+            assert E == npt_ and E <= 8  # header word 5: pieces per thread
             part, segrow, hasg = [], [], False
-            pi = 0
+            want_t = np.zeros((CT, 2), np.int64)
+            for pc, (q, e0, sz) in enumerate(pieces):
+                th, qq = pc // npt_, pc % npt_
+                t, i, lt, g0, ln, nold, deps = rows[q]
+                want_t[th, 0] |= (sz - 1) << (2 * qq)
+                segrow.append(q)
+                acc = 0.0
+                for jj in range(sz):
+                    j = PIECE - sz + jj
+                    kk = e0 + jj
+                    if level[deps[kk]] == lt - 2:
+                        want_t[th, 1] |= 1 << (PIECE * qq + j)
+                    sl_ = ne + (PIECE * qq + j) * CT + th
+                    cd = code[sl_]
+                    hasg = hasg or cd >= 0
+                    assert dval[g0 + kk] == vbase + sl_
+                    acc -= vals_lo[vmap[g0 + kk]] * read(cd, deps[kk], lt, True)
+                part.append(acc)
             for th in range(CT):
-                m0, m1, z, kd2 = (int(v) for v in tinfo[th])
-                mask = (m0 & 0xFFFFFFFF) | ((m1 & 0xFFFFFFFF) << 32)
-                seg0, nt = z & 0xFFFF, z >> 16
-                assert seg0 == len(part)
-                mine = []
-                while pi < len(pieces) and runs[pi] == th:
-                    mine.append(pieces[pi])
-                    pi += 1
-                assert nt == sum(pc[2] for pc in mine) and nt <= E
-                k2, want_mask, want_kd2 = 0, 0, E
-                for (q, kk0, sz) in mine:
-                    t, i, lt, g0, ln, nold, deps = rows[q]
-                    want_mask |= 1 << k2
-                    segrow.append(q)
-                    acc = 0.0
-                    for j in range(sz):
-                        kk = kk0 + j
-                        if want_kd2 == E and level[deps[kk]] == lt - 2:
-                            want_kd2 = k2
-                        sl_ = ne + k2 * CT + th
-                        cd = code[sl_]
-                        hasg = hasg or cd >= 0
-                        assert dval[g0 + kk] == vbase + sl_
-                        acc -= vals_lo[vmap[g0 + kk]] * read(cd, deps[kk], lt, True)
-                        k2 += 1
-                    part.append(acc)
-                assert mask == want_mask and kd2 == want_kd2
-            assert pi == len(pieces)
-            assert nseg == len(part) and nseg <= 1024
+                assert (int(tinfo[th, 0]) & 0xFFFFFFFF) == want_t[th, 0] and (int(tinfo[th, 1]) & 0xFFFFFFFF) == want_t[th, 1]
+                assert tinfo[th, 2] == 0 and tinfo[th, 3] == 0
+            assert nseg == len(part) and nseg <= 8 * CT
             assert (rec[w + 3] >> 16) == int(hasg)  # the record's flag: some older entry read from memory
             assert np.all(np.diff(segrow) >= 0)
             for q in range(slots + 1):
