@@ -14,19 +14,12 @@
 //     reads it (st.async), each push counted on the receiver's mbarrier for the
 //     producer's level, so a CTA starts level l as soon as its own level l-1 is
 //     done and the values other CTAs produced at level l-1 have landed;
-//   * each row's entries are split by dependency level: the newest (one level
-//     below the row) are summed by one warp group after the wait, one fused
-//     multiply-add each; the older ones by the other warp group a level early,
-//     while the first finishes level l and pushes its results;
-//   * each row's older entries are cut into pieces of four (ss_push_plan.hpp);
-//     a level chunk's pieces are dealt evenly to the group's 128 threads, and a
-//     thread sums four pieces at a time as four independent chains: GB300
-//     issues one FP64 warp instruction per ~19 cycles per SM and a dependent
-//     fused multiply-add takes ~64 cycles or more, so short chains over full
-//     warps, not one long chain per row, keep the FP64 pipe busy; the wait for
-//     the pushes of level l-1 comes only before the first position that reads
-//     one of them;
-//   * the newest entries fill warps densely (row q on thread q % 128);
+//   * each row's entries are summed in the order of their dependency levels,
+//     oldest first. One warp group sums the entries of levels <= l-1 of level
+//     l+1's rows while the other finishes level l (its entries of level l-1,
+//     one fused multiply-add each after the wait) and pushes the results;
+//   * rows fill warps densely: a warp instruction on GB300's FP64 pipe costs
+//     the same with 17 or 32 active lanes;
 //   * each level's chunk is one record (ss_push_plan.hpp) staged by one
 //     cp.async.bulk copy NB - 1 levels ahead;
 //   * a CTA runs at most LEAD levels ahead of the slowest CTA (progress words
@@ -34,19 +27,18 @@
 //     how long a receive slot or a receive barrier phase must stay valid; the
 //     plan proves every slot reuse safe under that bound or is infeasible.
 //
-// Per-row arithmetic: the older entries, in (dependency level, column) order,
-// go into one partial sum per piece; the row adds its pieces' partials in order
-// (the forward right-hand side first) and scales (forward: by 1/L_ii;
-// backward: aux + D * sum); each newest entry then adds -(v * 1/L_ii) * x
-// (forward) or -(v * D) * x (backward) with a fused multiply-add. The summation
-// order differs from the other sweeps', so results agree with theirs at
-// rounding level; the push sweep is deterministic run to run.
+// Per-row arithmetic: the older entries go into two interleaved partial sums
+// (the forward right-hand side starts the first), which are added and scaled
+// (forward: by 1/L_ii; backward: aux + D * sum); each newest entry adds
+// -(v * 1/L_ii) * x (forward) or -(v * D) * x (backward) with a fused
+// multiply-add. The summation order differs from the other sweeps', so results
+// agree with theirs at rounding level; the push sweep is deterministic run to
+// run.
 //
 // Every wait is bounded (the handle's spin limit); on a timeout the kernel
 // records ERR_TIMEOUT, every CTA leaves its level loop at the next step, waits
 // for the copies it issued and for the pushes in flight, and returns.
 #include <algorithm>
-#include <type_traits>
 
 #include "sparsesolv_gb300.h"
 #include "ss_internal.cuh"
@@ -171,7 +163,7 @@ struct PsArgs {
 };
 
 template <typename T, int MODE>
-__global__ void __launch_bounds__(PS_THREADS, 1) k_sweep_push(PsArgs a) {
+__global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
     if (a.st && !a.st->active) return;  // uniform across the cluster
     extern __shared__ __align__(16) unsigned char ps_smem[];
     const PushLayout &L = a.L;
@@ -253,87 +245,62 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_sweep_push(PsArgs a) {
     int seen = 0;      // stager lane q: the last progress seen of CTA q
     int produced = 0;  // values this CTA has produced (own ring position)
     // Older entries of level l's rows, by the older-entry group during step l-1 (the
-    // entries of levels <= l-2): each thread sums its pieces of the record's older entries,
-    // four at a time (four independent chains), into one partial per piece; after the
-    // group's barrier, thread q adds row q's partials in order and scales, so that each
-    // newest entry is one fused multiply-add after the wait (the newest values are stored
-    // pre-scaled). The receive phase of level l-2 (the producers of the entries two
-    // levels below the row) is waited for by each warp just before the first position
-    // that reads such an entry, or after its pieces. Every thread of the group reaches
-    // the group barrier, also after a failed wait.
-    T *tp = (T *)(ps_smem + L.o_tp);
+    // entries of levels <= l-2), scaled so that each newest entry is one fused
+    // multiply-add after the wait; the newest values are rescaled in place in the
+    // staged record.
     auto old_part = [&](int l) {
         const int b = l % L.NB;
-        bool ok = !bad && wait_phase(mbs + 8u * b, (unsigned)((l / L.NB) & 1), false);
-        const unsigned char *rb = ps_smem + L.o_buf + b * bufb;
-        const int *hd = (const int *)rb;
-        const int cnt = ok ? hd[0] : 0;
-        const PsRec R = ps_rec(hd[3] & 0xFFFF, hd[1], ok ? hd[5] : 0, hd[2], VB);
-        const int *code = (const int *)(rb + R.o_code) + hd[1];
-        const T *val = (const T *)(rb + R.o_val) + hd[1];
-        const unsigned rbar = mbr + 8u * ((l - 2 + 2 * L.R) % L.R);
-        const unsigned rpar = (unsigned)(((l - 2) / L.R) & 1);
-        const bool need_recv = l >= 2;
-        // this thread's pieces: [ct * npt, ct * npt + my) of the record's npc
-        const int npt = ok ? hd[5] : 0, npc = ok ? hd[6] : 0;
-        const int my = max(0, min(npt, npc - ct * npt));
-        const int4 ti = ok ? ((const int4 *)(rb + R.o_tinfo))[ct] : make_int4(0, 0, 0, 0);
-        const unsigned sizes = (unsigned)ti.x, d2m = (unsigned)ti.y;
-        // every lane of the warp runs the same rounds (also after a failed wait)
-        const int rounds = (__reduce_max_sync(0xffffffffu, npt) + PS_PIECE - 1) / PS_PIECE;
-        bool waited = !need_recv;
-        const bool mem = ok && (hd[3] >> 16) != 0;  // some older entry of the record is in the output vector
-        for (int r4 = 0; r4 < rounds; ++r4) {
-            // the warp waits once, before the first position where one of its lanes reads
-            // an entry of dependency level two below the row (pushed by level l-2)
-            unsigned lm = 0;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) lm |= (d2m >> (4 * (4 * r4 + q))) & 0xFu;
-            const unsigned wm = __reduce_or_sync(0xffffffffu, waited ? 0u : lm);
-            const int jw = waited ? PS_PIECE : (wm ? __ffs(wm) - 1 : PS_PIECE);
-            T a[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) a[q] = Sc<T>::zero();
-#pragma unroll
-            for (int j = 0; j < PS_PIECE; ++j) {
-                if (j == jw) {
-                    if (ok && !wait_phase(rbar, rpar, true)) ok = false;
-                    waited = true;
-                }
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int pq = 4 * r4 + q;
-                    const int sz = (int)((sizes >> (2 * pq)) & 3u) + 1;
-                    if (ok && pq < my && j >= PS_PIECE - sz) {
-                        const int i = (PS_PIECE * pq + j) * PS_CT + ct, c = code[i];
-                        const T x = (mem && c >= 0) ? ps_ldg(out + c) : X[-1 - c];
-                        a[q] = madd(a[q], -val[i], x);
-                    }
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                if (ok && 4 * r4 + q < my) tp[ct * npt + 4 * r4 + q] = a[q];
-        }
-        if (!waited && ok && !wait_phase(rbar, rpar, true)) ok = false;
-        // every thread of the group arrives here, also after a failed wait; the next
-        // record's runs overwrite the partials only after the next step's CTA barrier
-        asm volatile("bar.sync 1, %0;" ::"r"(PS_CT) : "memory");
-        if (!ok) {
+        if (!wait_phase(mbs + 8u * b, (unsigned)((l / L.NB) & 1), false)) {
             bad = true;
             return;
         }
-        const int *sbeg = (const int *)(rb + R.o_sbeg);
+        unsigned char *rb = ps_smem + L.o_buf + b * bufb;
+        const int *hd = (const int *)rb;
+        const int npass = hd[3] & 0xFFFF;
+        const bool hasg = (hd[3] >> 16) != 0;
+        const PsRec R = ps_rec(npass, hd[1], hd[2], VB);
         const int4 *info = (const int4 *)(rb + R.o_info);
+        const int *code = (const int *)(rb + R.o_code);
+        const T *val = (const T *)(rb + R.o_val);
         const T *lv = (const T *)(rb + R.o_lv);
         const T *rhs = (const T *)(rb + R.o_rhs);
         T *hb = hand + (l & 1) * (PS_MAXQ * PS_CT);
 #pragma unroll
         for (int j = 0; j < PS_MAXQ; ++j) {
             const int p = j * PS_CT + ct;
-            if (p >= cnt || info[p].z < 0) continue;
-            T sum = (MODE == SW_FWD_DIV) ? rhs[p] : Sc<T>::zero();
-            for (int g = sbeg[p]; g < sbeg[p + 1]; ++g) sum = sum + tp[g];
+            if (j >= npass) continue;
+            const int4 ri = info[p];
+            if (ri.z < 0) continue;
+            const int e = ri.x, nold = ri.y & 0xFFFF;
+            T s0 = (MODE == SW_FWD_DIV) ? rhs[p] : Sc<T>::zero(), s1 = Sc<T>::zero();
+            int k = 0;
+            if (!hasg) {
+                // every read from shared memory: no branch, the loads run ahead of the sums
+#pragma unroll 2
+                for (; k + 2 <= nold; k += 2) {
+                    const int i0 = e + 32 * k;
+                    s0 = madd(s0, -val[i0], X[-1 - code[i0]]);
+                    s1 = madd(s1, -val[i0 + 32], X[-1 - code[i0 + 32]]);
+                }
+                if (k < nold) {
+                    const int i = e + 32 * k;
+                    s0 = madd(s0, -val[i], X[-1 - code[i]]);
+                }
+            } else {
+                for (; k + 2 <= nold; k += 2) {
+                    const int i0 = e + 32 * k;
+                    const int c0 = code[i0], c1 = code[i0 + 32];
+                    const T x0 = c0 < 0 ? X[-1 - c0] : ps_ldg(out + c0);
+                    const T x1 = c1 < 0 ? X[-1 - c1] : ps_ldg(out + c1);
+                    s0 = madd(s0, -val[i0], x0);
+                    s1 = madd(s1, -val[i0 + 32], x1);
+                }
+                if (k < nold) {
+                    const int i = e + 32 * k, c = code[i];
+                    s0 = madd(s0, -val[i], c < 0 ? X[-1 - c] : ps_ldg(out + c));
+                }
+            }
+            const T sum = s0 + s1;
             const T d = lv[p];
             hb[p] = (MODE == SW_FWD_DIV) ? sum * d : madd(rhs[p], d, sum);
         }
@@ -386,21 +353,20 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_sweep_push(PsArgs a) {
             }
             continue;
         }
-        if (!newg) {
-            // older entries of level l+1 (the receive phase of level l-1 is waited for inside)
-            if (l + 1 < nlev) old_part(l + 1);
-            continue;
-        }
-        // values other CTAs produced at level l-1 have landed
+        // values other CTAs produced at level l-1 have landed (both groups read them)
         if (l >= 1 && !wait_phase(mbr + 8u * ((l - 1) % L.R), (unsigned)(((l - 1) / L.R) & 1), true)) {
             bad = true;
+            continue;
+        }
+        if (!newg) {
+            if (l + 1 < nlev) old_part(l + 1);
             continue;
         }
         const int b = l % L.NB;
         const unsigned char *rb = ps_smem + L.o_buf + b * bufb;
         const int *hd = (const int *)rb;
         const int cnt = hd[0], npass = hd[3] & 0xFFFF;
-        const PsRec R = ps_rec(npass, hd[1], hd[5], hd[2], VB);
+        const PsRec R = ps_rec(npass, hd[1], hd[2], VB);
         const int4 *info = (const int4 *)(rb + R.o_info);
         const int *code = (const int *)(rb + R.o_code);
         const int *push = (const int *)(rb + R.o_push);
@@ -413,10 +379,10 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_sweep_push(PsArgs a) {
             if (j >= npass) continue;
             const int4 ri = info[p];
             if (ri.z < 0) continue;
-            const int e = ri.x, nnew = ri.y;
+            const int e = ri.x, nold = ri.y & 0xFFFF, len = ri.y >> 16;
             T res = hb[p];
             // the newest entries always come from shared memory (the plan guarantees it)
-            for (int k = 0; k < nnew; ++k) {
+            for (int k = nold; k < len; ++k) {
                 const int i = e + 32 * k;
                 res = madd(res, val[i], X[-1 - code[i]]);
             }

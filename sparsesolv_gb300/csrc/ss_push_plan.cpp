@@ -37,8 +37,6 @@ PushLayout push_layout(int S_own, int S_recv, int cap_rec, int elem, int NB) {
     o += ps_al16((S_own + S_recv) * elem);
     L.o_base = o;  // partial sums handed from the older-entry group to the newest-entry group, two levels
     o += ps_al16(2 * PS_MAXQ * PS_CT * elem);
-    L.o_tp = o;  // the older-entry group's segment partials of one record
-    o += ps_al16(PS_SEGMAX * elem);
     L.o_mbr = o;
     o += ps_al16(8 * L.R);
     L.o_mbs = o;
@@ -162,38 +160,26 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
     std::vector<int> pptr(n + 1, 0);
     for (auto &p : pushes) pptr[p.pj + 1]++;
     for (int t = 0; t < n; ++t) pptr[t + 1] += pptr[t];
-    // records: per (pass, warp) slab widths of the newest entries; the older entries' run
-    // length E; sizes; the largest
+    // records: per (pass, warp) slab widths; sizes; the largest
     std::vector<int> K;
     auto slab_widths = [&](int rs, int re) {
         const int cnt = re - rs, npass = (cnt + PS_CT - 1) / PS_CT;
         K.assign((size_t)npass * 4, 0);
         for (int q = 0; q < cnt; ++q) {
             const int j = q / PS_CT, w = (q % PS_CT) / 32;
-            K[j * 4 + w] = std::max(K[j * 4 + w], sprp[rs + q + 1] - sprp[rs + q] - nsp[rs + q]);
+            K[j * 4 + w] = std::max(K[j * 4 + w], sprp[rs + q + 1] - sprp[rs + q]);
         }
         int ne = 0;
         for (int v : K) ne += 32 * v;
         return ne;
     };
-    // pieces of the chunk's rows and pieces per thread
-    auto pieces_of = [&](int rs, int re, int &W, int &npc) {
-        W = 0;
-        npc = 0;
-        for (int t = rs; t < re; ++t) {
-            W += nsp[t];
-            npc += (nsp[t] + PS_PIECE - 1) / PS_PIECE;
-        }
-        return (npc + PS_CT - 1) / PS_CT;
-    };
-    int cap_rec = 32, cnt_max = 0;
+    int cap_rec = 16, cnt_max = 0;
     for (int l = 0; l < nlev; ++l)
         for (int c = 0; c < C; ++c) {
-            int rs, re, W, npc;
+            int rs, re;
             chunk_of(l, c, rs, re);
-            const int ne = slab_widths(rs, re), npt = pieces_of(rs, re, W, npc);
-            if (npt > PS_NPT) return fail("a level chunk has more older entries than the threads hold");
-            const PsRec r = ps_rec((re - rs + PS_CT - 1) / PS_CT, ne, npt, pptr[re] - pptr[rs], elem);
+            const int ne = slab_widths(rs, re);
+            const PsRec r = ps_rec((re - rs + PS_CT - 1) / PS_CT, ne, pptr[re] - pptr[rs], elem);
             cap_rec = std::max(cap_rec, r.size);
             cnt_max = std::max(cnt_max, re - rs);
         }
@@ -235,14 +221,13 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
     dlv.assign(n, 0);
     drhs.assign(n, 0);
     long long off = 0;
-    std::vector<int> segrow;  // per record: row of each piece
     for (int l = 0; l < nlev; ++l)
         for (int c = 0; c < C; ++c) {
-            int rs, re, W, npc;
+            int rs, re;
             chunk_of(l, c, rs, re);
             const int cnt = re - rs, npass = (cnt + PS_CT - 1) / PS_CT, np = pptr[re] - pptr[rs];
-            const int ne = slab_widths(rs, re), npt = pieces_of(rs, re, W, npc);
-            const PsRec r = ps_rec(npass, ne, npt, np, elem);
+            const int ne = slab_widths(rs, re);
+            const PsRec r = ps_rec(npass, ne, np, elem);
             if (off + r.size >= (1ll << 31)) return fail("records exceed 2 GB");
             if (bin[(size_t)l * C + c] >= (1 << 20)) return fail("a level pushes more bytes than a barrier counts");
             int *tr = &tab[((size_t)l * C + c) * 4];
@@ -251,52 +236,15 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
             tr[2] = (int)bin[(size_t)l * C + c];
             const size_t w0 = (size_t)(off / 4);
             rec.resize(w0 + r.size / 4, 0);
-            const int vbase = (int)((off + r.o_val) / elem);
-            // older entries: pieces cut from each row's end, right-aligned, dealt npt to a thread
-            segrow.clear();
-            bool hasg = false;  // an older entry read from the output vector (the kernel's slow path)
-            {
-                int pc = 0;
-                for (int t = rs; t < re; ++t) {
-                    const int nold = nsp[t], lt = level[perm[t]];
-                    for (int e0 = 0; e0 < nold;) {
-                        const int sz = (e0 == 0 && nold % PS_PIECE) ? nold % PS_PIECE : PS_PIECE;
-                        const int th = pc / npt, q = pc % npt;
-                        int *ti = &rec[w0 + (r.o_tinfo + 16 * th) / 4];
-                        ti[0] |= (sz - 1) << (2 * q);
-                        for (int j = PS_PIECE - sz, e = sprp[t] + e0; j < PS_PIECE; ++j, ++e) {
-                            const int slot = ne + (PS_PIECE * q + j) * PS_CT + th;
-                            rec[w0 + r.o_code / 4 + slot] = code[e];
-                            hasg = hasg || code[e] >= 0;
-                            dval[e] = vbase + slot;
-                            if (level[dep[e]] == lt - 2) ti[1] |= 1 << (PS_PIECE * q + j);
-                        }
-                        segrow.push_back(t - rs);
-                        ++pc;
-                        e0 += sz;
-                    }
-                }
-                if (pc != npc) return fail("piece count mismatch");
-            }
-            const int nseg = (int)segrow.size();
-            if (nseg > PS_SEGMAX) return fail("a record has more segments than the partials hold");
             rec[w0 + 0] = cnt;
             rec[w0 + 1] = ne;
             rec[w0 + 2] = np;
+            bool hasg = false;  // an older entry read from the output vector (the kernel's slow path)
+            for (int t = rs; t < re; ++t)
+                for (int k = sprp[t]; k < sprp[t + 1]; ++k) hasg = hasg || code[k] >= 0;
             rec[w0 + 3] = npass | ((hasg ? 1 : 0) << 16);
-            rec[w0 + 4] = W;
-            rec[w0 + 5] = npt;
-            rec[w0 + 6] = nseg;
             const int slots = npass * PS_CT;
-            {
-                int *sb = &rec[w0 + r.o_sbeg / 4];
-                int g = 0;
-                for (int q = 0; q <= slots; ++q) {
-                    while (g < nseg && segrow[g] < q) ++g;
-                    sb[q] = g;
-                }
-            }
-            std::vector<int> slab(npass * 4, 0);  // first newest slot of each (pass, warp) slab
+            std::vector<int> slab(npass * 4, 0);  // first entry slot of each (pass, warp) slab
             for (int i = 0, acc = 0; i < npass * 4; ++i) {
                 slab[i] = acc;
                 acc += 32 * K[i];
@@ -312,14 +260,14 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
                     continue;
                 }
                 const int j = q / PS_CT, w = (q % PS_CT) / 32, lane = q % 32;
-                const int t = rs + q, e0 = sprp[t] + nsp[t], nnew = sprp[t + 1] - e0;
+                const int t = rs + q, e0 = sprp[t], len = sprp[t + 1] - e0;
                 const int first = slab[j * 4 + w] + lane;
                 ri[0] = first;
-                ri[1] = nnew;
+                ri[1] = nsp[t] | (len << 16);
                 ri[2] = perm[t];
-                for (int k = 0; k < nnew; ++k) {
+                for (int k = 0; k < len; ++k) {
                     rec[w0 + r.o_code / 4 + first + 32 * k] = code[e0 + k];
-                    dval[e0 + k] = vbase + first + 32 * k;
+                    dval[e0 + k] = (int)((off + r.o_val) / elem) + first + 32 * k;
                 }
                 for (int k = pptr[t]; k < pptr[t + 1]; ++k) rec[w0 + r.o_push / 4 + pnext++] = plist[k];
                 dlv[t] = (int)((off + r.o_lv) / elem) + q;

@@ -52,18 +52,15 @@ int pp_consts(int *out) {
     return 7;
 }
 
-// record section offsets for (passes, newest entry slots, run length, pushes, elem):
-// info, sbeg, tinfo, code, push, val, lv, rhs, size
-void pp_rec(int npass, int ne, int E, int np, int elem, int *out) {
-    const ssg::PsRec r = ssg::ps_rec(npass, ne, E, np, elem);
+// record section offsets for (passes, entry slots, pushes, elem): info, code, push, val, lv, rhs, size
+void pp_rec(int npass, int ne, int np, int elem, int *out) {
+    const ssg::PsRec r = ssg::ps_rec(npass, ne, np, elem);
     out[0] = r.o_info;
-    out[1] = r.o_sbeg;
-    out[2] = r.o_tinfo;
-    out[3] = r.o_code;
-    out[4] = r.o_push;
-    out[5] = r.o_val;
-    out[6] = r.o_lv;
-    out[7] = r.o_rhs;
-    out[8] = r.size;
+    out[1] = r.o_code;
+    out[2] = r.o_push;
+    out[3] = r.o_val;
+    out[4] = r.o_lv;
+    out[5] = r.o_rhs;
+    out[6] = r.size;
 }
 }

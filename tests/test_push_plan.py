@@ -53,8 +53,8 @@ def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
-LAYOUT = ["S_own", "S_recv", "R", "NB", "LEAD", "cap_rec", "o_x", "o_base", "o_tp", "o_mbr", "o_mbs", "o_prog",
-          "o_tabring", "o_buf", "total"]
+LAYOUT = ["S_own", "S_recv", "R", "NB", "LEAD", "cap_rec", "o_x", "o_base", "o_mbr", "o_mbs", "o_prog", "o_tabring",
+          "o_buf", "total"]
 
 
 def plan(lib, tri, C, elem):
@@ -79,10 +79,10 @@ def plan(lib, tri, C, elem):
     return out
 
 
-def rec_layout(lib, npass, ne, E, np_, elem):
-    o = np.zeros(9, np.int32)
-    lib.pp_rec(ctypes.c_int(npass), ctypes.c_int(ne), ctypes.c_int(E), ctypes.c_int(np_), ctypes.c_int(elem), _p(o))
-    return dict(zip(["info", "sbeg", "tinfo", "code", "push", "val", "lv", "rhs", "size"], o.tolist()))
+def rec_layout(lib, npass, ne, np_, elem):
+    o = np.zeros(7, np.int32)
+    lib.pp_rec(ctypes.c_int(npass), ctypes.c_int(ne), ctypes.c_int(np_), ctypes.c_int(elem), _p(o))
+    return dict(zip(["info", "code", "push", "val", "lv", "rhs", "size"], o.tolist()))
 
 
 def level_ordered(oracle, rp, ci, lower):
@@ -111,9 +111,7 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
     NS = S_own + S_recv
     assert R >= LEAD + 2 and P["total"] <= k["SMEM_MAX"] and P["cnt_max"] <= k["CT"] * k["MAXQ"]
     assert P["o_buf"] + P["NB"] * (-(-P["cap_rec"] // 16) * 16) == P["total"] and P["o_x"] % 16 == 0
-    assert P["o_base"] >= NS * elem and P["o_tp"] - P["o_base"] >= 2 * k["MAXQ"] * k["CT"] * elem
-    assert P["o_mbr"] - P["o_tp"] >= 8 * k["CT"] * elem
-    CT = k["CT"]
+    assert P["o_base"] >= NS * elem and P["o_mbr"] - P["o_base"] >= 2 * k["MAXQ"] * k["CT"] * elem
     assert P["o_buf"] % 16 == 0
     tab = P["tab"].reshape(nlev, C, 4)
     rec = P["rec"]
@@ -151,103 +149,54 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
             prev_end = off + size
             w = off // 4
             cnt, ne, np_, npass = rec[w], rec[w + 1], rec[w + 2], rec[w + 3] & 0xFFFF
-            W, E, nseg = rec[w + 4], rec[w + 5], rec[w + 6]
-            assert cnt == re - rs and npass == -(-cnt // CT)
-            Lr = rec_layout(lib, npass, ne, E, np_, elem)
+            assert cnt == re - rs and npass == -(-cnt // k["CT"])
+            Lr = rec_layout(lib, npass, ne, np_, elem)
             assert Lr["size"] == size
-            slots = npass * CT
+            slots = npass * k["CT"]
             info = rec[w + Lr["info"] // 4: w + Lr["info"] // 4 + 4 * (slots + 1)].reshape(slots + 1, 4)
             assert tuple(info[slots]) == (ne, 0, -1, np_)
-            sbeg = rec[w + Lr["sbeg"] // 4: w + Lr["sbeg"] // 4 + slots + 1]
-            tinfo = rec[w + Lr["tinfo"] // 4: w + Lr["tinfo"] // 4 + 4 * CT].reshape(CT, 4)
-            code = rec[w + Lr["code"] // 4: w + Lr["code"] // 4 + ne + 4 * E * CT]
+            code = rec[w + Lr["code"] // 4: w + Lr["code"] // 4 + ne]
+            hasg = any(code[info[q, 0] + 32 * kk] >= 0 for q in range(cnt) for kk in range(info[q, 1] >> 16))
+            assert (rec[w + 3] >> 16) == int(hasg)  # the record's flag: some entry read from memory
             push = rec[w + Lr["push"] // 4: w + Lr["push"] // 4 + np_]
-            vbase = (off + Lr["val"]) // elem
             assert np.all(np.diff(info[:, 3]) >= 0)
             assert np.all(code >= -NS) and np.all(code < n)
             cons, slot = push >> 24, push & 0xFFFFFF
             assert np.all((cons >= 0) & (cons < C) & (cons != c)) and np.all(slot < S_recv)
-            # rows: sorted entries, older / newest split
-            rows = []
-            for q in range(cnt):
+            for q in range(slots):
+                first, nl, rid, p0 = info[q]
+                if q >= cnt:
+                    assert rid == -1 and info[q + 1, 3] == p0
+                    continue
                 t = rs + q
                 i = perm[t]
+                assert rid == i
                 lt = level[i]
-                g0, ln = sprp_g[t], prp[t + 1] - prp[t] - 1
+                nold, ln = nl & 0xFFFF, nl >> 16
+                assert first % 32 == q % 32 and (ln == 0 or first + 32 * (ln - 1) < ne)
+                eidx = first + 32 * np.arange(ln)
+                g0 = sprp_g[t]
+                assert np.array_equal(dval[g0:g0 + ln], (off + Lr["val"]) // elem + eidx)
+                assert dlv[t] == (off + Lr["lv"]) // elem + q and drhs[t] == (off + Lr["rhs"]) // elem + q
                 deps = pci[vmap[g0:g0 + ln]]
                 assert np.all(level[deps] < lt) and np.all(deps != i)
                 ld = level[deps]
                 assert np.all(np.diff(ld.astype(np.int64) * (n + 1) + deps) > 0)  # sorted (level, column)
-                nold = int(np.sum(ld < lt - 1))
-                assert np.all(ld[nold:] == lt - 1)
-                rows.append((t, i, lt, g0, ln, nold, deps))
+                assert np.all(ld[:nold] < lt - 1) and np.all(ld[nold:] == lt - 1)
                 newest.update((g0 + kk, t) for kk in range(nold, ln))
-            def read(cd, d_, lt, older):
-                if cd >= 0:
-                    assert older and cd == d_  # memory only for older entries
-                    if owner[ipos[d_]] != c:
-                        assert lt - level[d_] >= LEAD + 2
-                else:
-                    sl = -1 - cd
-                    assert tag[c, sl] == d_, (l, c, sl)
-                    key = (c, sl, d_)
-                    lastread[key] = max(lastread.get(key, -1), lt)
-                return y[d_]
-            # older entries: pieces of PIECE cut from each row's end (the first may be
-            # shorter), right-aligned, dealt npt consecutive pieces to a thread
-            PIECE = 4
-            pieces = []
-            for q in range(cnt):
-                nold_ = rows[q][5]
-                e0 = 0
-                while e0 < nold_:
-                    sz = nold_ % PIECE if (e0 == 0 and nold_ % PIECE) else PIECE
-                    pieces.append((q, e0, sz))
-                    e0 += sz
-            assert W == sum(rw[5] for rw in rows)
-            npt_ = -(-len(pieces) // CT)
-            assert E == npt_ and E <= 8  # header word 5: pieces per thread
-            part, segrow, hasg = [], [], False
-            want_t = np.zeros((CT, 2), np.int64)
-            for pc, (q, e0, sz) in enumerate(pieces):
-                th, qq = pc // npt_, pc % npt_
-                t, i, lt, g0, ln, nold, deps = rows[q]
-                want_t[th, 0] |= (sz - 1) << (2 * qq)
-                segrow.append(q)
-                acc = 0.0
-                for jj in range(sz):
-                    j = PIECE - sz + jj
-                    kk = e0 + jj
-                    if level[deps[kk]] == lt - 2:
-                        want_t[th, 1] |= 1 << (PIECE * qq + j)
-                    sl_ = ne + (PIECE * qq + j) * CT + th
-                    cd = code[sl_]
-                    hasg = hasg or cd >= 0
-                    assert dval[g0 + kk] == vbase + sl_
-                    acc -= vals_lo[vmap[g0 + kk]] * read(cd, deps[kk], lt, True)
-                part.append(acc)
-            for th in range(CT):
-                assert (int(tinfo[th, 0]) & 0xFFFFFFFF) == want_t[th, 0] and (int(tinfo[th, 1]) & 0xFFFFFFFF) == want_t[th, 1]
-                assert tinfo[th, 2] == 0 and tinfo[th, 3] == 0
-            assert nseg == len(part) and nseg <= 8 * CT
-            assert (rec[w + 3] >> 16) == int(hasg)  # the record's flag: some older entry read from memory
-            assert np.all(np.diff(segrow) >= 0)
-            for q in range(slots + 1):
-                assert sbeg[q] == sum(1 for g in segrow if g < q)
-            for q in range(slots):
-                first, nnew, rid, p0 = info[q]
-                if q >= cnt:
-                    assert rid == -1 and info[q + 1, 3] == p0 and sbeg[q] == sbeg[q + 1]
-                    continue
-                t, i, lt, g0, ln, nold, deps = rows[q]
-                assert rid == i and nnew == ln - nold
-                assert first % 32 == q % 32 and (nnew == 0 or first + 32 * (nnew - 1) < ne)
-                s_ = r[i] + sum(part[sbeg[q]:sbeg[q + 1]])
-                for kk in range(nold, ln):
-                    sl_ = first + 32 * (kk - nold)
-                    assert dval[g0 + kk] == vbase + sl_
-                    s_ -= vals_lo[vmap[g0 + kk]] * read(code[sl_], deps[kk], lt, False)
-                assert dlv[t] == (off + Lr["lv"]) // elem + q and drhs[t] == (off + Lr["rhs"]) // elem + q
+                s_ = r[i]
+                for kk, d_ in enumerate(deps):
+                    cd = code[eidx[kk]]
+                    if cd >= 0:
+                        assert cd == d_ and ld[kk] < lt - 1  # memory only for older entries
+                        if owner[ipos[d_]] != c:
+                            assert lt - level[d_] >= LEAD + 2
+                    else:
+                        sl = -1 - cd
+                        assert tag[c, sl] == d_, (l, c, q, sl)
+                        key = (c, sl, d_)
+                        lastread[key] = max(lastread.get(key, -1), lt)
+                    s_ -= vals_lo[vmap[g0 + kk]] * y[d_]
                 osl = (produced[c] + q) % S_own
                 writes.append((c, osl, tag[c, osl], l, True))
                 tag[c, osl] = i
