@@ -39,7 +39,6 @@
 // records ERR_TIMEOUT, every CTA leaves its level loop at the next step, waits
 // for the copies it issued and for the pushes in flight, and returns.
 #include <algorithm>
-#include <type_traits>
 
 #include "sparsesolv_gb300.h"
 #include "ss_internal.cuh"
@@ -164,7 +163,7 @@ struct PsArgs {
 };
 
 template <typename T, int MODE>
-__global__ void __launch_bounds__(PS_THREADS, 1) k_sweep_push(PsArgs a) {
+__global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
     if (a.st && !a.st->active) return;  // uniform across the cluster
     extern __shared__ __align__(16) unsigned char ps_smem[];
     const PushLayout &L = a.L;
@@ -247,77 +246,64 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_sweep_push(PsArgs a) {
     int produced = 0;  // values this CTA has produced (own ring position)
     // Older entries of level l's rows, by the older-entry group during step l-1 (the
     // entries of levels <= l-2), scaled so that each newest entry is one fused
-    // multiply-add after the wait (the newest values are stored pre-scaled). A row's
-    // older entries go alternately into two partial sums (entry k into s[k & 1]); within
-    // each warp the rows are right-aligned by an even shift (entry k at step
-    // shift + k, shift = (longest - own) rounded down to even), so that the entries of
-    // dependency level l-2, the last of each row, come last for every lane: the warp
-    // waits for the pushes of level l-2 once, just before the first step that reads one.
-    // The alignment moves no entry between the partial sums, so a row's arithmetic
-    // depends on the row alone. Every lane of a warp runs the same steps (the warp-wide
-    // reductions), also after a failed wait.
+    // multiply-add after the wait; the newest values are rescaled in place in the
+    // staged record.
     auto old_part = [&](int l) {
         const int b = l % L.NB;
-        const bool ok = !bad && wait_phase(mbs + 8u * b, (unsigned)((l / L.NB) & 1), false);
-        if (!ok) bad = true;
-        const unsigned char *rb = ps_smem + L.o_buf + b * bufb;
+        if (!wait_phase(mbs + 8u * b, (unsigned)((l / L.NB) & 1), false)) {
+            bad = true;
+            return;
+        }
+        unsigned char *rb = ps_smem + L.o_buf + b * bufb;
         const int *hd = (const int *)rb;
-        const int npass = ok ? hd[3] & 0xFFFF : 0;
-        const bool hasg = ok && (hd[3] >> 16) != 0;
-        const PsRec R = ps_rec(npass, ok ? hd[1] : 0, ok ? hd[2] : 0, VB);
+        const int npass = hd[3] & 0xFFFF;
+        const bool hasg = (hd[3] >> 16) != 0;
+        const PsRec R = ps_rec(npass, hd[1], hd[2], VB);
         const int4 *info = (const int4 *)(rb + R.o_info);
         const int *code = (const int *)(rb + R.o_code);
         const T *val = (const T *)(rb + R.o_val);
         const T *lv = (const T *)(rb + R.o_lv);
         const T *rhs = (const T *)(rb + R.o_rhs);
         T *hb = hand + (l & 1) * (PS_MAXQ * PS_CT);
-        // the receive phase of producer level l-2
-        bool waited = l < 2;
-        const unsigned rbar = mbr + 8u * ((l + 2 * L.R - 2) % L.R);
-        const unsigned rpar = (unsigned)(((l - 2) / L.R) & 1);
-        auto recv = [&]() {
-            if (!waited && !bad && !wait_phase(rbar, rpar, true)) bad = true;
-            waited = true;
-        };
-        const int passes = __reduce_max_sync(0xffffffffu, npass);
-        for (int j = 0; j < passes; ++j) {
+#pragma unroll
+        for (int j = 0; j < PS_MAXQ; ++j) {
             const int p = j * PS_CT + ct;
-            const int4 ri = j < npass ? info[p] : make_int4(0, 0, -1, 0);
-            const bool row = ri.z >= 0;
-            const int e = ri.x & 0xFFFF, nd2 = row ? (ri.x >> 16) : 0, nold = row ? (ri.y & 0xFFFF) : 0;
-            const int ko = __reduce_max_sync(0xffffffffu, nold);
-            const int shift = (ko - nold) & ~1;
-            const int kw = __reduce_min_sync(0xffffffffu, nd2 > 0 ? shift + nold - nd2 : 0x7FFFFFFF);
-            T s0 = (MODE == SW_FWD_DIV && row) ? rhs[p] : Sc<T>::zero(), s1 = Sc<T>::zero();
-            auto pair = [&](auto mem) {
-                for (int k = 0; k < ko; k += 2) {
-                    if (kw < k + 2) recv();
-                    const int k0 = k - shift, i0 = e + 32 * k0;
-                    if (k0 >= 0 && k0 < nold) {
-                        const int c = code[i0];
-                        T x;
-                        if (decltype(mem)::value) x = c < 0 ? X[-1 - c] : ps_ldg(out + c);
-                        else x = X[-1 - c];
-                        s0 = madd(s0, -val[i0], x);
-                    }
-                    if (k0 + 1 >= 0 && k0 + 1 < nold) {
-                        const int c = code[i0 + 32];
-                        T x;
-                        if (decltype(mem)::value) x = c < 0 ? X[-1 - c] : ps_ldg(out + c);
-                        else x = X[-1 - c];
-                        s1 = madd(s1, -val[i0 + 32], x);
-                    }
+            if (j >= npass) continue;
+            const int4 ri = info[p];
+            if (ri.z < 0) continue;
+            const int e = ri.x, nold = ri.y & 0xFFFF;
+            T s0 = (MODE == SW_FWD_DIV) ? rhs[p] : Sc<T>::zero(), s1 = Sc<T>::zero();
+            int k = 0;
+            if (!hasg) {
+                // every read from shared memory: no branch, the loads run ahead of the sums
+#pragma unroll 2
+                for (; k + 2 <= nold; k += 2) {
+                    const int i0 = e + 32 * k;
+                    s0 = madd(s0, -val[i0], X[-1 - code[i0]]);
+                    s1 = madd(s1, -val[i0 + 32], X[-1 - code[i0 + 32]]);
                 }
-            };
-            if (hasg) pair(std::true_type{});
-            else pair(std::false_type{});
-            if (row) {
-                const T sum = s0 + s1;
-                const T d = lv[p];
-                hb[p] = (MODE == SW_FWD_DIV) ? sum * d : madd(rhs[p], d, sum);
+                if (k < nold) {
+                    const int i = e + 32 * k;
+                    s0 = madd(s0, -val[i], X[-1 - code[i]]);
+                }
+            } else {
+                for (; k + 2 <= nold; k += 2) {
+                    const int i0 = e + 32 * k;
+                    const int c0 = code[i0], c1 = code[i0 + 32];
+                    const T x0 = c0 < 0 ? X[-1 - c0] : ps_ldg(out + c0);
+                    const T x1 = c1 < 0 ? X[-1 - c1] : ps_ldg(out + c1);
+                    s0 = madd(s0, -val[i0], x0);
+                    s1 = madd(s1, -val[i0 + 32], x1);
+                }
+                if (k < nold) {
+                    const int i = e + 32 * k, c = code[i];
+                    s0 = madd(s0, -val[i], c < 0 ? X[-1 - c] : ps_ldg(out + c));
+                }
             }
+            const T sum = s0 + s1;
+            const T d = lv[p];
+            hb[p] = (MODE == SW_FWD_DIV) ? sum * d : madd(rhs[p], d, sum);
         }
-        recv();
     };
 
     if (!newg && !stager && nlev > 0) old_part(0);
@@ -367,14 +353,13 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_sweep_push(PsArgs a) {
             }
             continue;
         }
-        if (!newg) {
-            // older entries of level l+1 (the receive phase of level l-1 is waited for inside)
-            if (l + 1 < nlev) old_part(l + 1);
-            continue;
-        }
-        // values other CTAs produced at level l-1 have landed
+        // values other CTAs produced at level l-1 have landed (both groups read them)
         if (l >= 1 && !wait_phase(mbr + 8u * ((l - 1) % L.R), (unsigned)(((l - 1) / L.R) & 1), true)) {
             bad = true;
+            continue;
+        }
+        if (!newg) {
+            if (l + 1 < nlev) old_part(l + 1);
             continue;
         }
         const int b = l % L.NB;
@@ -394,7 +379,7 @@ __global__ void __launch_bounds__(PS_THREADS, 1) k_sweep_push(PsArgs a) {
             if (j >= npass) continue;
             const int4 ri = info[p];
             if (ri.z < 0) continue;
-            const int e = ri.x & 0xFFFF, nold = ri.y & 0xFFFF, len = ri.y >> 16;
+            const int e = ri.x, nold = ri.y & 0xFFFF, len = ri.y >> 16;
             T res = hb[p];
             // the newest entries always come from shared memory (the plan guarantees it)
             for (int k = nold; k < len; ++k) {

@@ -262,10 +262,7 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
                 const int j = q / PS_CT, w = (q % PS_CT) / 32, lane = q % 32;
                 const int t = rs + q, e0 = sprp[t], len = sprp[t + 1] - e0;
                 const int first = slab[j * 4 + w] + lane;
-                int nd2 = 0;  // older entries two levels below the row (sorted last among the older)
-                for (int k = e0; k < e0 + nsp[t]; ++k) nd2 += level[dep[k]] == level[perm[t]] - 2;
-                if (first >= (1 << 16) || nd2 >= (1 << 16)) return fail("a record has more entry slots than the row info holds");
-                ri[0] = first | (nd2 << 16);
+                ri[0] = first;
                 ri[1] = nsp[t] | (len << 16);
                 ri[2] = perm[t];
                 for (int k = 0; k < len; ++k) {

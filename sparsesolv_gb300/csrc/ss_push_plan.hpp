@@ -35,10 +35,9 @@ SSG_HD inline int ps_al16(int x) { return (x + 15) & ~15; }
 // Byte offsets from the record's start, each section 16-byte aligned:
 //   [0]       header: rows cnt, entry slots ne, pushes np, passes npass | (some entry
 //             read from memory) << 16
-//   [16]      row info, npass * PS_CT int4 by row: {first entry slot | (older entries of
-//             dependency level two below the row: the last of its older entries) << 16,
-//             old | all entries << 16, row id (-1: no row), first push}; a row's pushes
-//             run to the next row's first push (one closing int4 after the last slot)
+//   [16]      row info, npass * PS_CT int4 by row: {first entry slot, old | all entries << 16,
+//             row id (-1: no row), first push}; a row's pushes run to the next row's
+//             first push (one closing int4 after the last slot)
 //   codes     ne ints: >= 0 the output vector's row, < 0 shared-memory slot -1 - code
 //             (own ring [0, S_own), then the receive ring)
 //   pushes    np ints: consumer << 24 | receive slot

@@ -156,7 +156,7 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
             info = rec[w + Lr["info"] // 4: w + Lr["info"] // 4 + 4 * (slots + 1)].reshape(slots + 1, 4)
             assert tuple(info[slots]) == (ne, 0, -1, np_)
             code = rec[w + Lr["code"] // 4: w + Lr["code"] // 4 + ne]
-            hasg = any(code[(info[q, 0] & 0xFFFF) + 32 * kk] >= 0 for q in range(cnt) for kk in range(info[q, 1] >> 16))
+            hasg = any(code[info[q, 0] + 32 * kk] >= 0 for q in range(cnt) for kk in range(info[q, 1] >> 16))
             assert (rec[w + 3] >> 16) == int(hasg)  # the record's flag: some entry read from memory
             push = rec[w + Lr["push"] // 4: w + Lr["push"] // 4 + np_]
             assert np.all(np.diff(info[:, 3]) >= 0)
@@ -165,7 +165,6 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
             assert np.all((cons >= 0) & (cons < C) & (cons != c)) and np.all(slot < S_recv)
             for q in range(slots):
                 first, nl, rid, p0 = info[q]
-                nd2, first = first >> 16, first & 0xFFFF
                 if q >= cnt:
                     assert rid == -1 and info[q + 1, 3] == p0
                     continue
@@ -184,8 +183,6 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
                 ld = level[deps]
                 assert np.all(np.diff(ld.astype(np.int64) * (n + 1) + deps) > 0)  # sorted (level, column)
                 assert np.all(ld[:nold] < lt - 1) and np.all(ld[nold:] == lt - 1)
-                # the older entries of dependency level lt - 2 are the last nd2 of the older ones
-                assert nd2 == int(np.sum(ld[:nold] == lt - 2)) and np.all(ld[nold - nd2:nold] == lt - 2)
                 newest.update((g0 + kk, t) for kk in range(nold, ln))
                 s_ = r[i]
                 for kk, d_ in enumerate(deps):
