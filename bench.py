@@ -52,13 +52,24 @@ MAXIT = 20000
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel, from one ncu
-# capture of the same workload: profiles/k_sweep_cluster_80cube.md (cluster sweeps, the automatic mode's choice
-# here) and profiles/k_sweep_fwd_80cube.md (sync-free forward sweep)
+# capture of the same workload: profiles/k_sweep_push_80cube.md (push sweeps, the automatic mode's choice for
+# real values), profiles/k_sweep_cluster_80cube.md (lockstep cluster sweeps) and profiles/k_sweep_fwd_80cube.md
+# (sync-free forward sweep)
 NCU_TRAFFIC = {
+    ("cfg2", "fp64", "push", "forward sweep"): 473.8e6,
+    ("cfg2", "fp64", "push", "backward sweep"): 472.5e6,
     ("cfg2", "fp64", "cluster", "forward sweep"): 348.7e6,
     ("cfg2", "fp64", "cluster", "backward sweep"): 347.6e6,
     ("cfg2", "fp64", "sync-free", "forward sweep"): 360.6e6,
 }
+
+
+def sweep_kind(mode, cplx):
+    """The sweep schedule a mode runs: the automatic mode (0) takes the push sweep for real values and the
+    one-cluster lockstep sweep for complex ones, where their plans fit."""
+    if mode == 0:
+        return "cluster" if cplx else "push"
+    return {1: "sync-free", 2: "cluster", 3: "neighbour", 4: "push"}.get(mode, "cluster")
 
 
 def parse():
@@ -103,8 +114,36 @@ def workload(name):
         case, label = voxel.config3(), "eddy-current K + j omega sigma M, 60^3 voxels, complex128"
     else:
         case, label = voxel.config1(), "curl-curl 20^3 voxels, 1 seeded iron block"
+    t0 = time.perf_counter()
     rp, ci, val, b = case.assemble()
+    WORKLOAD_CASE[name] = (case, time.perf_counter() - t0)
     return label, rp, ci, val, b
+
+
+WORKLOAD_CASE = {}  # workload name -> (voxel case, seconds of its host assembly)
+
+
+def device_assembly(device, name, rp, ci, val, b):
+    """The same system assembled on the GPU (ssg_set_matrix_voxel) on a fresh handle: seconds (host maps and
+    element matrices, upload, assembly, scan), against the host generator's seconds, and whether pattern,
+    values and right-hand side are bit-identical to the host's."""
+    from sparsesolv_gb300 import _capi
+    case, t_host = WORKLOAD_CASE[name]
+    h = _capi.Handle(device)
+    try:
+        h.set_matrix_voxel(case)  # first call: the kernels' load
+        t0 = time.perf_counter()
+        bd = h.set_matrix_voxel(case)
+        t_dev = time.perf_counter() - t0
+        drp, dci, dva = h.get_matrix()
+        same = (np.array_equal(drp, rp) and np.array_equal(dci, ci) and
+                np.array_equal(dva.view(np.float64), np.asarray(val).view(np.float64)) and
+                np.array_equal(np.asarray(bd).view(np.float64), np.asarray(b).view(np.float64)))
+    finally:
+        h.close()
+    return {"host_generator_s": t_host, "device_s": t_dev, "speedup": t_host / t_dev, "bit_identical": bool(same),
+            "what": "the workload's matrix and right-hand side: host C generator (voxelgen.c) vs "
+                    "ssg_set_matrix_voxel into a handle (edge maps and element matrices from the host)"}
 
 
 def method_args(m):
@@ -461,9 +500,8 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_kind == "measured" else "fallback 6.8 TB/s",
-                     "traffic": None if K > 1 else NCU_TRAFFIC.get((args.workload, args.precision,
-                                                 {1: "sync-free", 3: "neighbour", 4: "push"}.get(
-                                                     tuned["mode"] if tuned else args.sweep_mode, "cluster"), dom)),
+                     "traffic": None if K > 1 else NCU_TRAFFIC.get((args.workload, args.precision, sweep_kind(
+                         tuned["mode"] if tuned else args.sweep_mode, np.iscomplexobj(val)), dom)),
                      "traffic_source": "ncu capture in profiles/ (per launch)", "algorithmic_bytes": dbytes / max(dlaunch, 1),
                      "launch_ms": dms / max(dlaunch, 1), "launches": dlaunch},
         "kernel_ms_per_step": {k: v[0] / args.steps for k, v in stats.items()},
@@ -475,6 +513,8 @@ def run_ours(args):
         return
     if ws == 1:
         line["new_pattern"] = new_pattern_solve(local, meth, pt, rp, ci, val, b1)
+        if K == 1 and args.workload in WORKLOAD_CASE:
+            line["assembly"] = device_assembly(local, args.workload, rp, ci, val, b1)
         ref = None
         if not args.no_cpu_baseline:
             ref = cpu_baseline(line, rp, ci, val, b1, args.method, pt, args.cpu_threads)
