@@ -187,6 +187,7 @@ void Handle::set_matrix_coo(int n_, int m, const int *rows, const int *cols, con
     pat_version = ~0ull;
     ltb_ready = ub_ready = false;
     fac_valid = sgs_valid = dad_valid = false;
+    note_row_lengths(nullptr);
 }
 
 }  // namespace ssg

@@ -63,7 +63,8 @@ int red_grid(int n);
 template <typename T>
 void k_spmv_launch(int n, int group, const int *rp, const int *ci, const T *val, const T *x, T *y, KState *st,
                    bool dot_alpha, double *part, cudaStream_t s);
-int spmv_group(int n, long long nnz, bool cplx);  // lanes a row from the mean row length
+int spmv_group(double rowlen, bool cplx);  // lanes a row from the nonzero-weighted median row length
+double spmv_rowlen(int n, const int *host_row_ptr);  // that length
 // ICCG: x += alpha p, r -= alpha Ap, |r| -> convergence decision
 template <typename T>
 void iccg_update(int n, KState *st, T *x, T *r, const T *p, const T *ap, double *part, double *log, cudaStream_t s);

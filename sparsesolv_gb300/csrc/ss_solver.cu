@@ -149,10 +149,24 @@ void Handle::set_matrix(int n_, int nnz_, const int32_t *rp, const int32_t *ci, 
         ++pattern_id;
         pat_version = ~0ull;
         ltb_ready = ub_ready = false;
+        note_row_lengths(kind == cudaMemcpyHostToDevice ? rp : nullptr);
     } else {
         pat_version = version;
     }
     fac_valid = sgs_valid = dad_valid = false;
+}
+
+// the SpMV's lanes a row follow the pattern's row-length distribution; rp on the host, or
+// null to read the device copy
+void Handle::note_row_lengths(const int32_t *host_rp) {
+    if (host_rp) {
+        spmv_len = spmv_rowlen(n, host_rp);
+        return;
+    }
+    std::vector<int> hrp((size_t)n + 1);
+    SSG_CUDA(cudaMemcpyAsync(hrp.data(), A_rp.p, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost, stream));
+    SSG_CUDA(cudaStreamSynchronize(stream));
+    spmv_len = spmv_rowlen(n, hrp.data());
 }
 
 void Handle::update_values(const double *val, cudaMemcpyKind kind) {

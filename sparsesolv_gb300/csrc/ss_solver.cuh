@@ -106,8 +106,10 @@ struct Handle {
                                    // 4 push (one cluster, no cluster-wide barrier; IC pair)
     unsigned long long fac_epoch = 0;  // bumped whenever the factor values change (push records refill)
     int batch_group = 0;           // lanes a row in the sweeps of the owning C handle's internal batch (0: auto)
-    int spmv_group_req = 0;        // lanes a row in the SpMV (0: from the mean row length)
-    int spmv_lanes() const { return spmv_group_req ? spmv_group_req : spmv_group(n, nnz, vtype == SSG_COMPLEX); }
+    int spmv_group_req = 0;        // lanes a row in the SpMV (0: from the row-length distribution)
+    double spmv_len = 0.0;         // nonzero-weighted median row length of the current pattern
+    int spmv_lanes() const { return spmv_group_req ? spmv_group_req : spmv_group(spmv_len, vtype == SSG_COMPLEX); }
+    void note_row_lengths(const int *host_rp);  // the pattern changed: its row-length distribution (host or device rp)
     // rows whose factor is a copy of another row's (a batch holds a system once per
     // right-hand side): only the rows without a source are factored
     DBuf rep_src;                  // [n] source row or -1

@@ -6,6 +6,9 @@
 // sum over the stored entries of row i. G lanes share a row (G from the mean
 // row length), consecutive groups take consecutive rows, so a warp streams a
 // contiguous stretch of the value and column arrays.
+#include <algorithm>
+#include <vector>
+
 #include "ss_internal.cuh"
 #include "ss_krylov.cuh"
 #include "ss_kdev.cuh"
@@ -123,16 +126,32 @@ __global__ void __launch_bounds__(RED_T) k_spmv(int n, const int *__restrict__ r
     }
 }
 
-// lanes a row from the mean row length: GB300 issues few FP64 operations per
-// clock, and every lane pays the butterfly adds and the padding of the last step,
-// so a lane takes about 8 real (16 complex) entries; measured on the 33-entry
-// rows of the voxel systems: 4 lanes 174 us, 8 lanes 233 us, 16 lanes 411 us
-// (80^3, real); 2 lanes 173 us, 4 lanes 195 us, 8 lanes 240 us (60^3, complex)
-int spmv_group(int n, long long nnz, bool cplx) {
-    const double lanes = (n ? (double)nnz / n : 0.0) / (cplx ? 16.0 : 8.0);
+// Lanes a row from the row-length distribution: the length at which half of the
+// nonzeros lie in rows of that length or shorter (the rows that carry the work),
+// divided by about 8 real (16 complex) entries a lane. GB300 issues few FP64
+// operations per clock, and every lane pays the butterfly adds and the padding of
+// its last step, while fewer lanes read the values and columns less coalesced;
+// measured on the 33-entry rows of the voxel systems: 2 lanes 191 us, 4 lanes
+// 173 us, 8 lanes 233 us, 16 lanes 411 us (80^3, real); 2 lanes 173 us, 4 lanes
+// 195 us, 8 lanes 240 us (60^3, complex).
+int spmv_group(double rowlen, bool cplx) {
+    const double lanes = rowlen / (cplx ? 16.0 : 8.0);
     int g = 2;
     while (g < 32 && 1.5 * g < lanes) g *= 2;
     return g;
+}
+
+// the nonzero-weighted median row length of a CSR pattern (host row pointers)
+double spmv_rowlen(int n, const int *rp) {
+    if (n <= 0 || rp[n] <= 0) return 0.0;
+    int mx = 0;
+    for (int i = 0; i < n; ++i) mx = std::max(mx, rp[i + 1] - rp[i]);
+    std::vector<long long> w((size_t)mx + 1, 0);
+    for (int i = 0; i < n; ++i) w[rp[i + 1] - rp[i]] += rp[i + 1] - rp[i];
+    long long acc = 0;
+    for (int len = 0; len <= mx; ++len)
+        if ((acc += w[len]) * 2 >= (long long)rp[n]) return (double)len;
+    return (double)mx;
 }
 
 template <typename T, int G>
