@@ -163,7 +163,7 @@ struct PsArgs {
 };
 
 template <typename T, int MODE>
-__global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
+__global__ void __launch_bounds__(PS_THREADS, 1) k_sweep_push(PsArgs a) {
     if (a.st && !a.st->active) return;  // uniform across the cluster
     extern __shared__ __align__(16) unsigned char ps_smem[];
     const PushLayout &L = a.L;
@@ -256,9 +256,9 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
         }
         unsigned char *rb = ps_smem + L.o_buf + b * bufb;
         const int *hd = (const int *)rb;
-        const int npass = hd[3] & 0xFFFF;
+        const int cnt = hd[0];
         const bool hasg = (hd[3] >> 16) != 0;
-        const PsRec R = ps_rec(npass, hd[1], hd[2], VB);
+        const PsRec R = ps_rec(cnt, hd[1], hd[2], VB);
         const int4 *info = (const int4 *)(rb + R.o_info);
         const int *code = (const int *)(rb + R.o_code);
         const T *val = (const T *)(rb + R.o_val);
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
 #pragma unroll
         for (int j = 0; j < PS_MAXQ; ++j) {
             const int p = j * PS_CT + ct;
-            if (j >= npass) continue;
+            if (p >= cnt) continue;
             const int4 ri = info[p];
             if (ri.z < 0) continue;
             const int e = ri.x, nold = ri.y & 0xFFFF;
@@ -365,8 +365,8 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
         const int b = l % L.NB;
         const unsigned char *rb = ps_smem + L.o_buf + b * bufb;
         const int *hd = (const int *)rb;
-        const int cnt = hd[0], npass = hd[3] & 0xFFFF;
-        const PsRec R = ps_rec(npass, hd[1], hd[2], VB);
+        const int cnt = hd[0];
+        const PsRec R = ps_rec(cnt, hd[1], hd[2], VB);
         const int4 *info = (const int4 *)(rb + R.o_info);
         const int *code = (const int *)(rb + R.o_code);
         const int *push = (const int *)(rb + R.o_push);
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(PS_THREADS) k_sweep_push(PsArgs a) {
 #pragma unroll
         for (int j = 0; j < PS_MAXQ; ++j) {
             const int p = j * PS_CT + ct;
-            if (j >= npass) continue;
+            if (p >= cnt) continue;
             const int4 ri = info[p];
             if (ri.z < 0) continue;
             const int e = ri.x, nold = ri.y & 0xFFFF, len = ri.y >> 16;

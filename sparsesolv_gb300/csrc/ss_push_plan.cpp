@@ -163,12 +163,9 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
     // records: per (pass, warp) slab widths; sizes; the largest
     std::vector<int> K;
     auto slab_widths = [&](int rs, int re) {
-        const int cnt = re - rs, npass = (cnt + PS_CT - 1) / PS_CT;
-        K.assign((size_t)npass * 4, 0);
-        for (int q = 0; q < cnt; ++q) {
-            const int j = q / PS_CT, w = (q % PS_CT) / 32;
-            K[j * 4 + w] = std::max(K[j * 4 + w], sprp[rs + q + 1] - sprp[rs + q]);
-        }
+        const int cnt = re - rs;
+        K.assign((size_t)ps_slots(cnt) / 32, 0);
+        for (int q = 0; q < cnt; ++q) K[q / 32] = std::max(K[q / 32], sprp[rs + q + 1] - sprp[rs + q]);
         int ne = 0;
         for (int v : K) ne += 32 * v;
         return ne;
@@ -179,7 +176,7 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
             int rs, re;
             chunk_of(l, c, rs, re);
             const int ne = slab_widths(rs, re);
-            const PsRec r = ps_rec((re - rs + PS_CT - 1) / PS_CT, ne, pptr[re] - pptr[rs], elem);
+            const PsRec r = ps_rec(re - rs, ne, pptr[re] - pptr[rs], elem);
             cap_rec = std::max(cap_rec, r.size);
             cnt_max = std::max(cnt_max, re - rs);
         }
@@ -225,9 +222,9 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
         for (int c = 0; c < C; ++c) {
             int rs, re;
             chunk_of(l, c, rs, re);
-            const int cnt = re - rs, npass = (cnt + PS_CT - 1) / PS_CT, np = pptr[re] - pptr[rs];
+            const int cnt = re - rs, npass = 1, np = pptr[re] - pptr[rs];
             const int ne = slab_widths(rs, re);
-            const PsRec r = ps_rec(npass, ne, np, elem);
+            const PsRec r = ps_rec(cnt, ne, np, elem);
             if (off + r.size >= (1ll << 31)) return fail("records exceed 2 GB");
             if (bin[(size_t)l * C + c] >= (1 << 20)) return fail("a level pushes more bytes than a barrier counts");
             int *tr = &tab[((size_t)l * C + c) * 4];
@@ -243,9 +240,9 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
             for (int t = rs; t < re; ++t)
                 for (int k = sprp[t]; k < sprp[t + 1]; ++k) hasg = hasg || code[k] >= 0;
             rec[w0 + 3] = npass | ((hasg ? 1 : 0) << 16);
-            const int slots = npass * PS_CT;
-            std::vector<int> slab(npass * 4, 0);  // first entry slot of each (pass, warp) slab
-            for (int i = 0, acc = 0; i < npass * 4; ++i) {
+            const int slots = ps_slots(cnt);
+            std::vector<int> slab(slots / 32, 0);  // first entry slot of each warp's slab
+            for (int i = 0, acc = 0; i < slots / 32; ++i) {
                 slab[i] = acc;
                 acc += 32 * K[i];
             }
@@ -259,9 +256,9 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
                     ri[2] = -1;
                     continue;
                 }
-                const int j = q / PS_CT, w = (q % PS_CT) / 32, lane = q % 32;
+                const int w = q / 32, lane = q % 32;
                 const int t = rs + q, e0 = sprp[t], len = sprp[t + 1] - e0;
-                const int first = slab[j * 4 + w] + lane;
+                const int first = slab[w] + lane;
                 ri[0] = first;
                 ri[1] = nsp[t] | (len << 16);
                 ri[2] = perm[t];

@@ -13,11 +13,11 @@
 
 namespace ssg {
 
-constexpr int PS_CT = 128;                  // threads of each compute group (one row each per pass)
+constexpr int PS_CT = 256;                  // threads of each compute group (one row each)
 // two compute groups (the newest entries of level l; the older entries of level l+1)
 // and one warp that stages records, arms barriers and watches progress
 constexpr int PS_THREADS = 2 * PS_CT + 32;
-constexpr int PS_MAXQ = 2;                  // rows a compute thread holds per level
+constexpr int PS_MAXQ = 1;                  // rows a compute thread holds per level
 constexpr int PS_SMEM_MAX = 220 * 1024;     // dynamic shared memory a CTA may use
 constexpr int PS_LEAD = 16;                 // levels a CTA may run ahead of the slowest
 constexpr int PS_R = PS_LEAD + 4;           // receive barriers (one per producer level, round robin)
@@ -27,29 +27,33 @@ constexpr int PS_S_OWN = 4096;              // own-ring slots at most
 SSG_HD inline int ps_al16(int x) { return (x + 15) & ~15; }
 
 // One level's chunk of one CTA as a contiguous record (staged with one bulk copy).
-// Row q of the chunk is held by thread q % PS_CT in pass q / PS_CT: rows fill warps
-// densely, because GB300's FP64 pipe costs a warp instruction whatever the number
-// of active lanes, so the fewest warps do a level's FP64 work in the fewest
-// instructions. Each warp's entries form a slab, entry k of lane's row at
-// slab + 32 * k + lane (ELL order: a warp's reads of entry k are consecutive).
+// Row q of the chunk is held by thread q of each compute group (at most PS_CT rows,
+// one pass): rows fill warps densely, because GB300's FP64 pipe costs a warp
+// instruction whatever the number of active lanes, so the fewest warps do a level's
+// FP64 work in the fewest instructions, and a wide chunk runs as more warps at once
+// rather than as a second pass. Each warp's entries form a slab, entry k of lane's
+// row at slab + 32 * k + lane (ELL order: a warp's reads of entry k are consecutive).
+// The per-row sections hold slots = rows rounded up to whole warps.
 // Byte offsets from the record's start, each section 16-byte aligned:
-//   [0]       header: rows cnt, entry slots ne, pushes np, passes npass | (some entry
-//             read from memory) << 16
-//   [16]      row info, npass * PS_CT int4 by row: {first entry slot, old | all entries << 16,
+//   [0]       header: rows cnt, entry slots ne, pushes np, 1 | (some entry read from
+//             memory) << 16
+//   [16]      row info, slots int4 by row: {first entry slot, old | all entries << 16,
 //             row id (-1: no row), first push}; a row's pushes run to the next row's
 //             first push (one closing int4 after the last slot)
 //   codes     ne ints: >= 0 the output vector's row, < 0 shared-memory slot -1 - code
 //             (own ring [0, S_own), then the receive ring)
 //   pushes    np ints: consumer << 24 | receive slot
 //   vals      ne values
-//   lv        npass * PS_CT values: 1 / L_ii (forward) or D_i (backward), by row
-//   rhs       npass * PS_CT values: the right-hand side (forward) or aux (backward)
+//   lv        slots values: 1 / L_ii (forward) or D_i (backward), by row
+//   rhs       slots values: the right-hand side (forward) or aux (backward)
 struct PsRec {
     int o_info, o_code, o_push, o_val, o_lv, o_rhs, size;
 };
-SSG_HD inline PsRec ps_rec(int npass, int ne, int np, int elem) {
+// row slots of a record: its rows rounded up to whole warps
+SSG_HD inline int ps_slots(int cnt) { return (cnt + 31) & ~31; }
+SSG_HD inline PsRec ps_rec(int cnt, int ne, int np, int elem) {
     PsRec r;
-    const int slots = npass * PS_CT;
+    const int slots = ps_slots(cnt);
     r.o_info = 16;
     r.o_code = r.o_info + 16 * (slots + 1);
     r.o_push = r.o_code + ps_al16(4 * ne);

@@ -52,9 +52,9 @@ int pp_consts(int *out) {
     return 7;
 }
 
-// record section offsets for (passes, entry slots, pushes, elem): info, code, push, val, lv, rhs, size
-void pp_rec(int npass, int ne, int np, int elem, int *out) {
-    const ssg::PsRec r = ssg::ps_rec(npass, ne, np, elem);
+// record section offsets for (rows, entry slots, pushes, elem): info, code, push, val, lv, rhs, size
+void pp_rec(int cnt, int ne, int np, int elem, int *out) {
+    const ssg::PsRec r = ssg::ps_rec(cnt, ne, np, elem);
     out[0] = r.o_info;
     out[1] = r.o_code;
     out[2] = r.o_push;

@@ -79,9 +79,9 @@ def plan(lib, tri, C, elem):
     return out
 
 
-def rec_layout(lib, npass, ne, np_, elem):
+def rec_layout(lib, cnt, ne, np_, elem):
     o = np.zeros(7, np.int32)
-    lib.pp_rec(ctypes.c_int(npass), ctypes.c_int(ne), ctypes.c_int(np_), ctypes.c_int(elem), _p(o))
+    lib.pp_rec(ctypes.c_int(cnt), ctypes.c_int(ne), ctypes.c_int(np_), ctypes.c_int(elem), _p(o))
     return dict(zip(["info", "code", "push", "val", "lv", "rhs", "size"], o.tolist()))
 
 
@@ -149,10 +149,10 @@ def check_and_emulate(lib, P, tri, vals_lo, r, ref, elem):
             prev_end = off + size
             w = off // 4
             cnt, ne, np_, npass = rec[w], rec[w + 1], rec[w + 2], rec[w + 3] & 0xFFFF
-            assert cnt == re - rs and npass == -(-cnt // k["CT"])
-            Lr = rec_layout(lib, npass, ne, np_, elem)
+            assert cnt == re - rs and npass == 1 and cnt <= k["CT"]
+            Lr = rec_layout(lib, cnt, ne, np_, elem)
             assert Lr["size"] == size
-            slots = npass * k["CT"]
+            slots = -(-cnt // 32) * 32  # rows rounded up to whole warps
             info = rec[w + Lr["info"] // 4: w + Lr["info"] // 4 + 4 * (slots + 1)].reshape(slots + 1, 4)
             assert tuple(info[slots]) == (ne, 0, -1, np_)
             code = rec[w + Lr["code"] // 4: w + Lr["code"] // 4 + ne]
