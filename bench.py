@@ -56,8 +56,8 @@ MAXIT = 20000
 # real values), profiles/k_sweep_cluster_80cube.md (lockstep cluster sweeps) and profiles/k_sweep_fwd_80cube.md
 # (sync-free forward sweep)
 NCU_TRAFFIC = {
-    ("cfg2", "fp64", "push", "forward sweep"): 473.8e6,
-    ("cfg2", "fp64", "push", "backward sweep"): 472.5e6,
+    ("cfg2", "fp64", "push", "forward sweep"): 434.4e6,
+    ("cfg2", "fp64", "push", "backward sweep"): 434.3e6,
     ("cfg2", "fp64", "cluster", "forward sweep"): 348.7e6,
     ("cfg2", "fp64", "cluster", "backward sweep"): 347.6e6,
     ("cfg2", "fp64", "sync-free", "forward sweep"): 360.6e6,
