@@ -100,6 +100,10 @@ def parse():
                     help="time the sweep schedules on the workload first (ssg_autotune) and keep the fastest")
     ap.add_argument("--batch-group", type=int, default=0, choices=[0, 4, 8, 16],
                     help="lanes a row in the sweeps of the handle's internal batch (mixed precision, --rhs); 0 auto")
+    ap.add_argument("--batch-sizes", default="8,32",
+                    help="cfg4: the range of N (voxels a side) of the 256 systems, N ~ U{lo..hi}")
+    ap.add_argument("--batch-persistent", action="store_true",
+                    help="cfg4: FP64 ICCG starts with one CTA per instance running all its iterations")
     ap.add_argument("--sweep-mode", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="triangular sweeps: 0 automatic, 1 sync-free, 2 one-cluster level-synchronous, "
                          "3 one-cluster neighbour-synchronised, 4 one-cluster push")
@@ -648,7 +652,8 @@ def run_batch(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    cases = voxel.batched_cases()
+    lo, hi = (int(v) for v in args.batch_sizes.split(","))
+    cases = voxel.batched_cases(lo=lo, hi=hi)
     mine = replicas.assign_systems([c.size()[1] for c, _ in cases], ws)[rank]
     systems = []
     for i in mine:
@@ -656,6 +661,7 @@ def run_batch(args):
         systems.append(case.assemble(coils_list=coils))
     bt = _capi.Batch(local)
     bt.set_precision(_capi.PREC_MIXED if args.precision == "mixed" else _capi.PREC_FP64)
+    bt.set_persistent(args.batch_persistent)
     for rp, ci, va, B in systems:
         bt.add(rp, ci, va, B)
     inst = sum(len(B) for _, _, _, B in systems)
@@ -746,7 +752,9 @@ def run_batch(args):
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
         "dtype": "f64" + ("+fp32-inner" if args.precision == "mixed" else ""),
         "data": "synthetic (seeded voxel generator)",
-        "config": {"workload": "256 curl-curl systems, N ~ U{8..32} voxels, 4 coil right-hand sides each",
+        "config": {"workload": "256 curl-curl systems, N ~ U{%d..%d} voxels, 4 coil right-hand sides each" % (lo, hi),
+                   "iterations_engine": "persistent (one CTA per instance)" if args.batch_persistent
+                   else "launches per phase (CUDA graphs)",
                    "instances": total_inst, "rows": int(sum(len(B) * (len(rp) - 1) for rp, _, _, B in systems)),
                    "method": "shifted ICCG", "alpha": ALPHA, "tolerance": TOL, "converged": conv_all,
                    "sweep_schedule": "autotuned: %s" % json.dumps(tuned) if tuned else "fixed (8 lanes a row)",

@@ -29,7 +29,7 @@ EXPORTED = [
     "ssg_launch_count", "ssg_set_tuning", "ssg_autotune", "ssg_ic_factor_noalloc", "ssg_batch_create", "ssg_batch_destroy",
     "ssg_batch_last_error", "ssg_batch_add", "ssg_batch_set_rhs", "ssg_batch_clear", "ssg_batch_start", "ssg_batch_poll", "ssg_batch_wait", "ssg_batch_step", "ssg_batch_finished",
     "ssg_batch_result", "ssg_batch_residual_log", "ssg_batch_timings", "ssg_batch_stream",
-    "ssg_batch_set_profiling", "ssg_batch_kernel_stats", "ssg_batch_set_graphs", "ssg_batch_autotune", "ssg_batch_set_precision",
+    "ssg_batch_set_profiling", "ssg_batch_kernel_stats", "ssg_batch_set_graphs", "ssg_batch_set_persistent", "ssg_batch_autotune", "ssg_batch_set_precision",
 ]
 NOALLOC_MAX_ROWS = 1 << 21
 TUNE_SWEEP_CTA_PER_SM = 0
@@ -111,6 +111,7 @@ def declare(lib):
         "ssg_batch_stream": ([H, ctypes.POINTER(ctypes.c_void_p)], I),
         "ssg_batch_set_profiling": ([H, I], I),
         "ssg_batch_set_graphs": ([H, I], I),
+        "ssg_batch_set_persistent": ([H, I], I),
         "ssg_batch_autotune": ([H, P, P, P, P], I),
         "ssg_batch_set_precision": ([H, I, D], I),
         "ssg_batch_kernel_stats": ([H, P, P, P, I], I),
@@ -504,6 +505,10 @@ class Batch:
 
     def set_graphs(self, on):
         self._check(self.lib.ssg_batch_set_graphs(self.b, 1 if on else 0), "ssg_batch_set_graphs")
+
+    def set_persistent(self, on):
+        """FP64 ICCG starts with one CTA per instance running all of its iterations (small systems)."""
+        self._check(self.lib.ssg_batch_set_persistent(self.b, 1 if on else 0), "ssg_batch_set_persistent")
 
     def autotune(self):
         """Times the sweep schedules on the batch and keeps the fastest: {mode, group, cta_per_sm, ms}."""

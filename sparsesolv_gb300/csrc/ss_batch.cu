@@ -263,6 +263,165 @@ __global__ void __launch_bounds__(BT) k_biccg_p(BDev B, T *p, const T *z) {
     }
 }
 
+// ---------------------------------------------------------------- persistent ICCG (small instances)
+// One CTA per instance runs all of its ICCG iterations: SpMV with p.Ap and alpha, the
+// x / r update and the convergence test, the forward and backward IC sweeps level by
+// level (a CTA barrier between levels), beta and the p update. Every piece does the
+// arithmetic of the launch-per-phase kernels above in the same order (tile partials
+// as 256-thread block sums added in tile order; the SpMV's 4 / 2 lanes a row; the
+// sync-free sweep's G lanes a row, negated sums, lane 0 starting from the forward
+// right-hand side, the same butterfly), so an instance gives the same bits either way;
+// what goes away are the launches, the grid-wide reductions and the sweep's polling.
+// An instance's rows stay in L2 between phases. No CTA waits on another.
+constexpr int PERSIST_MAX_TILES = 8;  // instances of at most 8 tiles (16,384 rows)
+
+struct BPer {
+    const int *rp, *ci;
+    const void *aval;
+    const int *fperm, *fprp, *fpci;  // forward triangle in level order
+    const void *fval, *dinv;         // its values; 1 / L_ii by row
+    const int *bperm, *bprp, *bpci;  // backward triangle in level order
+    const void *bval, *D;            // its values; D by row
+    const int *flev, *blev;          // [S + 1]: first level range of each instance
+    const int2 *frng, *brng;         // level ranges (positions in the level order) of each instance
+    void *x, *r, *p, *z, *y, *v;
+    int iters;                       // iterations to run at most
+};
+
+// one level range of a sweep: rows at positions [a, b), G lanes a row (k_sweep's arithmetic)
+template <typename T, int G, int MODE>
+__device__ __forceinline__ void persist_level(int a, int b, const int *perm, const int *prp, const int *pci,
+                                              const T *val, const T *rhs, const T *aux, const T *Dv, const T *dinv,
+                                              T *out) {
+    const int g = threadIdx.x / G, gl = threadIdx.x % G;
+    const unsigned gm = group_mask(G);
+    for (int t = a + g; t < b; t += BT / G) {
+        const int r = perm[t];
+        const int ra = prp[t], re = prp[t + 1];
+        constexpr bool fwd = MODE == SW_FWD_DIV;
+        const int ob = fwd ? ra : ra + 1;
+        const int oe = fwd ? (re > ra ? re - 1 : ra) : re;
+        T acc = (fwd && gl == 0) ? rhs[r] : Sc<T>::zero();
+        for (int k = ob + gl; k < oe; k += G) acc = madd(acc, -val[k], out[pci[k]]);
+#pragma unroll
+        for (int m = G / 2; m >= 1; m >>= 1) acc = acc + gshfl_xor(acc, m, gm);
+        if (gl == 0) out[r] = fwd ? acc * dinv[r] : madd(aux[r], Dv[r], acc);
+    }
+}
+
+template <typename T, int G>
+__global__ void __launch_bounds__(BT) k_bpersist_iccg(BDev B, BPer P) {
+    const int s = blockIdx.x;
+    KState *st = B.st + s;
+    __shared__ double tp[PERSIST_MAX_TILES][2];
+    __shared__ int s_go;
+    if (threadIdx.x == 0) s_go = st->active;
+    __syncthreads();
+    if (!s_go) return;
+    using W = typename Wide<T>::type;
+    const int t0 = B.sys_tile[s], t1 = B.sys_tile[s + 1];
+    const T *aval = (const T *)P.aval;
+    T *x = (T *)P.x, *r = (T *)P.r, *p = (T *)P.p, *z = (T *)P.z, *y = (T *)P.y, *v = (T *)P.v;
+    double *log = inst_log(B, s);
+    constexpr int GS = Sc<T>::is_complex ? 2 : 4, RPB = BT / GS;
+    const int gs = threadIdx.x / GS, gls = threadIdx.x % GS;
+    for (int it = 0; it < P.iters; ++it) {
+        // SpMV v = A p with p . v per tile (k_bspmv), alpha = rur0 / (p . Ap)
+        for (int t = t0; t < t1; ++t) {
+            const int2 tr = B.tile[t];
+            double acc2[2] = {0.0, 0.0};
+            for (int row0 = tr.x; row0 < tr.y; row0 += RPB) {
+                const int row = row0 + gs;
+                T acc = Sc<T>::zero();
+                if (row < tr.y) {
+                    const int a = P.rp[row], e = P.rp[row + 1];
+                    for (int k = a + gls; k < e; k += GS) acc = madd(acc, aval[k], p[P.ci[k]]);
+                }
+#pragma unroll
+                for (int m = GS / 2; m >= 1; m >>= 1) acc = acc + Sc<T>::shfl_xor(acc, m);
+                if (row < tr.y && gls == 0) {
+                    v[row] = acc;
+                    acc_parts<T>(acc2, p[row] * acc);
+                }
+            }
+            block_partial<2>(acc2, tp[t - t0]);
+        }
+        if (threadIdx.x == 0) {
+            double tot[2] = {0.0, 0.0};
+            for (int t = t0; t < t1; ++t) {
+                tot[0] += tp[t - t0][0];
+                tot[1] += tp[t - t0][1];
+            }
+            st->dots[0] = tot[0];
+            st->dots[1] = tot[1];
+            putS<W>(st->alpha, getS<W>(st->rur0) / getS<W>(tot));
+        }
+        __syncthreads();
+        // x += alpha p, r -= alpha Ap, |r| (k_biccg_update), the convergence test
+        {
+            const T alpha = getS<T>(st->alpha);
+            for (int t = t0; t < t1; ++t) {
+                const int2 tr = B.tile[t];
+                double acc[1] = {0.0};
+                for (int i = tr.x + threadIdx.x; i < tr.y; i += BT) {
+                    x[i] = x[i] + alpha * p[i];
+                    const T ri = r[i] - alpha * v[i];
+                    r[i] = ri;
+                    acc[0] += Sc<T>::abs2(ri);
+                }
+                block_partial<1>(acc, tp[t - t0]);
+            }
+        }
+        if (threadIdx.x == 0) {
+            double tot = 0.0;
+            for (int t = t0; t < t1; ++t) tot += tp[t - t0][0];
+            decide(st, sqrt(tot), log);
+            s_go = st->active;
+        }
+        __syncthreads();
+        if (!s_go) break;
+        // z = (L D L^T)^{-1} r: forward then backward, level by level
+        for (int q = P.flev[s]; q < P.flev[s + 1]; ++q) {
+            const int2 rg = P.frng[q];
+            persist_level<T, G, SW_FWD_DIV>(rg.x, rg.y, P.fperm, P.fprp, P.fpci, (const T *)P.fval, r, nullptr,
+                                            nullptr, (const T *)P.dinv, y);
+            __syncthreads();
+        }
+        for (int q = P.blev[s]; q < P.blev[s + 1]; ++q) {
+            const int2 rg = P.brng[q];
+            persist_level<T, G, SW_BWD_IC>(rg.x, rg.y, P.bperm, P.bprp, P.bpci, (const T *)P.bval, nullptr, y,
+                                           (const T *)P.D, nullptr, z);
+            __syncthreads();
+        }
+        // beta = (r . z) / rur0 (k_biccg_beta), p = p beta + z (k_biccg_p)
+        for (int t = t0; t < t1; ++t) {
+            const int2 tr = B.tile[t];
+            double acc[2] = {0.0, 0.0};
+            for (int i = tr.x + threadIdx.x; i < tr.y; i += BT) acc_parts<T>(acc, r[i] * z[i]);
+            block_partial<2>(acc, tp[t - t0]);
+        }
+        if (threadIdx.x == 0) {
+            double tot[2] = {0.0, 0.0};
+            for (int t = t0; t < t1; ++t) {
+                tot[0] += tp[t - t0][0];
+                tot[1] += tp[t - t0][1];
+            }
+            const W rur1 = getS<W>(tot);
+            putS<W>(st->beta, rur1 / getS<W>(st->rur0));
+            putS<W>(st->rur0, rur1);
+        }
+        __syncthreads();
+        {
+            const T beta = getS<T>(st->beta);
+            for (int t = t0; t < t1; ++t) {
+                const int2 tr = B.tile[t];
+                for (int i = tr.x + threadIdx.x; i < tr.y; i += BT) p[i] = p[i] * beta + z[i];
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // ---------------------------------------------------------------- IC-MRTR steps
 template <typename T>
 __global__ void __launch_bounds__(BT) k_bmrtr_dots(BDev B, const T *a, const T *b, const T *c, const T *y) {
@@ -523,6 +682,7 @@ Batch::Batch(int dev) : h(dev) {
     // instance's arithmetic must not depend on the batch it is in
     h.swcfg.group = 8;
     h.cl_group = 8;
+    h.push_auto = false;
     SSG_CUDA(cudaEventCreateWithFlags(&ev_chunk, cudaEventDisableTiming));
     for (auto &e : ev) SSG_CUDA(cudaEventCreate(&e));
     SSG_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
@@ -658,6 +818,8 @@ void Batch::assemble() {
     }
     rp[(size_t)N] = (int)e;
     NT = (int)tiles.size();
+    h_sys_tile = sys_tile;
+    pr_key = ~0ull;
     h.set_matrix((int)N, (int)NNZ, rp.data(), ci.data(), val.data(), vtype, cudaMemcpyHostToDevice);
     // a system's instances for its second and later right-hand sides have the same matrix
     // as its first: their factor rows are copies of the first instance's
@@ -840,8 +1002,104 @@ void Batch::start(int method_, double alpha, double conv, int max_ite_) {
     queue_chunk<T>();
 }
 
+bool Batch::persist_ok() const {
+    if (!persist || method != SSG_METHOD_ICCG || precision != SSG_PREC_FP64 || h.prof.on || !h.use_inv_diag) return false;
+    const int G = h.swcfg.group;
+    if (G != 4 && G != 8 && G != 16 && G != 32) return false;
+    if ((int)h_sys_tile.size() != S + 1) return false;
+    for (int q = 0; q < S; ++q)
+        if (h_sys_tile[q + 1] - h_sys_tile[q] > PERSIST_MAX_TILES) return false;
+    return true;
+}
+
+// each instance's rows of each level of the forward and backward triangles: within a
+// level the rows are in row order and an instance's rows are contiguous, so each
+// (level, instance) is one range of positions; an instance's ranges in level order
+void Batch::persist_ranges() {
+    if (pr_key == h.pattern_id) return;
+    const int n = h.n;
+    std::vector<int> rinst((size_t)n);
+    for (int q = 0; q < S; ++q)
+        for (int i = inst_row[q]; i < inst_row[q + 1]; ++i) rinst[i] = q;
+    auto build = [&](const Tri &T, DBuf &dl, DBuf &dr) {
+        std::vector<int> perm((size_t)n);
+        if (n) SSG_CUDA(cudaMemcpy(perm.data(), T.perm.p, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
+        std::vector<int> first((size_t)S + 1, 0);
+        std::vector<int3> runs;  // (instance, start, end)
+        for (int L = 0; L < T.nlev; ++L)
+            for (int t = T.lptr[L]; t < T.lptr[L + 1];) {
+                const int q = rinst[perm[t]];
+                int e = t + 1;
+                while (e < T.lptr[L + 1] && rinst[perm[e]] == q) ++e;
+                runs.push_back(make_int3(q, t, e));
+                ++first[q + 1];
+                t = e;
+            }
+        for (int q = 0; q < S; ++q) first[q + 1] += first[q];
+        std::vector<int2> rng(runs.size() + 1, make_int2(0, 0));
+        std::vector<int> fill(first.begin(), first.end() - 1);
+        for (const int3 &r : runs) rng[fill[r.x]++] = make_int2(r.y, r.z);
+        dl.ensure(sizeof(int) * (first.size()));
+        dr.ensure(sizeof(int2) * rng.size());
+        SSG_CUDA(cudaMemcpy(dl.p, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice));
+        SSG_CUDA(cudaMemcpy(dr.p, rng.data(), sizeof(int2) * rng.size(), cudaMemcpyHostToDevice));
+    };
+    build(h.Lf, d_pl_f, d_pr_f);
+    build(h.Ltb, d_pl_b, d_pr_b);
+    pr_key = h.pattern_id;
+}
+
+template <typename T>
+void Batch::queue_persistent() {
+    cudaStream_t s = h.stream;
+    persist_ranges();
+    BDev B = dev_view();
+    BPer P;
+    P.rp = h.A_rp.as<int>();
+    P.ci = h.A_ci.as<int>();
+    P.aval = h.A_val.p;
+    P.fperm = h.Lf.perm.as<int>();
+    P.fprp = h.Lf.prp.as<int>();
+    P.fpci = h.Lf.pci.as<int>();
+    P.fval = h.Lval.p;
+    P.dinv = h.invL.p;
+    P.bperm = h.Ltb.perm.as<int>();
+    P.bprp = h.Ltb.prp.as<int>();
+    P.bpci = h.Ltb.pci.as<int>();
+    P.bval = h.Ltval.p;
+    P.D = h.Dvec.p;
+    P.flev = d_pl_f.as<int>();
+    P.frng = d_pr_f.as<int2>();
+    P.blev = d_pl_b.as<int>();
+    P.brng = d_pr_b.as<int2>();
+    P.x = h.vec[8].p;
+    P.r = h.vec[1].p;
+    P.p = h.vec[2].p;
+    P.z = h.vec[3].p;
+    P.y = h.vec[10].p;
+    P.v = h.vec[6].p;
+    P.iters = max_ite - queued;
+    if (S > 0 && P.iters > 0) {
+        switch (h.swcfg.group) {
+            case 4: k_bpersist_iccg<T, 4><<<S, BT, 0, s>>>(B, P); break;
+            case 8: k_bpersist_iccg<T, 8><<<S, BT, 0, s>>>(B, P); break;
+            case 16: k_bpersist_iccg<T, 16><<<S, BT, 0, s>>>(B, P); break;
+            default: k_bpersist_iccg<T, 32><<<S, BT, 0, s>>>(B, P); break;
+        }
+        SSG_LAUNCHED();
+    }
+    queued = max_ite;
+    SSG_CUDA(cudaMemcpyAsync(h_ctl, ctl(), sizeof(KState), cudaMemcpyDeviceToHost, s));
+    SSG_CUDA(cudaMemcpyAsync(h_st, d_st.p, sizeof(KState) * (size_t)S, cudaMemcpyDeviceToHost, s));
+    SSG_CUDA(cudaEventRecord(ev_chunk, s));
+}
+
 template <typename T>
 void Batch::queue_chunk() {
+    if (persist_ok()) {
+        queue_persistent<T>();
+        return;
+    }
     cudaStream_t s = h.stream;
     const int n = h.n;
     BDev B = dev_view();
@@ -1258,6 +1516,9 @@ int solve_batched(Handle &h, Batch *&mb, uint64_t &mver, uint64_t &mpat, int pre
     mb->h.swcfg.group = mb->h.cl_group = g;
     mb->h.swcfg.cta_per_sm = h.swcfg.cta_per_sm;
     mb->h.sweep_mode = h.sweep_mode;
+    // a handle's own batch (mixed precision, several right-hand sides) serves one matrix:
+    // its automatic mode may take the push sweep, as the handle's single solves do
+    mb->h.push_auto = true;
     if (mb->h.spin_limit_us != h.spin_limit_us) mb->h.set_spin_limit(h.spin_limit_us);
     AllocStream as(mb->h.stream);  // the batch's buffers are ordered on its own stream
     const int w = h.vtype == SSG_COMPLEX ? 2 : 1;

@@ -121,6 +121,16 @@ struct Batch {
     // every whole group of that many iterations (not while profiling)
     static constexpr int GRAPH_ITERS = 8;
     bool use_graphs = true;
+    // persistent ICCG (one CTA per instance runs all its iterations, ss_batch.cu): used
+    // for FP64 ICCG starts when on and every instance has at most 8 tiles
+    bool persist = false;
+    std::vector<int> h_sys_tile;        // host copy of the first tile of each instance
+    DBuf d_pl_f, d_pr_f, d_pl_b, d_pr_b;  // per-instance level ranges of the forward / backward triangles
+    uint64_t pr_key = ~0ull;            // pattern the ranges were made for
+    bool persist_ok() const;
+    void persist_ranges();
+    template <typename T>
+    void queue_persistent();
     cudaGraphExec_t graph_exec = nullptr;
     long long graph_kernels = 0;
     void drop_graph();

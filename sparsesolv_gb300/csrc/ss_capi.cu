@@ -670,6 +670,14 @@ int ssg_batch_set_graphs(ssg_batch bd, int enable) {
     });
 }
 
+int ssg_batch_set_persistent(ssg_batch bd, int enable) {
+    return bguarded(bd, [&](ssg::Batch &b) {
+        if (b.running) return SSG_ERR_STATE;
+        b.persist = enable != 0;
+        return SSG_OK;
+    });
+}
+
 int ssg_batch_autotune(ssg_batch bd, int *mode, int *group, int *cta_per_sm, double *ms) {
     return bguarded(bd, [&](ssg::Batch &b) {
         if (b.running) return SSG_ERR_STATE;

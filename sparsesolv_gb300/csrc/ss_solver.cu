@@ -377,7 +377,8 @@ bool Handle::cluster_ok(Tri &t, size_t elem, bool ic) {
 bool Handle::push_ok(Tri &t, size_t elem) {
     if (!use_inv_diag || t.n == 0) return false;
     if (sweep_mode != 4 && sweep_mode != 0) return false;
-    if (sweep_mode == 0 && (vtype == SSG_COMPLEX || (double)t.n > kAutoClusterRowsPerLevel * (double)t.nlev))
+    if (sweep_mode == 0 &&
+        (!push_auto || vtype == SSG_COMPLEX || (double)t.n > kAutoClusterRowsPerLevel * (double)t.nlev))
         return false;
     return push_plan(t, elem, stream);
 }

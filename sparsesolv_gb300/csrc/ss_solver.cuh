@@ -124,6 +124,10 @@ struct Handle {
     // ic: an IC sweep (the only kind the neighbour-synchronised plan serves)
     bool cluster_ok(Tri &t, size_t elem, bool ic);
     bool push_ok(Tri &t, size_t elem);
+    // the automatic mode may take the push sweep (off in the standalone batches: their
+    // instances' bits must not depend on which schedule a batch's size leads to, and the
+    // lane-summed schedules give the same bits at the same lanes a row)
+    bool push_auto = true;
 
     Prof prof;
     int prof_begin(int cls);

@@ -250,3 +250,48 @@ def test_autotuned_batch_meets_the_bar_and_stays_deterministic(gpu, oracle, syst
                 check_against_oracle(oracle, "iccg", rp, ci, va, b, X[0], bt.residual_log(k), int(it[0]), False)
     finally:
         bt.close()
+
+
+def _persist_run(persist, systems, Bs):
+    bt = _capi.Batch(0)
+    try:
+        bt.set_persistent(persist)
+        for (rp, ci, va, _), B in zip(systems, Bs):
+            bt.add(rp, ci, va, B)
+        bt.start(_capi.METHOD_ICCG, ALPHA, conv=1e-8, max_ite=5000)
+        bt.wait()
+        res = [bt.result(k) for k in range(len(systems))]
+        logs = [[bt.residual_log(k, j) for j in range(len(Bs[k]))] for k in range(len(systems))]
+        return res, logs
+    finally:
+        bt.close()
+
+
+def test_persistent_batch_same_bits_as_launches(gpu, oracle):
+    """ssg_batch_set_persistent: one CTA per instance runs all of its iterations. Every
+    instance gives the same bits as the launch-per-phase iterations (x, iteration
+    count, residual log) and meets the oracle. A batch holding a system of more than
+    16,384 rows runs the launches (same bits again)."""
+    rng = np.random.default_rng(17)
+    systems = [voxel.curl_curl_case(N, seed=30 + N, iron_size=max(2, N // 3)).assemble() for N in (6, 8, 10, 12)]
+    import scipy.sparse as sp
+    Bs = []
+    for rp, ci, va, b in systems:
+        A = sp.csr_matrix((va, ci, rp))
+        Bs.append(np.stack([b, A @ rng.standard_normal(len(b))]))  # a consistent second right-hand side
+    ref, ref_logs = _persist_run(False, systems, Bs)
+    got, got_logs = _persist_run(True, systems, Bs)
+    for k in range(len(systems)):
+        assert np.array_equal(got[k][0], ref[k][0]) and np.array_equal(got[k][1], ref[k][1]), k
+        for a, m in zip(got_logs[k], ref_logs[k]):
+            assert np.array_equal(a, m)
+        rp, ci, va, b = systems[k]
+        check_against_oracle(oracle, "iccg", rp, ci, va, b, got[k][0][0], got_logs[k][0], int(got[k][1][0]), False)
+    # with a 20^3 system (21,660 rows) in the batch: the launches run
+    big = voxel.config1().assemble()
+    systems2 = systems[:2] + [big]
+    Bs2 = Bs[:2] + [np.atleast_2d(big[3])]
+    ref2, _ = _persist_run(False, systems2, Bs2)
+    got2, _ = _persist_run(True, systems2, Bs2)
+    for k in range(3):
+        assert np.array_equal(got2[k][0], ref2[k][0]) and np.array_equal(got2[k][1], ref2[k][1])
