@@ -102,8 +102,9 @@ def parse():
                     help="lanes a row in the sweeps of the handle's internal batch (mixed precision, --rhs); 0 auto")
     ap.add_argument("--batch-sizes", default="8,32",
                     help="cfg4: the range of N (voxels a side) of the 256 systems, N ~ U{lo..hi}")
-    ap.add_argument("--batch-persistent", action="store_true",
-                    help="cfg4: FP64 ICCG starts with one CTA per instance running all its iterations")
+    ap.add_argument("--batch-persistent", action=argparse.BooleanOptionalAction, default=True,
+                    help="cfg4: FP64 ICCG starts with one CTA per instance running all its iterations where every "
+                         "instance is small enough (the default); --no-batch-persistent: launches per phase")
     ap.add_argument("--sweep-mode", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="triangular sweeps: 0 automatic, 1 sync-free, 2 one-cluster level-synchronous, "
                          "3 one-cluster neighbour-synchronised, 4 one-cluster push")
@@ -753,7 +754,8 @@ def run_batch(args):
         "dtype": "f64" + ("+fp32-inner" if args.precision == "mixed" else ""),
         "data": "synthetic (seeded voxel generator)",
         "config": {"workload": "256 curl-curl systems, N ~ U{%d..%d} voxels, 4 coil right-hand sides each" % (lo, hi),
-                   "iterations_engine": "persistent (one CTA per instance)" if args.batch_persistent
+                   "iterations_engine": "persistent (one CTA per instance) where every instance has at most "
+                                        "16,384 rows, else launches per phase" if args.batch_persistent
                    else "launches per phase (CUDA graphs)",
                    "instances": total_inst, "rows": int(sum(len(B) * (len(rp) - 1) for rp, _, _, B in systems)),
                    "method": "shifted ICCG", "alpha": ALPHA, "tolerance": TOL, "converged": conv_all,

@@ -331,14 +331,15 @@ int ssg_batch_set_profiling(ssg_batch b, int enable);
 /* 1 (default): each start captures 8 iterations in a CUDA graph once and replays it
  * for the later chunks (direct launches while profiling); 0: direct launches only */
 int ssg_batch_set_graphs(ssg_batch b, int enable);
-/* 1: FP64 ICCG starts run persistent: one CTA per (system, right-hand side) runs all
+/* 1 (default): FP64 ICCG starts run persistent: one CTA per (system, right-hand side) runs all
  * of its iterations (SpMV, update and convergence test, both IC sweeps level by level
  * with a CTA barrier between levels, beta, p) with no further launch and no wait on
  * another CTA; the same bits as the launch-per-phase iterations with the sync-free
  * sweep. Used when every system has at most 16,384 rows, the sweeps have a fixed lane
  * count (the batch default, 8) and the reciprocal diagonal is on; otherwise, and for
- * IC-MRTR and mixed precision, the launches run. 0 (default): launches. No reference
- * counterpart (the reference solves one system per call). */
+ * IC-MRTR and mixed precision, the launches run. 0: launches always. On 1,024
+ * instances of 1-4k rows: 24,300 solves/s against 19,600 with the launches. No
+ * reference counterpart (the reference solves one system per call). */
 int ssg_batch_set_persistent(ssg_batch b, int enable);
 /* Times the sweep schedules on the batch's block-diagonal matrix (as ssg_autotune:
  * sync-free with 4/8/16 lanes a row and 2..16 CTAs per SM, one-cluster lockstep and

@@ -280,7 +280,7 @@ def test_persistent_batch_same_bits_as_launches(gpu, oracle):
         A = sp.csr_matrix((va, ci, rp))
         Bs.append(np.stack([b, A @ rng.standard_normal(len(b))]))  # a consistent second right-hand side
     ref, ref_logs = _persist_run(False, systems, Bs)
-    got, got_logs = _persist_run(True, systems, Bs)
+    got, got_logs = _persist_run(True, systems, Bs)  # the default
     for k in range(len(systems)):
         assert np.array_equal(got[k][0], ref[k][0]) and np.array_equal(got[k][1], ref[k][1]), k
         for a, m in zip(got_logs[k], ref_logs[k]):
