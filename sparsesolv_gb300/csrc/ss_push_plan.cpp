@@ -51,9 +51,8 @@ PushLayout push_layout(int S_own, int S_recv, int cap_rec, int elem, int NB) {
     return L;
 }
 
-static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *prp, const int *pci,
-                                  const int *perm, const int *level, const int *ipos, int C, int elem, int S_own,
-                                  int NB) {
+PushPlanHost push_plan_host(int n, int nlev, const int *lptr, const int *prp, const int *pci, const int *perm,
+                            const int *level, const int *ipos, int C, int elem) {
     PushPlanHost P;
     auto fail = [&](const char *why) {
         P.ok = false;
@@ -86,7 +85,6 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
             }
         }
     if (cap_r > PS_CT * PS_MAXQ) return fail("a level chunk has more rows than the CTA holds");
-    if (2 * cap_r > S_own) return fail("own ring smaller than two levels");
     // entries (off-diagonal) sorted per row by (dependency level, column)
     std::vector<int> sprp(n + 1, 0), nsp(n, 0), &vmap = P.vmap;
     vmap.reserve(prp[n]);
@@ -129,14 +127,9 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
     for (int t = 0; t < n; ++t) {
         const int c = owner[t], lt = level[perm[t]];
         for (int k = sprp[t]; k < sprp[t + 1]; ++k) {
-            const int j = dep[k], lj = level[j], pj = ipos[j], cj = owner[pj], oj = ordc[pj];
-            const bool newest = (lj == lt - 1);
+            const int j = dep[k], lj = level[j], pj = ipos[j], cj = owner[pj];
             if (cj == c) {
-                const int reuse = oj + S_own;
-                const bool in_ring = reuse >= (int)levof[c].size() || levof[c][reuse] >= lt + 1;
-                if (in_ring) code[k] = -1 - (oj % S_own);
-                else if (!newest) code[k] = j;
-                else return fail("a newest own dependency left the own ring");
+                continue;  // own ring or memory: depends on the ring size (per layout below)
             } else if (lt - lj <= LEAD + 1) {
                 reqs.push_back({((long long)c << 58) | ((long long)lj << 32) | (unsigned)pj, k, lt});
             } else {
@@ -180,118 +173,138 @@ static PushPlanHost push_plan_try(int n, int nlev, const int *lptr, const int *p
             cap_rec = std::max(cap_rec, r.size);
             cnt_max = std::max(cnt_max, re - rs);
         }
-    // the receive ring takes the shared memory left next to the staged records
-    PushLayout lay = push_layout(S_own, 0, cap_rec, elem, NB);
-    int S_recv = std::min(1 << 16, (PS_SMEM_MAX - lay.total) / elem - 16);
-    S_recv = (S_recv / 64) * 64;
-    if (S_recv < 512) return fail("no shared memory left for the receive ring");
-    lay = push_layout(S_own, S_recv, cap_rec, elem, NB);
-    if (lay.total > PS_SMEM_MAX) return fail("layout exceeds shared memory");
-    // receive slots per consumer, and the reuse proof
-    std::vector<int> slot(pushes.size());
-    {
-        std::vector<int> run(C, 0);
-        std::vector<std::vector<int>> hist(C);
-        for (size_t q = 0; q < pushes.size(); ++q) {
-            const int c = pushes[q].c;
-            const int k = run[c]++;
-            slot[q] = k % S_recv;
-            hist[c].push_back((int)q);
-            if (k >= S_recv) {
-                const Push &old = pushes[hist[c][k - S_recv]];
-                if (old.last_use + 1 > pushes[q].lp - LEAD) return fail("a receive slot is reused too early");
+    // the layouts, largest rings and most staged records first: the ring sizes decide
+    // which own entries stay in shared memory, the space left decides the receive ring
+    const std::vector<int> code0 = code;  // the entries read from memory (the others are set per layout)
+    auto attempt = [&](int S_own, int NB) -> const char * {
+        if (2 * cap_r > S_own) return "own ring smaller than two levels";
+        PushLayout lay = push_layout(S_own, 0, cap_rec, elem, NB);
+        // the receive ring takes the shared memory left next to the staged records
+        int S_recv = std::min(1 << 16, (PS_SMEM_MAX - lay.total) / elem - 16);
+        S_recv = (S_recv / 64) * 64;
+        if (S_recv < 512) return ("no shared memory left for the receive ring");
+        lay = push_layout(S_own, S_recv, cap_rec, elem, NB);
+        if (lay.total > PS_SMEM_MAX) return ("layout exceeds shared memory");
+        // own entries: the own ring while their slot is not reused before the end of the
+        // reading row's level, else the output vector (never a newest entry)
+        code = code0;
+        for (int t = 0; t < n; ++t) {
+            const int c = owner[t], lt = level[perm[t]];
+            for (int k = sprp[t]; k < sprp[t + 1]; ++k) {
+                const int j = dep[k], pj = ipos[j];
+                if (owner[pj] != c) continue;
+                const int oj = ordc[pj], reuse = oj + S_own;
+                const bool in_ring = reuse >= (int)levof[c].size() || levof[c][reuse] >= lt + 1;
+                if (in_ring) code[k] = -1 - (oj % S_own);
+                else if (level[j] != lt - 1) code[k] = j;
+                else return "a newest own dependency left the own ring";
             }
         }
-    }
-    for (size_t q = 0; q < reqs.size(); ++q) code[reqs[q].entry] = -1 - (S_own + slot[pushof[q]]);
-    std::vector<int> plist(pushes.size());
-    {
-        std::vector<int> fillp(pptr.begin(), pptr.end() - 1);
-        for (size_t q = 0; q < pushes.size(); ++q) plist[fillp[pushes[q].pj]++] = (pushes[q].c << 24) | slot[q];
-    }
-    std::vector<long long> bin((size_t)nlev * C, 0);
-    for (auto &p : pushes) bin[(size_t)p.lp * C + p.c] += elem;
-    // the records, in (level, CTA) order
-    std::vector<int> &tab = P.tab, &rec = P.rec, &dval = P.dval, &dlv = P.dlv, &drhs = P.drhs;
-    tab.assign((size_t)nlev * C * 4, 0);
-    dval.assign(nent, 0);
-    dlv.assign(n, 0);
-    drhs.assign(n, 0);
-    long long off = 0;
-    for (int l = 0; l < nlev; ++l)
-        for (int c = 0; c < C; ++c) {
-            int rs, re;
-            chunk_of(l, c, rs, re);
-            const int cnt = re - rs, npass = 1, np = pptr[re] - pptr[rs];
-            const int ne = slab_widths(rs, re);
-            const PsRec r = ps_rec(cnt, ne, np, elem);
-            if (off + r.size >= (1ll << 31)) return fail("records exceed 2 GB");
-            if (bin[(size_t)l * C + c] >= (1 << 20)) return fail("a level pushes more bytes than a barrier counts");
-            int *tr = &tab[((size_t)l * C + c) * 4];
-            tr[0] = (int)(off / 16);
-            tr[1] = r.size / 16;
-            tr[2] = (int)bin[(size_t)l * C + c];
-            const size_t w0 = (size_t)(off / 4);
-            rec.resize(w0 + r.size / 4, 0);
-            rec[w0 + 0] = cnt;
-            rec[w0 + 1] = ne;
-            rec[w0 + 2] = np;
-            bool hasg = false;  // an older entry read from the output vector (the kernel's slow path)
-            for (int t = rs; t < re; ++t)
-                for (int k = sprp[t]; k < sprp[t + 1]; ++k) hasg = hasg || code[k] >= 0;
-            rec[w0 + 3] = npass | ((hasg ? 1 : 0) << 16);
-            const int slots = ps_slots(cnt);
-            std::vector<int> slab(slots / 32, 0);  // first entry slot of each warp's slab
-            for (int i = 0, acc = 0; i < slots / 32; ++i) {
-                slab[i] = acc;
-                acc += 32 * K[i];
-            }
-            int pnext = 0;
-            for (int q = 0; q <= slots; ++q) {
-                int *ri = &rec[w0 + (r.o_info + 16 * q) / 4];
-                ri[3] = pnext;
-                if (q == slots || q >= cnt) {
-                    ri[0] = q == slots ? ne : 0;
-                    ri[1] = 0;
-                    ri[2] = -1;
-                    continue;
+        // receive slots per consumer, and the reuse proof
+        std::vector<int> slot(pushes.size());
+        {
+            std::vector<int> run(C, 0);
+            std::vector<std::vector<int>> hist(C);
+            for (size_t q = 0; q < pushes.size(); ++q) {
+                const int c = pushes[q].c;
+                const int k = run[c]++;
+                slot[q] = k % S_recv;
+                hist[c].push_back((int)q);
+                if (k >= S_recv) {
+                    const Push &old = pushes[hist[c][k - S_recv]];
+                    if (old.last_use + 1 > pushes[q].lp - LEAD) return ("a receive slot is reused too early");
                 }
-                const int w = q / 32, lane = q % 32;
-                const int t = rs + q, e0 = sprp[t], len = sprp[t + 1] - e0;
-                const int first = slab[w] + lane;
-                ri[0] = first;
-                ri[1] = nsp[t] | (len << 16);
-                ri[2] = perm[t];
-                for (int k = 0; k < len; ++k) {
-                    rec[w0 + r.o_code / 4 + first + 32 * k] = code[e0 + k];
-                    dval[e0 + k] = (int)((off + r.o_val) / elem) + first + 32 * k;
-                }
-                for (int k = pptr[t]; k < pptr[t + 1]; ++k) rec[w0 + r.o_push / 4 + pnext++] = plist[k];
-                dlv[t] = (int)((off + r.o_lv) / elem) + q;
-                drhs[t] = (int)((off + r.o_rhs) / elem) + q;
             }
-            off += r.size;
         }
-    rec.resize(rec.size() + 16, 0);  // a copy never reads past the buffer
-    P.C = C;
-    P.nent = nent;
-    P.npush = (int)pushes.size();
-    P.cnt_max = cnt_max;
-    P.lay = lay;
-    P.ok = true;
-    return P;
-}
-
-PushPlanHost push_plan_host(int n, int nlev, const int *lptr, const int *prp, const int *pci, const int *perm,
-                            const int *level, const int *ipos, int C, int elem) {
-    PushPlanHost best;
+        for (size_t q = 0; q < reqs.size(); ++q) code[reqs[q].entry] = -1 - (S_own + slot[pushof[q]]);
+        std::vector<int> plist(pushes.size());
+        {
+            std::vector<int> fillp(pptr.begin(), pptr.end() - 1);
+            for (size_t q = 0; q < pushes.size(); ++q) plist[fillp[pushes[q].pj]++] = (pushes[q].c << 24) | slot[q];
+        }
+        std::vector<long long> bin((size_t)nlev * C, 0);
+        for (auto &p : pushes) bin[(size_t)p.lp * C + p.c] += elem;
+        // the records, in (level, CTA) order
+        std::vector<int> &tab = P.tab, &rec = P.rec, &dval = P.dval, &dlv = P.dlv, &drhs = P.drhs;
+        tab.assign((size_t)nlev * C * 4, 0);
+        rec.clear();
+        dval.assign(nent, 0);
+        dlv.assign(n, 0);
+        drhs.assign(n, 0);
+        long long off = 0;
+        for (int l = 0; l < nlev; ++l)
+            for (int c = 0; c < C; ++c) {
+                int rs, re;
+                chunk_of(l, c, rs, re);
+                const int cnt = re - rs, npass = 1, np = pptr[re] - pptr[rs];
+                const int ne = slab_widths(rs, re);
+                const PsRec r = ps_rec(cnt, ne, np, elem);
+                if (off + r.size >= (1ll << 31)) return ("records exceed 2 GB");
+                if (bin[(size_t)l * C + c] >= (1 << 20)) return ("a level pushes more bytes than a barrier counts");
+                int *tr = &tab[((size_t)l * C + c) * 4];
+                tr[0] = (int)(off / 16);
+                tr[1] = r.size / 16;
+                tr[2] = (int)bin[(size_t)l * C + c];
+                const size_t w0 = (size_t)(off / 4);
+                rec.resize(w0 + r.size / 4, 0);
+                rec[w0 + 0] = cnt;
+                rec[w0 + 1] = ne;
+                rec[w0 + 2] = np;
+                bool hasg = false;  // an older entry read from the output vector (the kernel's slow path)
+                for (int t = rs; t < re; ++t)
+                    for (int k = sprp[t]; k < sprp[t + 1]; ++k) hasg = hasg || code[k] >= 0;
+                rec[w0 + 3] = npass | ((hasg ? 1 : 0) << 16);
+                const int slots = ps_slots(cnt);
+                std::vector<int> slab(slots / 32, 0);  // first entry slot of each warp's slab
+                for (int i = 0, acc = 0; i < slots / 32; ++i) {
+                    slab[i] = acc;
+                    acc += 32 * K[i];
+                }
+                int pnext = 0;
+                for (int q = 0; q <= slots; ++q) {
+                    int *ri = &rec[w0 + (r.o_info + 16 * q) / 4];
+                    ri[3] = pnext;
+                    if (q == slots || q >= cnt) {
+                        ri[0] = q == slots ? ne : 0;
+                        ri[1] = 0;
+                        ri[2] = -1;
+                        continue;
+                    }
+                    const int w = q / 32, lane = q % 32;
+                    const int t = rs + q, e0 = sprp[t], len = sprp[t + 1] - e0;
+                    const int first = slab[w] + lane;
+                    ri[0] = first;
+                    ri[1] = nsp[t] | (len << 16);
+                    ri[2] = perm[t];
+                    for (int k = 0; k < len; ++k) {
+                        rec[w0 + r.o_code / 4 + first + 32 * k] = code[e0 + k];
+                        dval[e0 + k] = (int)((off + r.o_val) / elem) + first + 32 * k;
+                    }
+                    for (int k = pptr[t]; k < pptr[t + 1]; ++k) rec[w0 + r.o_push / 4 + pnext++] = plist[k];
+                    dlv[t] = (int)((off + r.o_lv) / elem) + q;
+                    drhs[t] = (int)((off + r.o_rhs) / elem) + q;
+                }
+                off += r.size;
+            }
+        rec.resize(rec.size() + 16, 0);  // a copy never reads past the buffer
+        P.C = C;
+        P.nent = nent;
+        P.npush = (int)pushes.size();
+        P.cnt_max = cnt_max;
+        P.lay = lay;
+        P.ok = true;
+        return nullptr;
+    };
+    const char *why = "no layout";
     for (int S_own : {PS_S_OWN, PS_S_OWN / 2, PS_S_OWN / 4, PS_S_OWN / 8})
         for (int NB = PS_NB; NB >= 3; --NB) {
-            PushPlanHost P = push_plan_try(n, nlev, lptr, prp, pci, perm, level, ipos, C, elem, S_own, NB);
-            if (P.ok) return P;
-            best = std::move(P);
+            why = attempt(S_own, NB);
+            if (!why) {
+                P.ok = true;
+                return P;
+            }
         }
-    return best;
+    return fail(why);
 }
 
 }  // namespace ssg
