@@ -108,7 +108,7 @@ def build_solver(force=False, verbose=False):
         for _, out in results:
             sys.stdout.write(out)
     # every symbol resolved at link time: a missing definition fails the build, not the first load
-    _run([NVCC, *ARCH_FLAGS, "-shared", "-Xlinker", "--no-undefined", "-o", SOLVER_LIB, *objs, "-lcudart"])
+    _run([NVCC, *ARCH_FLAGS, "-shared", "-Xlinker", "--no-undefined", "-o", SOLVER_LIB, *objs, "-lcudart", "-lpthread"])
     return SOLVER_LIB
 
 

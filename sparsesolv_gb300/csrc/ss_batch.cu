@@ -1305,7 +1305,7 @@ void Batch::precond32(const Ti *r, Ti *z, const KState *stp) {
     const int n = h.n;
     Ti *y = v32[10].as<Ti>();
     const double fb = (4.0 + v) * h.Lf.nnz + 4.0 * (n + 1) + 2.0 * v * n;
-    if (h.push_ok(h.Lf, v) && h.push_ok(h.Ltb, v)) {
+    if (h.push_ok(v)) {
         h.timed(PC_FWD, fb, [&] {
             sweep_push<Ti>(h.Lf, L32.as<Ti>(), SW_FWD_DIV, r, invL32_lev.as<Ti>(), mix_epoch, y, stp, h.err(), s);
         });

@@ -178,8 +178,9 @@ void sweep_cluster(const Tri &tri, const T *val, int mode, const T *rhs, const T
                    const KState *st, int group, int *err, cudaStream_t s);
 
 // ss_push.cu: one-cluster push sweeps (IC pair: SW_FWD_DIV with lvec = 1/diagonal, SW_BWD_IC with lvec = D)
-// plan once per pattern and value size; false when the schedule does not fit (then another sweep serves)
-bool push_plan(Tri &T, size_t elem_bytes, cudaStream_t s);
+// plan once per pattern and value size; false when a schedule does not fit (then another sweep serves);
+// the count triangles of one call are planned side by side on host threads
+bool push_plan(Tri *const *tris, int count, size_t elem_bytes, cudaStream_t s);
 // val: the triangle's values in its level-ordered layout, lvec: per level-ordered row; epoch changes whenever
 // the values behind val / lvec change (the records are refilled then)
 template <typename T>

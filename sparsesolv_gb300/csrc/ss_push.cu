@@ -39,6 +39,8 @@
 // records ERR_TIMEOUT, every CTA leaves its level loop at the next step, waits
 // for the copies it issued and for the pushes in flight, and returns.
 #include <algorithm>
+#include <exception>
+#include <thread>
 
 #include "sparsesolv_gb300.h"
 #include "ss_internal.cuh"
@@ -492,61 +494,111 @@ static void upload(DBuf &d, const std::vector<I> &h, size_t pad_elems, cudaStrea
     if (!h.empty()) SSG_CUDA(cudaMemcpyAsync(d.p, h.data(), sizeof(I) * h.size(), cudaMemcpyHostToDevice, s));
 }
 
-// The plan: once per pattern and value size, on the host (ss_push_plan.cpp).
-bool push_plan(Tri &T, size_t elem_bytes, cudaStream_t s) {
+// The plans: once per pattern and value size, on the host (ss_push_plan.cpp). The triangles
+// of one call (the IC pair) are planned side by side on host threads; each plan depends on
+// its own triangle only, so the result is the one a call per triangle gives.
+bool push_plan(Tri *const *tris, int count, size_t elem_bytes, cudaStream_t s) {
     const int elem = (int)elem_bytes;
     const int ebit = elem == 4 ? 1 : elem == 8 ? 2 : 4;
-    PushPlan &P = T.push[elem == 4 ? 0 : elem == 8 ? 1 : 2];
-    if (P.n != T.n || P.nnz != T.nnz || P.nlev != T.nlev) {
-        // made for another triangle: start over (the shape is recorded before any attempt,
-        // so an infeasible plan is not retried on every call)
-        P.ready = false;
-        P.fail = 0;
-        P.n = T.n;
-        P.nnz = T.nnz;
-        P.nlev = T.nlev;
-    }
-    if (P.ready && P.elem == elem) return true;
-    if (P.fail & ebit) return false;
-    P.ready = false;
+    const int slot = elem == 4 ? 0 : elem == 8 ? 1 : 2;
+    struct Job {
+        Tri *T;
+        std::vector<int> prp, pci, perm, level, ipos;
+        PushPlanHost H;
+    };
+    std::vector<Job> jobs;
     const int C = push_cluster_size();
-    const int n = T.n;
-    if (C <= 0 || n == 0 || T.nlev < 2) {
-        P.fail |= ebit;
-        return false;
+    for (int i = 0; i < count; ++i) {
+        Tri &T = *tris[i];
+        PushPlan &P = T.push[slot];
+        if (P.n != T.n || P.nnz != T.nnz || P.nlev != T.nlev) {
+            // made for another triangle: start over (the shape is recorded before any attempt,
+            // so an infeasible plan is not retried on every call)
+            P.ready = false;
+            P.fail = 0;
+            P.n = T.n;
+            P.nnz = T.nnz;
+            P.nlev = T.nlev;
+        }
+        if (P.ready && P.elem == elem) continue;
+        if (P.fail & ebit) return false;
+        P.ready = false;
+        if (C <= 0 || T.n == 0 || T.nlev < 2) {
+            P.fail |= ebit;
+            return false;
+        }
+        jobs.push_back(Job{&T, {}, {}, {}, {}, {}, {}});
     }
-    std::vector<int> prp(n + 1), pci(T.nnz), perm(n), level(n), ipos(n);
-    SSG_CUDA(cudaMemcpyAsync(prp.data(), T.prp.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s));
-    SSG_CUDA(cudaMemcpyAsync(pci.data(), T.pci.p, sizeof(int) * (size_t)T.nnz, cudaMemcpyDeviceToHost, s));
-    SSG_CUDA(cudaMemcpyAsync(perm.data(), T.perm.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
-    SSG_CUDA(cudaMemcpyAsync(level.data(), T.level.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
-    SSG_CUDA(cudaMemcpyAsync(ipos.data(), T.ipos.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
-    SSG_CUDA(cudaStreamSynchronize(s));
-    PushPlanHost H = push_plan_host(n, T.nlev, T.lptr.data(), prp.data(), pci.data(), perm.data(), level.data(),
-                                    ipos.data(), C, elem);
-    if (!H.ok) {
-        P.fail |= ebit;
-        return false;
+    if (jobs.empty()) return true;
+    for (Job &j : jobs) {
+        const Tri &T = *j.T;
+        const int n = T.n;
+        j.prp.resize(n + 1);
+        j.pci.resize(T.nnz);
+        j.perm.resize(n);
+        j.level.resize(n);
+        j.ipos.resize(n);
+        SSG_CUDA(cudaMemcpyAsync(j.prp.data(), T.prp.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s));
+        SSG_CUDA(cudaMemcpyAsync(j.pci.data(), T.pci.p, sizeof(int) * (size_t)T.nnz, cudaMemcpyDeviceToHost, s));
+        SSG_CUDA(cudaMemcpyAsync(j.perm.data(), T.perm.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+        SSG_CUDA(cudaMemcpyAsync(j.level.data(), T.level.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+        SSG_CUDA(cudaMemcpyAsync(j.ipos.data(), T.ipos.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
     }
-    upload(P.tab, H.tab, 4, s);
-    upload(P.rec, H.rec, 16, s);
-    upload(P.vmap, H.vmap, 4, s);
-    upload(P.dval, H.dval, 4, s);
-    upload(P.dlv, H.dlv, 4, s);
-    upload(P.drhs, H.drhs, 4, s);
-    upload(P.perm, perm, 4, s);
-    upload(P.dnew, H.dnew, 4, s);
     SSG_CUDA(cudaStreamSynchronize(s));
-    P.key_val = P.key_lv = nullptr;
-    P.key_epoch = ~0ull;
-    P.elem = elem;
-    P.C = C;
-    P.nent = H.nent;
-    P.npush = H.npush;
-    P.nnew = (int)(H.dnew.size() / 2);
-    P.lay = H.lay;
-    P.ready = true;
-    return true;
+    auto plan = [&](Job &j) {
+        const Tri &T = *j.T;
+        j.H = push_plan_host(T.n, T.nlev, T.lptr.data(), j.prp.data(), j.pci.data(), j.perm.data(), j.level.data(),
+                             j.ipos.data(), C, elem);
+    };
+    {
+        std::vector<std::thread> pool;
+        std::vector<std::exception_ptr> errs(jobs.size());
+        for (size_t i = 1; i < jobs.size(); ++i)
+            pool.emplace_back([&, i] {
+                try {
+                    plan(jobs[i]);
+                } catch (...) {
+                    errs[i] = std::current_exception();
+                }
+            });
+        try {
+            plan(jobs[0]);
+        } catch (...) {
+            errs[0] = std::current_exception();
+        }
+        for (auto &t : pool) t.join();
+        for (auto &e : errs)
+            if (e) std::rethrow_exception(e);
+    }
+    bool all = true;
+    for (Job &j : jobs) {
+        PushPlan &P = j.T->push[slot];
+        const PushPlanHost &H = j.H;
+        if (!H.ok) {
+            P.fail |= ebit;
+            all = false;
+            continue;
+        }
+        upload(P.tab, H.tab, 4, s);
+        upload(P.rec, H.rec, 16, s);
+        upload(P.vmap, H.vmap, 4, s);
+        upload(P.dval, H.dval, 4, s);
+        upload(P.dlv, H.dlv, 4, s);
+        upload(P.drhs, H.drhs, 4, s);
+        upload(P.perm, j.perm, 4, s);
+        upload(P.dnew, H.dnew, 4, s);
+        SSG_CUDA(cudaStreamSynchronize(s));
+        P.key_val = P.key_lv = nullptr;
+        P.key_epoch = ~0ull;
+        P.elem = elem;
+        P.C = C;
+        P.nent = H.nent;
+        P.npush = H.npush;
+        P.nnew = (int)(H.dnew.size() / 2);
+        P.lay = H.lay;
+        P.ready = true;
+    }
+    return all;
 }
 
 template <typename T>

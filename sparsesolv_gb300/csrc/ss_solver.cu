@@ -373,14 +373,16 @@ bool Handle::cluster_ok(Tri &t, size_t elem, bool ic) {
 }
 
 // the push sweep (IC pair, with the reciprocal diagonal): forced by mode 4; the automatic
-// choice for real values wherever the one-cluster sweep would be and the push plan fits
-bool Handle::push_ok(Tri &t, size_t elem) {
-    if (!use_inv_diag || t.n == 0) return false;
+// choice for real values wherever the one-cluster sweep would be and both push plans fit
+bool Handle::push_ok(size_t elem) {
+    if (!use_inv_diag || Lf.n == 0) return false;
     if (sweep_mode != 4 && sweep_mode != 0) return false;
-    if (sweep_mode == 0 &&
-        (!push_auto || vtype == SSG_COMPLEX || (double)t.n > kAutoClusterRowsPerLevel * (double)t.nlev))
-        return false;
-    return push_plan(t, elem, stream);
+    for (const Tri *t : {&Lf, &Ltb})
+        if (sweep_mode == 0 &&
+            (!push_auto || vtype == SSG_COMPLEX || (double)t->n > kAutoClusterRowsPerLevel * (double)t->nlev))
+            return false;
+    Tri *pair[2] = {&Lf, &Ltb};
+    return push_plan(pair, 2, elem, stream);
 }
 
 // z = (L D L^T)^{-1} r using vec[10] as the forward result
@@ -388,7 +390,7 @@ template <typename T>
 void Handle::apply_precond(const T *d_r, T *d_z, const KState *stp) {
     T *y = vec[10].as<T>();
     const size_t v = sizeof(T);
-    if (push_ok(Lf, v) && push_ok(Ltb, v)) {
+    if (push_ok(v)) {
         timed(PC_FWD, tri_bytes(Lf, v, 2), [&] {
             sweep_push<T>(Lf, Lval.as<T>(), SW_FWD_DIV, d_r, invL_lev.as<T>(), fac_epoch, y, stp, err(), stream);
         });
@@ -714,7 +716,7 @@ Handle::TuneChoice Handle::autotune(bool keep_group, bool with_push) {
             cl_group = c.group;
             swcfg.cta_per_sm = c.cta_per_sm;
             // a cluster candidate whose plan does not fit would time the sync-free sweep again
-            if (c.mode == 4 && !(push_ok(Lf, sizeof(T)) && push_ok(Ltb, sizeof(T)))) continue;
+            if (c.mode == 4 && !push_ok(sizeof(T))) continue;
             if ((c.mode == 2 || c.mode == 3) && !(cluster_ok(Lf, sizeof(T), true) && cluster_ok(Ltb, sizeof(T), true)))
                 continue;
             if (c.mode == 3 && !(Lf.cl_p2p && Ltb.cl_p2p)) continue;

@@ -123,7 +123,7 @@ struct Handle {
     int cl_group = 4;              // lanes per row in the cluster sweep
     // ic: an IC sweep (the only kind the neighbour-synchronised plan serves)
     bool cluster_ok(Tri &t, size_t elem, bool ic);
-    bool push_ok(Tri &t, size_t elem);
+    bool push_ok(size_t elem);  // both triangles of the IC pair
     // the automatic mode may take the push sweep (off in the standalone batches: their
     // instances' bits must not depend on which schedule a batch's size leads to, and the
     // lane-summed schedules give the same bits at the same lanes a row)

@@ -106,7 +106,15 @@ def test_single_system_solve_with_mixed_precision(gpu):
             log = h.residual_log()
             assert log[-1] < TOL and h.iters() > 0
         ref = solve_batch([(rp, ci, va, b)], _capi.METHOD_ICCG)[0]
+        # the automatic schedule of a handle's own batch may take the push sweep (its own
+        # rounding); a standalone batch keeps to the lane-summed sweeps
+        assert range_err(rp, ci, va, b, x, ref[0][0]) <= 3e-8
+        # with the lane-summed sweep pinned the handle gives the batch's bits
+        h.set_tuning(_capi.TUNE_SWEEP_MODE, 2)
+        x = np.zeros_like(b)
+        assert h.solve(_capi.METHOD_ICCG, b, x, conv=TOL, max_ite=5000)
         assert np.array_equal(x, ref[0][0])
+        h.set_tuning(_capi.TUNE_SWEEP_MODE, 0)
         # unsupported combinations are refused, not approximated
         o.is_diag_scale = 1
         h.set_options(o)
