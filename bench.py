@@ -12,8 +12,9 @@ buffers (values, b and x0 copied in, x copied out inside the timed region).
 The line also carries, for the same matrix on the same GPU: the solution's
 distance from a full FP64 solve of the oracle (``parity``), the mixed-precision
 solve against this plain FP64 one (``mixed``), the serving stream against the
-plain path one request at a time (``serving``), and the first solve of a new
-sparsity pattern (``new_pattern``).
+plain path one request at a time (``serving``), the first solve of a new
+sparsity pattern (``new_pattern``), and the 256-system batch of the cfg4
+workload in FP64 and mixed precision (``batch``).
 
     python bench.py [--steps K] [--warmup W] [--method iccg|sgs|mrtr_ic]
                     [--workload cfg2|cfg1|cfg3|cfg4|cfg5] [--sweep-mode 0..4]
@@ -94,6 +95,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="leave the mixed-precision comparison out of the line")
     ap.add_argument("--no-serving", action="store_true", help="leave the serving stream out of the line")
+    ap.add_argument("--no-batch", action="store_true", help="leave the 256-system batch out of the line")
     ap.add_argument("--cpu-threads", type=int, default=0,
                     help="OpenMP threads of the CPU path (reference arm and cpu_baseline); 0: all host cores")
     ap.add_argument("--autotune", action="store_true",
@@ -530,6 +532,8 @@ def run_ours(args):
         if not args.no_serving and args.workload == "cfg2" and K == 1:
             line["serving"] = serving_measure(local, args.requests, args.slots, args.share, None, warm_runs=1,
                                               sweep=False)
+        if not args.no_batch and args.workload == "cfg2" and K == 1:
+            line["batch"] = batch_measure(local, args.batch_sizes, args.batch_persistent)
     h.close()
     print(json.dumps(line), flush=True)
     if ws > 1:
@@ -777,6 +781,51 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def batch_measure(local, sizes, persistent, steps=2):
+    """The 256-system batch (the --workload cfg4 line's workload: curl-curl systems
+    of N ~ U{8..32} voxels a side, 4 coil right-hand sides each, ICCG alpha 1.1 to
+    1e-8) in FP64 and in mixed precision: instances solved per second over `steps`
+    steps after a warm step, CUDA events on the batch's stream, each step
+    re-factoring every system. The full line (latency, e2e, plain GPU ratio) is
+    --workload cfg4's."""
+    import torch
+    from sparsesolv_gb300 import _capi, voxel
+    dev = torch.device("cuda", local)
+    lo, hi = (int(v) for v in sizes.split(","))
+    systems = []
+    for case, coils in voxel.batched_cases(lo=lo, hi=hi):
+        systems.append(case.assemble(coils_list=coils))
+    out = {"workload": "256 curl-curl systems, N ~ U{%d..%d} voxels, 4 coil right-hand sides each" % (lo, hi),
+           "instances": int(sum(len(B) for _, _, _, B in systems)), "steps": steps,
+           "what": "instances solved per second, each step re-factoring every system (CUDA events)"}
+    for prec in ("fp64", "mixed"):
+        bt = _capi.Batch(local)
+        try:
+            bt.set_precision(_capi.PREC_MIXED if prec == "mixed" else _capi.PREC_FP64)
+            bt.set_persistent(persistent)
+            for rp, ci, va, B in systems:
+                bt.add(rp, ci, va, B)
+            bt.start(_capi.METHOD_ICCG, ALPHA, conv=TOL, max_ite=MAXIT)
+            bt.wait()
+            stream = torch.cuda.ExternalStream(bt.stream(), device=dev)
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                bt.start(_capi.METHOD_ICCG, ALPHA, conv=TOL, max_ite=MAXIT)
+                bt.wait()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms = e0.elapsed_time(e1)
+            ok = all(bt.result(k)[3] for k in range(len(systems)))
+            out[prec] = {"solves_per_s": out["instances"] * steps / (ms / 1e3), "ms_per_step": ms / steps,
+                         "converged": bool(ok)}
+        finally:
+            bt.close()
+    out["mixed_vs_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    return out
 
 
 def serving_measure(local, requests, slots, share, precision, warm_runs=1, sweep=True):
