@@ -253,8 +253,9 @@ __global__ void __launch_bounds__(ff_warps<T>() * 32) k_ic_factor_fast(int n, co
                                                                        T *D, int *done, double alpha, int *ticket,
                                                                        int *err, int backoff_ns, const int *sub) {
     constexpr int FF_WARPS = ff_warps<T>();
-    __shared__ int s_c[FF_WARPS][FF_MAXROW][FF_MAXROW - 1];
-    __shared__ T s_v[FF_WARPS][FF_MAXROW][FF_MAXROW - 1];
+    __shared__ int s_c[FF_WARPS][FF_MAXROW][FF_MAXROW - 1];            // columns of row j
+    __shared__ unsigned char s_p[FF_WARPS][FF_MAXROW][FF_MAXROW - 1];  // step kk: position of c_kk in row j
+    __shared__ T s_v[FF_WARPS][FF_MAXROW][FF_MAXROW - 1];              // step kk: L_jk
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (;;) {
         int t = 0;
@@ -285,7 +286,33 @@ __global__ void __launch_bounds__(ff_warps<T>() * 32) k_ic_factor_fast(int n, co
             continue;
         }
         const bool off = have && lane < m - 1;  // off-diagonal entry (column < i)
+        // Before the wait, from the pattern alone: row j = c (without its diagonal, its last
+        // entry) has its columns staged, and each lane finds, for every earlier step kk,
+        // whether row j holds column c_kk and where (the merge the step would otherwise walk
+        // on the critical path).
+        int2 dj = make_int2(0, 0);
         int mj = 0;
+        unsigned hits = 0u;  // bit kk: row j holds column c_kk
+        if (off) {
+            dj = NAT ? make_int2(prp[c], prp[c + 1] - prp[c]) : dep[a + lane];
+            mj = min(dj.y - 1, FF_MAXROW - 1);
+#pragma unroll
+            for (int l = 0; l < FF_MAXROW - 1; ++l)
+                if (l < mj) s_c[w][lane][l] = __ldg(pci + dj.x + l);
+        }
+        {
+            int ptr = 0;
+            for (int kk = 0; kk < m - 1; ++kk) {
+                const int ck = __shfl_sync(0xffffffffu, c, kk);
+                if (off && lane > kk) {
+                    while (ptr < mj && s_c[w][lane][ptr] < ck) ++ptr;
+                    if (ptr < mj && s_c[w][lane][ptr] == ck) {
+                        hits |= 1u << kk;
+                        s_p[w][lane][kk] = (unsigned char)ptr;
+                    }
+                }
+            }
+        }
         T dk = Sc<T>::zero();
         if (off) {
             const volatile int *f = done + c;
@@ -304,33 +331,25 @@ __global__ void __launch_bounds__(ff_warps<T>() * 32) k_ic_factor_fast(int n, co
                 }
             }
             __threadfence();
+            // row j is final: its pivot and the values this row's steps use
             dk = ldcg(D + c);
-            // row j = c without its diagonal (its last entry); the loads are independent
-            // (start, length) of row j in level order
-            const int2 dj = NAT ? make_int2(prp[c], prp[c + 1] - prp[c]) : dep[a + lane];
-            mj = min(dj.y - 1, FF_MAXROW - 1);
-#pragma unroll
-            for (int l = 0; l < FF_MAXROW - 1; ++l) {
-                if (l < mj) {
-                    s_c[w][lane][l] = ldcg(pci + dj.x + l);
-                    s_v[w][lane][l] = ldcg(lval + dj.x + l);
-                }
+            for (unsigned h = hits; h; h &= h - 1) {
+                const int kk = __ffs(h) - 1;
+                s_v[w][lane][kk] = ldcg(lval + dj.x + s_p[w][lane][kk]);
             }
         }
         __syncwarp();
         // diagonal lane starts from alpha * a_ii (src/SprsPreconditioner.cpp:95)
         if (lane == m - 1) v = v * Sc<T>::from(alpha);
-        int ptr = 0;
         for (int kk = 0; kk < m - 1; ++kk) {
-            const T Lk = Sc<T>::shfl(v, kk);       // final L_ik
-            const int ck = __shfl_sync(0xffffffffu, c, kk);
+            const T Lk = Sc<T>::shfl(v, kk);  // final L_ik
             const T Dk = Sc<T>::shfl(dk, kk);
-            if (off && lane > kk) {
-                while (ptr < mj && s_c[w][lane][ptr] < ck) ++ptr;
-                if (ptr < mj && s_c[w][lane][ptr] == ck) v = v - (Lk * s_v[w][lane][ptr]) * Dk;
-            } else if (lane == m - 1) {
-                v = v - (Lk * Lk) * Dk;
-            }
+            // an off-diagonal lane subtracts L_ik L_jk D_k when row j holds column k; the
+            // diagonal lane L_ik L_ik D_k: one update for both
+            const bool diag = lane == m - 1;
+            const bool hit = diag || ((hits >> kk) & 1u);
+            const T o = diag ? Lk : s_v[w][lane][kk];
+            if (hit) v = v - (Lk * o) * Dk;
         }
         if (have) lval[a + lane] = v;
         if (lane == m - 1) D[i] = (Sc<T>::absv(v) < 1.0e-12) ? Sc<T>::from(1.0 / DBL_EPSILON) : Sc<T>::one() / v;
