@@ -462,14 +462,14 @@ def run_ours(args):
     h.set_profiling(False)
     # ---- end-to-end through the C ABI with host buffers
     barrier()
-    f0 = torch.cuda.Event(enable_timing=True)
-    f1 = torch.cuda.Event(enable_timing=True)
-    f0.record(stream)
-    for _ in range(args.steps):
+    fe = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    fe[0].record(stream)
+    for k in range(args.steps):
         ok = step_host() and ok
-    f1.record(stream)
+        fe[k + 1].record(stream)
     barrier()
-    ms_e2e = f0.elapsed_time(f1)
+    ms_e2e = fe[0].elapsed_time(fe[-1])
+    e2e_step_ms = [fe[k].elapsed_time(fe[k + 1]) for k in range(args.steps)]
     gpu_log = h.residual_log()
     xs = x_h.numpy().reshape(K, n).copy()
     bs = b.reshape(K, n)
@@ -501,7 +501,9 @@ def run_ours(args):
         "time_to_tolerance_s": ms_max / args.steps / 1e3,
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
                        "steps": len(step_ms)},
-        "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": val.itemsize * nnz + 2 * b.itemsize * n * K,
+        "e2e": {"value": e2e, "unit": "solves/s",
+                "step_ms": {"min": min(e2e_step_ms), "median": float(np.median(e2e_step_ms)), "max": max(e2e_step_ms)},
+                "h2d_bytes_per_step": val.itemsize * nnz + 2 * b.itemsize * n * K,
                 "d2h_bytes_per_step": b.itemsize * n * K},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
