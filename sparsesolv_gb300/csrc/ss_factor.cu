@@ -230,16 +230,17 @@ __global__ void __launch_bounds__(256) k_ic_factor(int n, const int *perm, const
 }
 
 // ---------------------------------------------------------------- fast factor
-// Rows of at most 32 entries (every row of the voxel curl-curl matrices has 17
-// in its lower triangle): lane k owns entry k of row i. The entries are
+// Rows of at most 32 entries (the voxel curl-curl matrices have 16 to 18 in
+// their lower triangle): lane k owns entry k of row i. The entries are
 // finished left to right; as soon as entry kk is final, every lane jj > kk
 // subtracts its contribution L_ik L_jk D_k (when column k also appears in
 // row j) -- the same terms, subtracted in the same order, as the reference's
 // loop over kk, so with FMA contraction off (this file is compiled with
-// -fmad=false) the real factor is bit-identical to the reference's. Row j of
-// each entry is staged in shared memory once its done flag is seen; its start
-// in the level-ordered arrays comes from a per-entry table built once per
-// pattern.
+// -fmad=false) the real factor is bit-identical to the reference's. Before a
+// lane waits for row j (its entry's column), it stages row j's columns (the
+// row's start in the level-ordered arrays comes from a per-entry table built
+// once per pattern) and finds where row j holds each earlier column of row i;
+// once row j's done flag is seen, only its pivot and those values are loaded.
 constexpr int FF_MAXROW = 32;
 int factor_blocks_per_sm = 4;  // rows in flight: enough for a level, few enough not to congest L2
 template <typename T>
