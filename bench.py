@@ -463,11 +463,14 @@ def run_ours(args):
     # ---- end-to-end through the C ABI with host buffers
     barrier()
     fe = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    clocks_e2e = Clocks(local)
+    clocks_e2e.start()
     fe[0].record(stream)
     for k in range(args.steps):
         ok = step_host() and ok
         fe[k + 1].record(stream)
     barrier()
+    clk_e2e = clocks_e2e.stop()
     ms_e2e = fe[0].elapsed_time(fe[-1])
     e2e_step_ms = [fe[k].elapsed_time(fe[k + 1]) for k in range(args.steps)]
     gpu_log = h.residual_log()
@@ -503,6 +506,7 @@ def run_ours(args):
                        "steps": len(step_ms)},
         "e2e": {"value": e2e, "unit": "solves/s",
                 "step_ms": {"min": min(e2e_step_ms), "median": float(np.median(e2e_step_ms)), "max": max(e2e_step_ms)},
+                "clocks": clk_e2e,
                 "h2d_bytes_per_step": val.itemsize * nnz + 2 * b.itemsize * n * K,
                 "d2h_bytes_per_step": b.itemsize * n * K},
         "gpu_launches": launches,
