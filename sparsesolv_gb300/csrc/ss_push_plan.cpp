@@ -21,8 +21,48 @@
 #include "ss_push_plan.hpp"
 
 #include <algorithm>
+#include <exception>
+#include <thread>
 
 namespace ssg {
+
+// The plan's row-, consumer- and record-wise passes run on host threads: each item's
+// output has a place fixed before the pass (prefix sums), so the plan does not depend on
+// the thread count. Two triangles are planned at once, so a plan takes half the cores.
+static int plan_threads() {
+    const unsigned hc = std::thread::hardware_concurrency();
+    return (int)std::max(1u, std::min(16u, hc / 2));
+}
+// f(begin, end) over [0, n) in nt contiguous parts; an exception in a part is rethrown here
+template <typename F>
+static void par_for(int n, int nt, F f) {
+    if (nt <= 1 || n < 4096) {
+        f(0, n);
+        return;
+    }
+    const int part = (n + nt - 1) / nt;
+    std::vector<std::thread> pool;
+    std::vector<std::exception_ptr> errs(nt);
+    for (int q = 1; q < nt; ++q) {
+        const int b = q * part, e = std::min(n, b + part);
+        if (b >= e) break;
+        pool.emplace_back([&, b, e, q] {
+            try {
+                f(b, e);
+            } catch (...) {
+                errs[q] = std::current_exception();
+            }
+        });
+    }
+    try {
+        f(0, std::min(n, part));
+    } catch (...) {
+        errs[0] = std::current_exception();
+    }
+    for (auto &t : pool) t.join();
+    for (auto &e : errs)
+        if (e) std::rethrow_exception(e);
+}
 
 PushLayout push_layout(int S_own, int S_recv, int cap_rec, int elem, int NB) {
     PushLayout L{};
@@ -85,36 +125,65 @@ PushPlanHost push_plan_host(int n, int nlev, const int *lptr, const int *prp, co
             }
         }
     if (cap_r > PS_CT * PS_MAXQ) return fail("a level chunk has more rows than the CTA holds");
-    // entries (off-diagonal) sorted per row by (dependency level, column)
+    const int nt = plan_threads();
+    // entries (off-diagonal) sorted per row by (dependency level, column); a failing row
+    // is reported as the first in row order, whatever the thread count
     std::vector<int> sprp(n + 1, 0), nsp(n, 0), &vmap = P.vmap;
-    vmap.reserve(prp[n]);
-    std::vector<int> dep;
-    dep.reserve(prp[n]);
-    std::vector<std::pair<long long, int>> row;  // (level << 32 | column, entry)
-    for (int t = 0; t < n; ++t) {
-        const int i = perm[t], lt = level[i];
-        row.clear();
-        for (int k = prp[t]; k < prp[t + 1]; ++k) {
-            const int j = pci[k];
-            if (j == i) continue;
-            if (j < 0 || j >= n || level[j] >= lt) return fail("an entry is not a dependency of its row");
-            row.push_back({((long long)level[j] << 32) | (unsigned)j, k});
+    par_for(n, nt, [&](int b, int e) {
+        for (int t = b; t < e; ++t) {
+            const int i = perm[t];
+            int m = 0;
+            for (int k = prp[t]; k < prp[t + 1]; ++k) m += pci[k] != i;
+            sprp[t + 1] = m;
         }
-        std::sort(row.begin(), row.end());
-        int nold = 0;
-        for (auto &e : row) {
-            if ((int)(e.first >> 32) < lt - 1) ++nold;
-            vmap.push_back(e.second);
-            dep.push_back((int)(e.first & 0xFFFFFFFF));
-        }
-        nsp[t] = nold;
-        sprp[t + 1] = (int)vmap.size();
-        for (int k = sprp[t] + nold; k < sprp[t + 1]; ++k) {
+    });
+    for (int t = 0; t < n; ++t) sprp[t + 1] += sprp[t];
+    vmap.assign((size_t)sprp[n], 0);
+    std::vector<int> dep((size_t)sprp[n]);
+    std::vector<int> bad_row(nt, n), bad_why(nt, 0);  // per part: first failing row, 1 not a dependency, 2 too long
+    {
+        const int part = (n + nt - 1) / nt;
+        par_for(n, nt, [&](int b, int e) {
+            const int q = n < 4096 ? 0 : b / part;
+            std::vector<std::pair<long long, int>> row;  // (level << 32 | column, entry)
+            for (int t = b; t < e; ++t) {
+                const int i = perm[t], lt = level[i];
+                row.clear();
+                bool ok = true;
+                for (int k = prp[t]; k < prp[t + 1]; ++k) {
+                    const int j = pci[k];
+                    if (j == i) continue;
+                    if (j < 0 || j >= n || level[j] >= lt) {
+                        ok = false;
+                        break;
+                    }
+                    row.push_back({((long long)level[j] << 32) | (unsigned)j, k});
+                }
+                if (!ok || row.size() > 0xFFFF) {
+                    bad_row[q] = t;
+                    bad_why[q] = ok ? 2 : 1;
+                    return;
+                }
+                std::sort(row.begin(), row.end());
+                int nold = 0, o = sprp[t];
+                for (auto &en : row) {
+                    if ((int)(en.first >> 32) < lt - 1) ++nold;
+                    vmap[o] = en.second;
+                    dep[o] = (int)(en.first & 0xFFFFFFFF);
+                    ++o;
+                }
+                nsp[t] = nold;
+            }
+        });
+    }
+    for (int q = 0; q < nt; ++q)
+        if (bad_why[q]) return fail(bad_why[q] == 1 ? "an entry is not a dependency of its row"
+                                                    : "a row longer than 65535 entries");
+    for (int t = 0; t < n; ++t)
+        for (int k = sprp[t] + nsp[t]; k < sprp[t + 1]; ++k) {
             P.dnew.push_back(k);
             P.dnew.push_back(t);
         }
-        if (sprp[t + 1] - sprp[t] > 0xFFFF) return fail("a row longer than 65535 entries");
-    }
     const int nent = (int)vmap.size();
     // codes; reads through the receive ring collected per consumer
     std::vector<int> code(nent, 0);
@@ -123,21 +192,63 @@ PushPlanHost push_plan_host(int n, int nlev, const int *lptr, const int *prp, co
         int entry, use;
         bool operator<(const Req &o) const { return key < o.key || (key == o.key && entry < o.entry); }
     };
-    std::vector<Req> reqs;
-    for (int t = 0; t < n; ++t) {
-        const int c = owner[t], lt = level[perm[t]];
-        for (int k = sprp[t]; k < sprp[t + 1]; ++k) {
-            const int j = dep[k], lj = level[j], pj = ipos[j], cj = owner[pj];
-            if (cj == c) {
-                continue;  // own ring or memory: depends on the ring size (per layout below)
-            } else if (lt - lj <= LEAD + 1) {
-                reqs.push_back({((long long)c << 58) | ((long long)lj << 32) | (unsigned)pj, k, lt});
-            } else {
-                code[k] = j;
+    // collected per part and consumer, then per consumer sorted: the key's top bits are the
+    // consumer, so the consumers' sorted runs in order are the whole sorted list
+    std::vector<std::vector<std::vector<Req>>> parts(nt, std::vector<std::vector<Req>>(C));
+    {
+        const int part = (n + nt - 1) / nt;
+        par_for(n, nt, [&](int b, int e) {
+            std::vector<std::vector<Req>> &mine = parts[n < 4096 ? 0 : b / part];
+            for (int t = b; t < e; ++t) {
+                const int c = owner[t], lt = level[perm[t]];
+                for (int k = sprp[t]; k < sprp[t + 1]; ++k) {
+                    const int j = dep[k], lj = level[j], pj = ipos[j], cj = owner[pj];
+                    if (cj == c) {
+                        continue;  // own ring or memory: depends on the ring size (per layout below)
+                    } else if (lt - lj <= LEAD + 1) {
+                        mine[c].push_back({((long long)c << 58) | ((long long)lj << 32) | (unsigned)pj, k, lt});
+                    } else {
+                        code[k] = j;
+                    }
+                }
             }
+        });
+    }
+    std::vector<std::vector<Req>> byc(C);
+    {
+        std::vector<std::thread> pool;
+        std::vector<std::exception_ptr> errs(C);
+        auto one = [&](int c) {
+            try {
+                size_t total = 0;
+                for (int q = 0; q < nt; ++q) total += parts[q][c].size();
+                byc[c].reserve(total);
+                for (int q = 0; q < nt; ++q) byc[c].insert(byc[c].end(), parts[q][c].begin(), parts[q][c].end());
+                std::sort(byc[c].begin(), byc[c].end());
+            } catch (...) {
+                errs[c] = std::current_exception();
+            }
+        };
+        for (int c0 = 0; c0 < C; c0 += nt) {  // at most nt consumers at a time
+            for (int c = c0 + 1; c < std::min(C, c0 + nt); ++c) pool.emplace_back(one, c);
+            one(c0);
+            for (auto &t : pool) t.join();
+            pool.clear();
+        }
+        for (auto &e : errs)
+            if (e) std::rethrow_exception(e);
+    }
+    parts.clear();
+    std::vector<Req> reqs;
+    {
+        size_t total = 0;
+        for (int c = 0; c < C; ++c) total += byc[c].size();
+        reqs.reserve(total);
+        for (int c = 0; c < C; ++c) {
+            reqs.insert(reqs.end(), byc[c].begin(), byc[c].end());
+            std::vector<Req>().swap(byc[c]);
         }
     }
-    std::sort(reqs.begin(), reqs.end());
     struct Push {
         int c, pj, lp, last_use;
     };
@@ -188,18 +299,27 @@ PushPlanHost push_plan_host(int n, int nlev, const int *lptr, const int *prp, co
         // own entries: the own ring while their slot is not reused before the end of the
         // reading row's level, else the output vector (never a newest entry)
         code = code0;
-        for (int t = 0; t < n; ++t) {
-            const int c = owner[t], lt = level[perm[t]];
-            for (int k = sprp[t]; k < sprp[t + 1]; ++k) {
-                const int j = dep[k], pj = ipos[j];
-                if (owner[pj] != c) continue;
-                const int oj = ordc[pj], reuse = oj + S_own;
-                const bool in_ring = reuse >= (int)levof[c].size() || levof[c][reuse] >= lt + 1;
-                if (in_ring) code[k] = -1 - (oj % S_own);
-                else if (level[j] != lt - 1) code[k] = j;
-                else return "a newest own dependency left the own ring";
-            }
+        std::vector<char> left_ring(nt, 0);
+        {
+            const int part = (n + nt - 1) / nt;
+            par_for(n, nt, [&](int b, int e) {
+                char &flag = left_ring[n < 4096 ? 0 : b / part];
+                for (int t = b; t < e && !flag; ++t) {
+                    const int c = owner[t], lt = level[perm[t]];
+                    for (int k = sprp[t]; k < sprp[t + 1]; ++k) {
+                        const int j = dep[k], pj = ipos[j];
+                        if (owner[pj] != c) continue;
+                        const int oj = ordc[pj], reuse = oj + S_own;
+                        const bool in_ring = reuse >= (int)levof[c].size() || levof[c][reuse] >= lt + 1;
+                        if (in_ring) code[k] = -1 - (oj % S_own);
+                        else if (level[j] != lt - 1) code[k] = j;
+                        else flag = 1;
+                    }
+                }
+            });
         }
+        for (char f : left_ring)
+            if (f) return "a newest own dependency left the own ring";
         // receive slots per consumer, and the reuse proof
         std::vector<int> slot(pushes.size());
         {
@@ -224,29 +344,46 @@ PushPlanHost push_plan_host(int n, int nlev, const int *lptr, const int *prp, co
         }
         std::vector<long long> bin((size_t)nlev * C, 0);
         for (auto &p : pushes) bin[(size_t)p.lp * C + p.c] += elem;
-        // the records, in (level, CTA) order
+        // the records, in (level, CTA) order: sizes and offsets first (with the checks, in
+        // record order), then every record filled on its own
         std::vector<int> &tab = P.tab, &rec = P.rec, &dval = P.dval, &dlv = P.dlv, &drhs = P.drhs;
-        tab.assign((size_t)nlev * C * 4, 0);
-        rec.clear();
-        dval.assign(nent, 0);
-        dlv.assign(n, 0);
-        drhs.assign(n, 0);
-        long long off = 0;
+        const int nrec = nlev * C;
+        std::vector<long long> roff((size_t)nrec + 1, 0);
+        std::vector<int> rne(nrec);
         for (int l = 0; l < nlev; ++l)
             for (int c = 0; c < C; ++c) {
                 int rs, re;
                 chunk_of(l, c, rs, re);
-                const int cnt = re - rs, npass = 1, np = pptr[re] - pptr[rs];
+                const size_t id = (size_t)l * C + c;
                 const int ne = slab_widths(rs, re);
+                const PsRec r = ps_rec(re - rs, ne, pptr[re] - pptr[rs], elem);
+                if (roff[id] + r.size >= (1ll << 31)) return ("records exceed 2 GB");
+                if (bin[id] >= (1 << 20)) return ("a level pushes more bytes than a barrier counts");
+                rne[id] = ne;
+                roff[id + 1] = roff[id] + r.size;
+            }
+        tab.assign((size_t)nrec * 4, 0);
+        rec.assign((size_t)(roff[nrec] / 4) + 16, 0);  // a copy never reads past the buffer
+        dval.assign(nent, 0);
+        dlv.assign(n, 0);
+        drhs.assign(n, 0);
+        par_for(nrec, nt, [&](int b, int e) {
+            std::vector<int> Kl, slab;  // this part's slab widths and slab starts
+            for (int id = b; id < e; ++id) {
+                const int l = id / C, c = id % C;
+                int rs, re;
+                chunk_of(l, c, rs, re);
+                const int cnt = re - rs, npass = 1, np = pptr[re] - pptr[rs];
+                const int ne = rne[id];
                 const PsRec r = ps_rec(cnt, ne, np, elem);
-                if (off + r.size >= (1ll << 31)) return ("records exceed 2 GB");
-                if (bin[(size_t)l * C + c] >= (1 << 20)) return ("a level pushes more bytes than a barrier counts");
-                int *tr = &tab[((size_t)l * C + c) * 4];
+                const long long off = roff[id];
+                Kl.assign((size_t)ps_slots(cnt) / 32, 0);
+                for (int q = 0; q < cnt; ++q) Kl[q / 32] = std::max(Kl[q / 32], sprp[rs + q + 1] - sprp[rs + q]);
+                int *tr = &tab[(size_t)id * 4];
                 tr[0] = (int)(off / 16);
                 tr[1] = r.size / 16;
-                tr[2] = (int)bin[(size_t)l * C + c];
+                tr[2] = (int)bin[id];
                 const size_t w0 = (size_t)(off / 4);
-                rec.resize(w0 + r.size / 4, 0);
                 rec[w0 + 0] = cnt;
                 rec[w0 + 1] = ne;
                 rec[w0 + 2] = np;
@@ -255,10 +392,10 @@ PushPlanHost push_plan_host(int n, int nlev, const int *lptr, const int *prp, co
                     for (int k = sprp[t]; k < sprp[t + 1]; ++k) hasg = hasg || code[k] >= 0;
                 rec[w0 + 3] = npass | ((hasg ? 1 : 0) << 16);
                 const int slots = ps_slots(cnt);
-                std::vector<int> slab(slots / 32, 0);  // first entry slot of each warp's slab
+                slab.assign(slots / 32, 0);  // first entry slot of each warp's slab
                 for (int i = 0, acc = 0; i < slots / 32; ++i) {
                     slab[i] = acc;
-                    acc += 32 * K[i];
+                    acc += 32 * Kl[i];
                 }
                 int pnext = 0;
                 for (int q = 0; q <= slots; ++q) {
@@ -284,9 +421,8 @@ PushPlanHost push_plan_host(int n, int nlev, const int *lptr, const int *prp, co
                     dlv[t] = (int)((off + r.o_lv) / elem) + q;
                     drhs[t] = (int)((off + r.o_rhs) / elem) + q;
                 }
-                off += r.size;
             }
-        rec.resize(rec.size() + 16, 0);  // a copy never reads past the buffer
+        });
         P.C = C;
         P.nent = nent;
         P.npush = (int)pushes.size();
