@@ -553,19 +553,22 @@ bool push_plan(Tri *const *tris, int count, size_t elem_bytes, cudaStream_t s) {
     {
         std::vector<std::thread> pool;
         std::vector<std::exception_ptr> errs(jobs.size());
-        for (size_t i = 1; i < jobs.size(); ++i)
-            pool.emplace_back([&, i] {
-                try {
-                    plan(jobs[i]);
-                } catch (...) {
-                    errs[i] = std::current_exception();
-                }
-            });
-        try {
-            plan(jobs[0]);
-        } catch (...) {
-            errs[0] = std::current_exception();
+        auto run = [&](size_t i) {
+            try {
+                plan(jobs[i]);
+            } catch (...) {
+                errs[i] = std::current_exception();
+            }
+        };
+        std::vector<size_t> here{0};  // plans run on this thread (a thread that cannot start)
+        for (size_t i = 1; i < jobs.size(); ++i) {
+            try {
+                pool.emplace_back(run, i);
+            } catch (...) {
+                here.push_back(i);
+            }
         }
+        for (size_t i : here) run(i);
         for (auto &t : pool) t.join();
         for (auto &e : errs)
             if (e) std::rethrow_exception(e);

@@ -33,7 +33,8 @@ static int plan_threads() {
     const unsigned hc = std::thread::hardware_concurrency();
     return (int)std::max(1u, std::min(16u, hc / 2));
 }
-// f(begin, end) over [0, n) in nt contiguous parts; an exception in a part is rethrown here
+// f(begin, end) over [0, n) in nt contiguous parts; an exception in a part is rethrown here.
+// A part whose thread cannot be started runs on the calling thread.
 template <typename F>
 static void par_for(int n, int nt, F f) {
     if (nt <= 1 || n < 4096) {
@@ -43,22 +44,25 @@ static void par_for(int n, int nt, F f) {
     const int part = (n + nt - 1) / nt;
     std::vector<std::thread> pool;
     std::vector<std::exception_ptr> errs(nt);
+    auto run = [&](int b, int e, int q) {
+        try {
+            f(b, e);
+        } catch (...) {
+            errs[q] = std::current_exception();
+        }
+    };
+    std::vector<int> inline_parts;
     for (int q = 1; q < nt; ++q) {
         const int b = q * part, e = std::min(n, b + part);
         if (b >= e) break;
-        pool.emplace_back([&, b, e, q] {
-            try {
-                f(b, e);
-            } catch (...) {
-                errs[q] = std::current_exception();
-            }
-        });
+        try {
+            pool.emplace_back(run, b, e, q);
+        } catch (...) {
+            inline_parts.push_back(q);
+        }
     }
-    try {
-        f(0, std::min(n, part));
-    } catch (...) {
-        errs[0] = std::current_exception();
-    }
+    run(0, std::min(n, part), 0);
+    for (int q : inline_parts) run(q * part, std::min(n, q * part + part), q);
     for (auto &t : pool) t.join();
     for (auto &e : errs)
         if (e) std::rethrow_exception(e);
@@ -230,8 +234,15 @@ PushPlanHost push_plan_host(int n, int nlev, const int *lptr, const int *prp, co
             }
         };
         for (int c0 = 0; c0 < C; c0 += nt) {  // at most nt consumers at a time
-            for (int c = c0 + 1; c < std::min(C, c0 + nt); ++c) pool.emplace_back(one, c);
-            one(c0);
+            std::vector<int> here{c0};        // consumers run on this thread
+            for (int c = c0 + 1; c < std::min(C, c0 + nt); ++c) {
+                try {
+                    pool.emplace_back(one, c);
+                } catch (...) {
+                    here.push_back(c);
+                }
+            }
+            for (int c : here) one(c);
             for (auto &t : pool) t.join();
             pool.clear();
         }
