@@ -21,6 +21,7 @@
 #include "ss_push_plan.hpp"
 
 #include <algorithm>
+#include <cstdlib>
 #include <exception>
 #include <thread>
 
@@ -28,8 +29,13 @@ namespace ssg {
 
 // The plan's row-, consumer- and record-wise passes run on host threads: each item's
 // output has a place fixed before the pass (prefix sums), so the plan does not depend on
-// the thread count. Two triangles are planned at once, so a plan takes half the cores.
+// the thread count. Two triangles are planned at once, so a plan takes half the cores;
+// SSG_PLAN_THREADS (1-64) sets the count.
 static int plan_threads() {
+    if (const char *e = std::getenv("SSG_PLAN_THREADS")) {
+        const int v = std::atoi(e);
+        if (v >= 1 && v <= 64) return v;
+    }
     const unsigned hc = std::thread::hardware_concurrency();
     return (int)std::max(1u, std::min(16u, hc / 2));
 }

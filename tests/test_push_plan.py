@@ -298,3 +298,20 @@ def test_push_plan_on_edge_matrices(planlib, oracle):
     tri, _, _, _ = level_ordered(oracle, Ar.indptr.astype(np.int32), Ar.indices.astype(np.int32), True)
     P = plan(planlib, tri, 16, 8)
     assert not P["ok"] and "shared memory" in P["why"]
+
+
+def test_push_plan_independent_of_thread_count(planlib, oracle, monkeypatch):
+    """The plan's passes run on host threads with every output's place fixed
+    beforehand: one thread and several give the same plan, array for array."""
+    rp, ci, va, b = voxel.curl_curl_case(32, seed=5, n_iron=2, iron_size=5).assemble()
+    keys = ["tab", "rec", "vmap", "dval", "dlv", "drhs", "dnew"]
+    for lower in (True, False):
+        tri, _, _, _ = level_ordered(oracle, rp, ci, lower)
+        plans = []
+        for nt in ("1", "3", "8"):
+            monkeypatch.setenv("SSG_PLAN_THREADS", nt)
+            plans.append(plan(planlib, tri, 16, 8))
+        assert plans[0]["ok"]
+        for P in plans[1:]:
+            assert all(np.array_equal(P[k], plans[0][k]) for k in keys)
+            assert all(P[k] == plans[0][k] for k in LAYOUT + ["nent", "npush", "cnt_max"])
