@@ -189,11 +189,21 @@ PushPlanHost push_plan_host(int n, int nlev, const int *lptr, const int *prp, co
     for (int q = 0; q < nt; ++q)
         if (bad_why[q]) return fail(bad_why[q] == 1 ? "an entry is not a dependency of its row"
                                                     : "a row longer than 65535 entries");
-    for (int t = 0; t < n; ++t)
-        for (int k = sprp[t] + nsp[t]; k < sprp[t + 1]; ++k) {
-            P.dnew.push_back(k);
-            P.dnew.push_back(t);
-        }
+    {
+        // (entry, row) of the newest entries, in row order: each row's place from a prefix sum
+        std::vector<long long> nwp((size_t)n + 1, 0);
+        for (int t = 0; t < n; ++t) nwp[t + 1] = nwp[t] + (sprp[t + 1] - sprp[t] - nsp[t]);
+        P.dnew.assign((size_t)(2 * nwp[n]), 0);
+        par_for(n, nt, [&](int b, int e) {
+            for (int t = b; t < e; ++t) {
+                size_t o = (size_t)(2 * nwp[t]);
+                for (int k = sprp[t] + nsp[t]; k < sprp[t + 1]; ++k) {
+                    P.dnew[o++] = k;
+                    P.dnew[o++] = t;
+                }
+            }
+        });
+    }
     const int nent = (int)vmap.size();
     // codes; reads through the receive ring collected per consumer
     std::vector<int> code(nent, 0);
@@ -303,7 +313,8 @@ PushPlanHost push_plan_host(int n, int nlev, const int *lptr, const int *prp, co
         }
     // the layouts, largest rings and most staged records first: the ring sizes decide
     // which own entries stay in shared memory, the space left decides the receive ring
-    const std::vector<int> code0 = code;  // the entries read from memory (the others are set per layout)
+    // every attempt rewrites the code of each own-CTA entry (own ring or memory) and each
+    // receive-ring entry; the entries read from memory across CTAs keep the code set above
     auto attempt = [&](int S_own, int NB) -> const char * {
         if (2 * cap_r > S_own) return "own ring smaller than two levels";
         PushLayout lay = push_layout(S_own, 0, cap_rec, elem, NB);
@@ -315,7 +326,6 @@ PushPlanHost push_plan_host(int n, int nlev, const int *lptr, const int *prp, co
         if (lay.total > PS_SMEM_MAX) return ("layout exceeds shared memory");
         // own entries: the own ring while their slot is not reused before the end of the
         // reading row's level, else the output vector (never a newest entry)
-        code = code0;
         std::vector<char> left_ring(nt, 0);
         {
             const int part = (n + nt - 1) / nt;
@@ -353,7 +363,9 @@ PushPlanHost push_plan_host(int n, int nlev, const int *lptr, const int *prp, co
                 }
             }
         }
-        for (size_t q = 0; q < reqs.size(); ++q) code[reqs[q].entry] = -1 - (S_own + slot[pushof[q]]);
+        par_for((int)reqs.size(), nt, [&](int b, int e) {
+            for (int q = b; q < e; ++q) code[reqs[q].entry] = -1 - (S_own + slot[pushof[q]]);
+        });
         std::vector<int> plist(pushes.size());
         {
             std::vector<int> fillp(pptr.begin(), pptr.end() - 1);
