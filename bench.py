@@ -525,23 +525,41 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
         return
     if ws == 1:
-        line["new_pattern"] = new_pattern_solve(local, meth, pt, rp, ci, val, b1)
+        # the measurements beside the headline: a failure in one is recorded in its place
+        # (and on stderr) and never costs the line
+        def aux(key, fn):
+            try:
+                line[key] = fn()
+            except Exception as e:
+                print("bench: %s failed: %r" % (key, e), file=sys.stderr, flush=True)
+                line[key] = {"error": "%s: %s" % (type(e).__name__, e)}
+
+        aux("new_pattern", lambda: new_pattern_solve(local, meth, pt, rp, ci, val, b1))
         if K == 1 and args.workload in WORKLOAD_CASE:
-            line["assembly"] = device_assembly(local, args.workload, rp, ci, val, b1)
+            aux("assembly", lambda: device_assembly(local, args.workload, rp, ci, val, b1))
         ref = None
         if not args.no_cpu_baseline:
-            ref = cpu_baseline(line, rp, ci, val, b1, args.method, pt, args.cpu_threads)
-            line["parity"] = parity_summary(rp, ci, val, b1, xs[0], iters if K == 1 else iters[0], gpu_log, ref)
+            try:
+                ref = cpu_baseline(line, rp, ci, val, b1, args.method, pt, args.cpu_threads)
+            except Exception as e:
+                print("bench: cpu_baseline failed: %r" % (e,), file=sys.stderr, flush=True)
+                line["cpu_baseline"] = {"error": "%s: %s" % (type(e).__name__, e)}
+            if ref is not None:
+                aux("parity", lambda: parity_summary(rp, ci, val, b1, xs[0], iters if K == 1 else iters[0], gpu_log,
+                                                     ref))
         if not args.no_mixed and K == 1 and args.method != "sgs" and args.precision == "fp64":
-            line["mixed"] = mixed_vs_fp64(h, o, step_device, stream, dev, x_d, args, ms_max / args.steps,
-                                          rp, ci, val, b1, xs[0], ref)
+            aux("mixed", lambda: mixed_vs_fp64(h, o, step_device, stream, dev, x_d, args, ms_max / args.steps,
+                                               rp, ci, val, b1, xs[0], ref))
         if not args.no_serving and args.workload == "cfg2" and K == 1:
-            line["serving"] = serving_measure(local, args.requests, args.slots, args.share, None, warm_runs=1,
-                                              sweep=False)
+            aux("serving", lambda: serving_measure(local, args.requests, args.slots, args.share, None, warm_runs=1,
+                                                   sweep=False))
         if not args.no_batch and args.workload == "cfg2" and K == 1:
-            line["batch"] = batch_measure(local, args.batch_sizes, args.batch_persistent)
-    h.close()
+            aux("batch", lambda: batch_measure(local, args.batch_sizes, args.batch_persistent))
     print(json.dumps(line), flush=True)
+    try:
+        h.close()
+    except Exception as e:
+        print("bench: closing the handle failed: %r" % (e,), file=sys.stderr, flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
 
