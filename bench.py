@@ -63,6 +63,12 @@ NCU_TRAFFIC = {
     ("cfg2", "fp64", "cluster", "backward sweep"): 347.6e6,
     ("cfg2", "fp64", "sync-free", "forward sweep"): 360.6e6,
 }
+# the same captures' FP64 pipe (sm__inst_executed_pipe_fp64, % of peak sustained on the active SMs, averaged over
+# all 152): the push sweep runs level by level on one 16-SM cluster, bound by FP64 latency and issue on those SMs
+NCU_FP64_PIPE = {
+    ("cfg2", "fp64", "push", "forward sweep"): 0.237,
+    ("cfg2", "fp64", "push", "backward sweep"): 0.245,
+}
 
 
 def sweep_kind(mode, cplx):
@@ -516,7 +522,11 @@ def run_ours(args):
                      "traffic": None if K > 1 else NCU_TRAFFIC.get((args.workload, args.precision, sweep_kind(
                          tuned["mode"] if tuned else args.sweep_mode, np.iscomplexobj(val)), dom)),
                      "traffic_source": "ncu capture in profiles/ (per launch)", "algorithmic_bytes": dbytes / max(dlaunch, 1),
-                     "launch_ms": dms / max(dlaunch, 1), "launches": dlaunch},
+                     "launch_ms": dms / max(dlaunch, 1), "launches": dlaunch,
+                     "fp64_pipe_frac": None if K > 1 else NCU_FP64_PIPE.get((args.workload, args.precision, sweep_kind(
+                         tuned["mode"] if tuned else args.sweep_mode, np.iscomplexobj(val)), dom)),
+                     "limit": "dependency levels swept one after another on one 16-SM cluster (about 1,400 at 80^3): "
+                              "FP64 latency and issue on those SMs and cross-SM latency, not HBM bandwidth"},
         "kernel_ms_per_step": {k: v[0] / args.steps for k, v in stats.items()},
         "clocks": clk, "host_s": t_host,
     }
